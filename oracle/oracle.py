@@ -1,0 +1,224 @@
+"""ctypes wrapper of the CPU oracle (test infrastructure only).
+
+Imported by tests/, ``__graft_entry__.smoke()`` and bench.py's cpu_baseline leg
+as the checker. The product package never imports this module.
+
+Arrays follow the reference's Fortran layout with the level/component index
+fastest; numpy arrays are returned with shape ``(outer, inner)`` in C order,
+i.e. ``a[node, level]`` for an ``(nl-1, nod2D)`` Fortran array.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libfesom_oracle.so")
+
+HOR = {"UPW1": 0, "MUSCL": 1, "MFCT": 2}
+VER = {"UPW1": 0, "QR4C": 1, "CDIFF": 2, "PPM": 3}
+LIM = {"NONE": 0, "FCT": 1}
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+
+def build() -> str:
+    """Compile the oracle with its Makefile (idempotent)."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        L = ctypes.CDLL(_LIB_PATH)
+        L.om_mesh_analytic.restype = ctypes.c_void_p
+        L.om_mesh_analytic.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                       ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                       _dp, _ip]
+        L.om_mesh_free.argtypes = [ctypes.c_void_p]
+        L.om_mesh_sizes.argtypes = [ctypes.c_void_p, _ip]
+        L.om_mesh_get_int.restype = ctypes.c_long
+        L.om_mesh_get_int.argtypes = [ctypes.c_void_p, ctypes.c_char_p, _ip]
+        L.om_mesh_get_dbl.restype = ctypes.c_long
+        L.om_mesh_get_dbl.argtypes = [ctypes.c_void_p, ctypes.c_char_p, _dp]
+        L.om_work_new.restype = ctypes.c_void_p
+        L.om_work_new.argtypes = [ctypes.c_void_p]
+        L.om_work_free.argtypes = [ctypes.c_void_p]
+        L.om_work_get.restype = ctypes.c_long
+        L.om_work_get.argtypes = [ctypes.c_void_p, ctypes.c_char_p, _dp]
+        L.om_do_oce_adv_tra.restype = ctypes.c_int
+        L.om_do_oce_adv_tra.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, _dp, _dp, _dp,
+                                        _dp, _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_int, _dp, _dp]
+        L.om_analytic_step.restype = ctypes.c_int
+        L.om_analytic_step.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_double,
+                                       _dp, _dp, _dp, _dp, _ip, _ip, _ip, _dp, _dp, ctypes.c_int, _dp]
+        L.om_cabi_step.restype = ctypes.c_int
+        L.om_cabi_step.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, _dp, _dp, _dp, _dp,
+                                   _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                   ctypes.c_double, _dp]
+        L.om_init_dwarf_fields.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, _dp, _dp]
+        L.om_stats.argtypes = [ctypes.c_void_p, _dp, _dp]
+        _lib = L
+    return _lib
+
+
+def _p(a, t=_dp):
+    return a.ctypes.data_as(t) if a is not None else None
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Mesh:
+    """An analytic mesh built by the oracle (lib/analytic_mesh.F90)."""
+
+    def __init__(self, nx, ny, nl, Lx=100000.0, Ly=100000.0, depth=1000.0, periodic=True,
+                 cluster_full=False, zbar=None, elem_nlev=None):
+        L = lib()
+        zb = _f64(zbar) if zbar is not None else None
+        en = np.ascontiguousarray(elem_nlev, dtype=np.int32) if elem_nlev is not None else None
+        self._zb, self._en = zb, en
+        h = L.om_mesh_analytic(nx, ny, nl, Lx, Ly, depth, int(periodic), int(cluster_full),
+                               _p(zb), _p(en, _ip))
+        if not h:
+            raise ValueError("invalid analytic mesh parameters")
+        self.h = ctypes.c_void_p(h)
+        s = np.zeros(7, np.int32)
+        L.om_mesh_sizes(self.h, _p(s, _ip))
+        (self.nod2D, self.nod2D_total, self.elem2D, self.edge2D, self.edge2D_in, self.nl,
+         self.max_nie) = (int(v) for v in s)
+        self.Lx, self.Ly, self.periodic = Lx, Ly, periodic
+
+    def __del__(self):
+        if getattr(self, "h", None) is not None and _lib is not None:
+            _lib.om_mesh_free(self.h)
+            self.h = None
+
+    _INT_SHAPES = {"elem2D_nodes": 3, "edges": 2, "edge_tri": 2, "edge_up_dn_tri": 2}
+    _DBL_SHAPES = {"coord": 2, "edge_dxdy": 2, "edge_cross_dxdy": 4, "gradient_sca": 6}
+
+    def geti(self, name):
+        L = lib()
+        n = L.om_mesh_get_int(self.h, name.encode(), None)
+        if n < 0:
+            raise KeyError(name)
+        out = np.zeros(n, np.int32)
+        L.om_mesh_get_int(self.h, name.encode(), _p(out, _ip))
+        if name in self._INT_SHAPES:
+            out = out.reshape(-1, self._INT_SHAPES[name])
+        elif name == "nod_in_elem2D":
+            out = out.reshape(-1, self.max_nie)
+        return out
+
+    def getd(self, name):
+        L = lib()
+        n = L.om_mesh_get_dbl(self.h, name.encode(), None)
+        if n < 0:
+            raise KeyError(name)
+        out = np.zeros(n, np.float64)
+        L.om_mesh_get_dbl(self.h, name.encode(), _p(out))
+        if name in self._DBL_SHAPES:
+            out = out.reshape(-1, self._DBL_SHAPES[name])
+        elif name in ("area", "areasvol", "zbar_3d_n"):
+            out = out.reshape(-1, self.nl)
+        elif name in ("hnode", "hnode_new", "helem", "Z_3d_n"):
+            out = out.reshape(-1, self.nl - 1)
+        return out
+
+    def dwarf_fields(self):
+        nz = self.nl - 1
+        T = np.zeros((self.nod2D, nz))
+        S = np.zeros((self.nod2D, nz))
+        lib().om_init_dwarf_fields(self.h, self.Lx, self.Ly, _p(T), _p(S))
+        return T, S
+
+    def stats(self, values):
+        out = np.zeros(4)
+        lib().om_stats(self.h, _p(_f64(values)), _p(out))
+        return out
+
+
+class Work:
+    def __init__(self, mesh: Mesh):
+        self.mesh = mesh
+        self.h = ctypes.c_void_p(lib().om_work_new(mesh.h))
+
+    def __del__(self):
+        if getattr(self, "h", None) is not None and _lib is not None:
+            _lib.om_work_free(self.h)
+            self.h = None
+
+    def get(self, name):
+        L = lib()
+        n = L.om_work_get(self.h, name.encode(), None)
+        if n < 0:
+            raise KeyError(name)
+        out = np.zeros(n)
+        L.om_work_get(self.h, name.encode(), _p(out))
+        m = self.mesh
+        if name in ("adv_flux_ver", "adf_v_raw"):
+            return out.reshape(m.nod2D, m.nl)
+        if name in ("adv_flux_hor", "adf_h_raw"):
+            return out.reshape(m.edge2D, m.nl - 1)
+        if name == "edge_up_dn_grad":
+            return out.reshape(m.edge2D, m.nl - 1, 4)
+        if name == "tr_xy":
+            return out.reshape(m.elem2D, m.nl - 1, 2)
+        return out.reshape(m.nod2D, m.nl - 1)
+
+
+def do_oce_adv_tra(mesh, work, dt, vel, w, ttf, ttfAB, hor="UPW1", ver="UPW1", lim="NONE",
+                   ph=1.0, pv=1.0, wi=None, we=None):
+    """One call of do_oce_adv_tra; returns (dttf_h, dttf_v) as (nod2D, nl-1)."""
+    vel, w, ttf, ttfAB = _f64(vel), _f64(w), _f64(ttf), _f64(ttfAB)
+    wi = w if wi is None else _f64(wi)
+    we = w if we is None else _f64(we)
+    dh = np.zeros((mesh.nod2D, mesh.nl - 1))
+    dv = np.zeros_like(dh)
+    rc = lib().om_do_oce_adv_tra(mesh.h, work.h, dt, _p(vel), _p(w), _p(wi), _p(we), _p(ttf), _p(ttfAB),
+                                 HOR[hor], VER[ver], LIM[lim], ph, pv, 0, _p(dh), _p(dv))
+    if rc != 0:
+        raise RuntimeError(f"om_do_oce_adv_tra failed: {rc}")
+    return dh, dv
+
+
+def analytic_step(mesh, work, dt, vel, w, values, valuesAB, schemes, copy_ab=False):
+    """One driver step for all tracers, in place. schemes: list of (hor, ver, lim[, ph, pv])."""
+    ntr = len(schemes)
+    assert values.flags.c_contiguous and values.dtype == np.float64
+    assert valuesAB.flags.c_contiguous and valuesAB.dtype == np.float64
+    vel, w = _f64(vel), _f64(w)
+    hor = np.array([HOR[s[0]] for s in schemes], np.int32)
+    ver = np.array([VER[s[1]] for s in schemes], np.int32)
+    lim = np.array([LIM[s[2]] for s in schemes], np.int32)
+    ph = np.array([s[3] if len(s) > 3 else 1.0 for s in schemes])
+    pv = np.array([s[4] if len(s) > 4 else 1.0 for s in schemes])
+    del_ttf = np.zeros((mesh.nod2D, mesh.nl - 1))
+    rc = lib().om_analytic_step(mesh.h, work.h, ntr, dt, _p(vel), _p(w), _p(values), _p(valuesAB),
+                                _p(hor, _ip), _p(ver, _ip), _p(lim, _ip), _p(ph), _p(pv), int(copy_ab),
+                                _p(del_ttf))
+    if rc != 0:
+        raise RuntimeError(f"om_analytic_step failed: {rc}")
+
+
+def cabi_step(mesh, work, dt, vel, w, values, valuesAB, del_ttf, hor="UPW1", ver="UPW1", lim="NONE",
+              ph=1.0, pv=1.0, wi=None, we=None):
+    vel, w = _f64(vel), _f64(w)
+    wi = np.zeros_like(w) if wi is None else _f64(wi)
+    we = np.zeros_like(w) if we is None else _f64(we)
+    rc = lib().om_cabi_step(mesh.h, work.h, dt, _p(vel), _p(w), _p(wi), _p(we), _p(values), _p(valuesAB),
+                            HOR[hor], VER[ver], LIM[lim], ph, pv, _p(del_ttf))
+    if rc != 0:
+        raise RuntimeError(f"om_cabi_step failed: {rc}")
