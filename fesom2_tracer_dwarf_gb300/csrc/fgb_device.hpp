@@ -1,0 +1,74 @@
+// Device-resident mesh and per-launch pointer bundles of the tracer step.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+namespace fgb {
+
+// Geometry in the storage precision of a form (FP64 and FP32 copies).
+template <typename R>
+struct GeoPtrs {
+  const R* hnode;       // (N,LZ)
+  const R* hnode_new;   // (N,LZ)
+  const R* areasvol;    // (N,LZ) layer areas
+  const R* area;        // (N,LW) interface areas
+  const R* Z3;          // (N,LZ) Z_3d_n
+  const R* zbar3;       // (N,LW) zbar_3d_n
+  const R* helem;       // (M,LZ)
+  const R* edge_cross;  // (E,4)
+  const R* edge_dxa;    // (E,2)
+  const R* grad_sca;    // (M,6)
+  const R* elem_area;   // (M)
+};
+
+// Everything the kernels read about the mesh; passed by value to kernels.
+struct DMesh {
+  int N, E, M, nl, nz, LZ, LW;
+  int min_layers;        // fewest layers in any node column
+  const int* nlev;       // (N) nlevels_nod2D
+  const int* ulev;       // (N) ulevels_nod2D
+  const int* nbl;        // (N) nboundary_lay
+  const int* ne_ptr;     // (N+1) incident edges, ascending edge index
+  const int* ne_code;    // 2*edge + role
+  const int* ne_other;   // other endpoint
+  const int* ne_lo;      // first layer of that edge's scatter range
+  const int* ne_hi;      // last layer of that edge's scatter range
+  const int* cl_ptr;     // (N+1) FCT cluster
+  const int* cl_node;
+  const int* cl_lev;
+  const int* cl_minlev;  // (N)
+  const int* nie_ptr;    // (N+1) nod_in_elem2D
+  const int* nie_idx;
+  const int* elem_nodes;  // (M,3)
+  const int* elem_nlev;   // (M)
+  const int* edge_nodes;  // (E,2)
+  const int* edge_tri;    // (E,2)
+  const int* edge_updn;   // (E,2)
+  const int* edge_lev;    // (E,4)
+  const int* edge_gm;     // (E,2)
+  GeoPtrs<double> g64;
+  GeoPtrs<float> g32;
+};
+
+// Per-launch field pointers. Tracer t of a batch lives at base + t*stride.
+template <typename R>
+struct StepPtrs {
+  R* T;             // (K,N,LZ) tracer values, updated in place
+  const R* TA;      // (K,N,LZ) values used for the high-order fluxes (valuesAB)
+  R* TAout;         // optional: written with the new values (copy-AB)
+  const R* vel;     // (M,LZ,2) horizontal velocity on elements
+  const R* w;       // (N,LW) vertical velocity used by the high-order flux under FCT
+  const R* we;      // (N,LW) explicit vertical velocity
+  R* vf;            // (E,LZ) volume flux through the edge segments
+  R* flo;           // (K,E,LZ) low-order horizontal flux
+  R* adfh;          // (K,E,LZ) antidiffusive (FCT) or high-order horizontal flux
+  R* lo;            // (K,N,LZ) low-order solution fct_LO
+  R* adfv;          // (K,N,LW) antidiffusive vertical flux
+  R* rp;            // (K,N,LZ) fct_plus limiting factor
+  R* rm;            // (K,N,LZ) fct_minus limiting factor
+  R* del;           // optional (K,N,LZ) persistent del_ttf
+  long long sT, sTA, sE, sN, sW;  // strides between tracers (elements)
+  R dt, ph, pv;
+};
+
+}  // namespace fgb

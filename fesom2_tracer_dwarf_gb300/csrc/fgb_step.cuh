@@ -1,0 +1,146 @@
+// Launch sequence of one tracer-advection step for a batch of tracers
+// (do_oce_adv_tra, lib/oce_adv_tra_driver.F90:23-294, plus the caller's
+// tendency update). Included by one translation unit per precision.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "fesom_tracer_gb300.h"
+#include "fgb_internal.hpp"
+#include "fgb_kernels.cuh"
+
+namespace fgb {
+
+constexpr int kEdgeWarps = 8;  // edges per 256-thread block
+constexpr int kNodeWarps = 4;  // node columns per 128-thread block
+
+template <typename R>
+WorkspaceLayout workspace_layout(const DMesh& m, int K) {
+  WorkspaceLayout w;
+  const long long E = m.E, N = m.N, LZ = m.LZ, LW = m.LW, s = sizeof(R);
+  auto al = [](long long b) { return (b + 255) / 256 * 256; };
+  long long off = 0;
+  w.off[0] = off; off += al(E * LZ * s);          // vf
+  w.off[1] = off; off += al((long long)K * E * LZ * s);  // flo
+  w.off[2] = off; off += al((long long)K * E * LZ * s);  // adfh
+  w.off[3] = off; off += al((long long)K * N * LZ * s);  // lo
+  w.off[4] = off; off += al((long long)K * N * LW * s);  // adfv
+  w.off[5] = off; off += al((long long)K * N * LZ * s);  // rp
+  w.off[6] = off; off += al((long long)K * N * LZ * s);  // rm
+  w.total = off;
+  return w;
+}
+
+template <typename R, int HOR>
+void launch_hflux(const DMesh& m, const StepPtrs<R>& a, bool fct, int K, cudaStream_t s) {
+  dim3 grid((m.E + kEdgeWarps - 1) / kEdgeWarps, K), block(kEdgeWarps * kWarp);
+  if (fct) k_hflux<R, HOR, true><<<grid, block, 0, s>>>(m, a);
+  else k_hflux<R, HOR, false><<<grid, block, 0, s>>>(m, a);
+}
+
+template <typename R, int VER>
+void launch_lo(const DMesh& m, const StepPtrs<R>& a, int K, cudaStream_t s) {
+  dim3 grid((m.N + kNodeWarps - 1) / kNodeWarps, K), block(kNodeWarps * kWarp);
+  size_t sm = (size_t)kNodeWarps * 10 * m.LW * sizeof(R);
+  k_fct_lo<R, VER><<<grid, block, sm, s>>>(m, a);
+}
+
+template <typename R, int VER>
+void launch_nofct(const DMesh& m, const StepPtrs<R>& a, int K, cudaStream_t s) {
+  dim3 grid((m.N + kNodeWarps - 1) / kNodeWarps, K), block(kNodeWarps * kWarp);
+  size_t sm = (size_t)kNodeWarps * 10 * m.LW * sizeof(R);
+  k_nofct_update<R, VER><<<grid, block, sm, s>>>(m, a);
+}
+
+template <typename R>
+int launch_stages(const DMesh& m, const fgb_step_desc& d, int mask, cudaStream_t s, int* nlaunch,
+                  std::string* err) {
+  const int K = d.ntracers;
+  if (K < 1 || K > 65535) { *err = "ntracers must be in 1..65535"; return -1; }
+  if (d.hor < 0 || d.hor > 2 || d.ver < 0 || d.ver > 3 || d.lim < 0 || d.lim > 1) {
+    *err = "unknown advection scheme";
+    return -1;
+  }
+  if (!d.T || !d.vel || !d.w || !d.we || !d.workspace) { *err = "null device pointer"; return -1; }
+  const WorkspaceLayout wl = workspace_layout<R>(m, K);
+  if (d.workspace_bytes < wl.total) { *err = "workspace too small"; return -1; }
+  if ((d.ver == FGB_VER_QR4C || d.ver == FGB_VER_PPM) && m.min_layers < 2) {
+    *err = "QR4C/PPM need at least two layers in every column";
+    return -1;
+  }
+  char* ws = static_cast<char*>(d.workspace);
+  StepPtrs<R> a;
+  a.T = static_cast<R*>(d.T);
+  a.TA = d.TA ? static_cast<const R*>(d.TA) : a.T;
+  a.TAout = static_cast<R*>(d.TAout);
+  a.vel = static_cast<const R*>(d.vel);
+  a.w = static_cast<const R*>(d.w);
+  a.we = static_cast<const R*>(d.we);
+  a.vf = reinterpret_cast<R*>(ws + wl.off[0]);
+  a.flo = reinterpret_cast<R*>(ws + wl.off[1]);
+  a.adfh = reinterpret_cast<R*>(ws + wl.off[2]);
+  a.lo = reinterpret_cast<R*>(ws + wl.off[3]);
+  a.adfv = reinterpret_cast<R*>(ws + wl.off[4]);
+  a.rp = reinterpret_cast<R*>(ws + wl.off[5]);
+  a.rm = reinterpret_cast<R*>(ws + wl.off[6]);
+  a.del = static_cast<R*>(d.del);
+  a.sT = d.strideT;
+  a.sTA = d.TA ? d.strideTA : d.strideT;
+  a.sE = (long long)m.E * m.LZ;
+  a.sN = (long long)m.N * m.LZ;
+  a.sW = (long long)m.N * m.LW;
+  a.dt = (R)d.dt;
+  a.ph = (R)d.ph;
+  a.pv = (R)d.pv;
+  const bool fct = d.lim == FGB_LIM_FCT;
+  int launches = 0;
+  if (mask & FGB_STAGE_VFLUX) {
+    dim3 grid((m.E + kEdgeWarps - 1) / kEdgeWarps), block(kEdgeWarps * kWarp);
+    k_vflux<R><<<grid, block, 0, s>>>(m, a.vel, a.vf);
+    ++launches;
+  }
+  if (mask & FGB_STAGE_HFLUX) {
+    if (d.hor == FGB_HOR_UPW1) launch_hflux<R, 0>(m, a, fct, K, s);
+    else if (d.hor == FGB_HOR_MUSCL) launch_hflux<R, 1>(m, a, fct, K, s);
+    else launch_hflux<R, 2>(m, a, fct, K, s);
+    ++launches;
+  }
+  dim3 ngrid((m.N + kNodeWarps - 1) / kNodeWarps, K), nblock(kNodeWarps * kWarp);
+  if (fct) {
+    if (mask & FGB_STAGE_LO) {
+      switch (d.ver) {
+        case FGB_VER_QR4C: launch_lo<R, 1>(m, a, K, s); break;
+        case FGB_VER_CDIFF: launch_lo<R, 2>(m, a, K, s); break;
+        case FGB_VER_PPM: launch_lo<R, 3>(m, a, K, s); break;
+        default: launch_lo<R, 0>(m, a, K, s); break;
+      }
+      ++launches;
+    }
+    if (mask & FGB_STAGE_RATIO) {
+      k_fct_ratio<R><<<ngrid, nblock, (size_t)kNodeWarps * 3 * m.LW * sizeof(R), s>>>(m, a);
+      ++launches;
+    }
+    if (mask & FGB_STAGE_UPDATE) {
+      k_fct_update<R><<<ngrid, nblock, (size_t)kNodeWarps * 3 * m.LW * sizeof(R), s>>>(m, a);
+      ++launches;
+    }
+  } else if (mask & FGB_STAGE_UPDATE) {
+    switch (d.ver) {
+      case FGB_VER_QR4C: launch_nofct<R, 1>(m, a, K, s); break;
+      case FGB_VER_CDIFF: launch_nofct<R, 2>(m, a, K, s); break;
+      case FGB_VER_PPM: launch_nofct<R, 3>(m, a, K, s); break;
+      default: launch_nofct<R, 0>(m, a, K, s); break;
+    }
+    ++launches;
+  }
+  *nlaunch = launches;
+  cudaError_t ce = cudaGetLastError();
+  if (ce != cudaSuccess) {
+    *err = std::string("kernel launch failed: ") + cudaGetErrorString(ce);
+    return -1;
+  }
+  return 0;
+}
+
+}  // namespace fgb

@@ -1,0 +1,150 @@
+"""GPU engine of the tracer-advection step: device fields as torch tensors,
+kernels launched through the C-ABI on torch's current CUDA stream.
+
+``TracerAdvection`` advances K tracers of one mesh with do_oce_adv_tra
+(lib/oce_adv_tra_driver.F90:23-294) followed by the analytic driver's
+tendency update (src/fesom_analytic.F90:404-437). Tracer values live in a
+(K, N, LZ) tensor (level index fastest, padded to LZ layers).
+
+valuesAB (the field the high-order fluxes read) is either frozen at the
+values given to ``set_tracers`` -- the analytic dwarf, src/fesom_analytic.F90:335
+-- or follows the values (``copy_ab=True``).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .mesh import Mesh
+
+_DT = {"fp64": torch.float64, "fp32": torch.float32}
+_PREC = {"fp64": _lib.FP64, "fp32": _lib.FP32}
+
+
+def _require_cuda():
+    if not torch.cuda.is_available():
+        raise RuntimeError("fesom2_tracer_dwarf_gb300 needs a CUDA GPU; there is no CPU path")
+
+
+class TracerAdvection:
+    def __init__(self, mesh: Mesh, ntracers: int, precision: str = "fp64", hor: str = "UPW1",
+                 ver: str = "UPW1", lim: str = "NONE", ph: float = 1.0, pv: float = 1.0,
+                 copy_ab: bool = False, device: str = "cuda"):
+        _require_cuda()
+        if precision not in _DT:
+            raise ValueError(f"precision must be one of {list(_DT)}")
+        self.mesh, self.K, self.precision = mesh, int(ntracers), precision
+        self.dtype = _DT[precision]
+        self.device = torch.device(device)
+        self.set_schemes(hor, ver, lim, ph, pv)
+        self.copy_ab = copy_ab
+        m = mesh
+        m.upload()
+        z = lambda *s: torch.zeros(*s, dtype=self.dtype, device=self.device)
+        self.T = z(self.K, m.N, m.LZ)
+        self.TA = None if copy_ab else z(self.K, m.N, m.LZ)
+        self.vel = z(m.M, m.LZ, 2)
+        self.w = z(m.N, m.LW)
+        self.we = self.w
+        L = _lib.load()
+        nbytes = L.fgb_workspace_bytes(m.handle, _PREC[precision], self.K)
+        if nbytes < 0:
+            raise RuntimeError(_lib.last_error())
+        self.workspace = torch.zeros(int(nbytes), dtype=torch.uint8, device=self.device)
+        self._stats_scratch = torch.zeros(int(L.fgb_stats_scratch_bytes(m.handle, self.K)), dtype=torch.uint8,
+                                          device=self.device)
+        self._stats_out = torch.zeros(self.K, 4, dtype=torch.float64, device=self.device)
+        self.launches = 0
+
+    # ---- configuration -----------------------------------------------------
+    def set_schemes(self, hor="UPW1", ver="UPW1", lim="NONE", ph=1.0, pv=1.0):
+        for name, table, v in (("hor", _lib.HOR, hor), ("ver", _lib.VER, ver), ("lim", _lib.LIM, lim)):
+            if v not in table:
+                raise ValueError(f"unknown {name} scheme {v!r}")
+        self.hor, self.ver, self.lim, self.ph, self.pv = hor, ver, lim, float(ph), float(pv)
+
+    def _pad_nodes(self, a, width, ld):
+        t = torch.as_tensor(np.asarray(a), dtype=self.dtype) if not torch.is_tensor(a) else a.to(self.dtype)
+        out = torch.zeros(*t.shape[:-1], ld, dtype=self.dtype)
+        out[..., :width] = t.cpu()
+        return out.to(self.device)
+
+    def set_tracers(self, values, values_ab=None):
+        """values: (K, N, nz) array. values_ab defaults to values."""
+        m = self.mesh
+        v = self._pad_nodes(values, m.nz, m.LZ).reshape(self.K, m.N, m.LZ)
+        self.T.copy_(v)
+        if self.TA is not None:
+            self.TA.copy_(v if values_ab is None else self._pad_nodes(values_ab, m.nz, m.LZ).reshape(self.K, m.N, m.LZ))
+
+    def set_velocity(self, vel, w, we=None):
+        """vel: (M, nz, 2) on elements; w, we: (N, nl) at node interfaces."""
+        m = self.mesh
+        v = torch.zeros(m.M, m.LZ, 2, dtype=self.dtype)
+        v[:, : m.nz, :] = torch.as_tensor(np.asarray(vel) if not torch.is_tensor(vel) else vel.cpu(), dtype=self.dtype)
+        self.vel.copy_(v.to(self.device))
+        self.w.copy_(self._pad_nodes(w, m.nl, m.LW))
+        if we is None:
+            self.we = self.w
+        else:
+            self.we = self._pad_nodes(we, m.nl, m.LW)
+
+    # ---- step --------------------------------------------------------------
+    def _desc(self, dt):
+        d = _lib.StepDesc()
+        d.precision = _PREC[self.precision]
+        d.ntracers = self.K
+        d.hor, d.ver, d.lim = _lib.HOR[self.hor], _lib.VER[self.ver], _lib.LIM[self.lim]
+        d.ph, d.pv, d.dt = self.ph, self.pv, float(dt)
+        m = self.mesh
+        d.T = self.T.data_ptr()
+        d.strideT = m.N * m.LZ
+        d.TA = None if self.TA is None else self.TA.data_ptr()
+        d.strideTA = m.N * m.LZ
+        d.TAout = None
+        d.vel, d.w, d.we = self.vel.data_ptr(), self.w.data_ptr(), self.we.data_ptr()
+        d.del_ = None
+        d.workspace = self.workspace.data_ptr()
+        d.workspace_bytes = self.workspace.numel()
+        return d
+
+    def step(self, dt: float, nsteps: int = 1, stages: int = _lib.STAGE_ALL):
+        L = _lib.load()
+        d = self._desc(dt)
+        stream = ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+        for _ in range(nsteps):
+            _lib.check(L.fgb_adv_stages(self.mesh.handle, ctypes.byref(d), stages, stream), "fgb_adv_stages")
+            self.launches += L.fgb_last_launch_count()
+
+    # ---- outputs -----------------------------------------------------------
+    def values(self) -> np.ndarray:
+        m = self.mesh
+        return self.T[:, :, : m.nz].double().cpu().numpy()
+
+    def workspace_view(self, name: str):
+        """A view of one workspace array: vf, flo, adfh, lo, adfv, rp, rm."""
+        m = self.mesh
+        L = _lib.load()
+        offs = (ctypes.c_longlong * 7)()
+        _lib.check(L.fgb_workspace_offsets(m.handle, _PREC[self.precision], self.K, offs), "offsets")
+        names = ["vf", "flo", "adfh", "lo", "adfv", "rp", "rm"]
+        i = names.index(name)
+        shape = {"vf": (m.E, m.LZ), "flo": (self.K, m.E, m.LZ), "adfh": (self.K, m.E, m.LZ),
+                 "lo": (self.K, m.N, m.LZ), "adfv": (self.K, m.N, m.LW), "rp": (self.K, m.N, m.LZ),
+                 "rm": (self.K, m.N, m.LZ)}[name]
+        n = int(np.prod(shape))
+        es = self.T.element_size()
+        return self.workspace[offs[i]: offs[i] + n * es].view(self.dtype).view(shape)
+
+    def stats(self) -> np.ndarray:
+        """(K, 4): min, max, plain sum, NaN count over all layers of the owned nodes."""
+        L = _lib.load()
+        m = self.mesh
+        stream = ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+        _lib.check(L.fgb_tracer_stats(m.handle, _PREC[self.precision], ctypes.c_void_p(self.T.data_ptr()),
+                                      m.N * m.LZ, self.K, ctypes.c_void_p(self._stats_scratch.data_ptr()),
+                                      ctypes.c_void_p(self._stats_out.data_ptr()), stream), "fgb_tracer_stats")
+        return self._stats_out.cpu().numpy()

@@ -1,0 +1,211 @@
+"""Seeded synthetic inputs of the benchmark configurations.
+
+No dataset is involved in the reference's measurements; the configurations
+are analytic meshes with these fields:
+
+- the analytic dwarf (src/fesom_analytic.F90:251-331): u=(0.1,0), W=0;
+- streamfunction flows: a P1 streamfunction on nodes made of random-phase
+  Fourier modes, decaying with depth; horizontal velocity on elements is its
+  rotated element gradient (gradient_sca), scaled to a target horizontal CFL;
+  on ragged meshes the vertical profile is normalised per element so the
+  depth-integrated transport is non-divergent; W is diagnosed from the
+  discrete continuity of the upwind flux of a uniform tracer;
+- T: Gaussian blob of 20 on a background of 2 plus N(0, 0.1) noise;
+  S: 35 + N(0, 0.3); passive tracers: random Gaussian blobs in [0, 1].
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .mesh import Mesh
+
+R_EARTH = 6367500.0
+
+
+def stretched_zbar(nz: int, top: float = 5.0, bottom: float = 250.0) -> np.ndarray:
+    """Interface depths (0 at the surface, negative down) of nz layers whose
+    thicknesses grow geometrically from top to bottom metres."""
+    r = (bottom / top) ** (1.0 / (nz - 1)) if nz > 1 else 1.0
+    h = top * r ** np.arange(nz)
+    return np.concatenate([[0.0], -np.cumsum(h)])
+
+
+def dwarf_velocity(m: Mesh):
+    """u=(0.1, 0) m/s on every element, W=0 (src/fesom_analytic.F90:251-256)."""
+    vel = np.zeros((m.M, m.nz, 2))
+    vel[..., 0] = 0.1
+    return vel, np.zeros((m.N, m.nl))
+
+
+def node_xy(m: Mesh):
+    c = m.get("coord")
+    return c[:, 0] * R_EARTH, c[:, 1] * R_EARTH
+
+
+def random_field(m: Mesh, rng, K: int = 1) -> np.ndarray:
+    """Smooth random tracer values (K, N, nz) for parity tests."""
+    x, y = node_xy(m)
+    out = np.zeros((K, m.N, m.nz))
+    z = np.arange(m.nz) / max(m.nz - 1, 1)
+    for t in range(K):
+        a = rng.uniform(0.5, 2.0, 4)
+        ph = rng.uniform(0, 2 * np.pi, 4)
+        base = (a[0] * np.sin(2 * np.pi * x / m.Lx + ph[0]) * np.cos(2 * np.pi * y / m.Ly + ph[1])
+                + a[1] * np.sin(4 * np.pi * x / m.Lx + ph[2]))
+        out[t] = 10.0 + base[:, None] * (1.0 - 0.5 * z)[None, :] - 3.0 * z[None, :] + a[3] * np.cos(6 * z + ph[3])
+        out[t] += rng.normal(0, 0.2, size=(m.N, m.nz))
+    return out
+
+
+def random_flow(m: Mesh, rng, umax: float = 0.3, wmax: float = 2e-3):
+    """Random (non-solenoidal) horizontal and vertical velocities for parity
+    tests; W is zero at each column's bottom interface."""
+    vel = rng.uniform(-umax, umax, size=(m.M, m.nz, 2))
+    w = rng.uniform(-wmax, wmax, size=(m.N, m.nl))
+    nlev = m.get("nlevels_nod2D")
+    for n in range(m.N):
+        w[n, nlev[n] - 1:] = 0.0
+    return vel, w
+
+
+def _edge_vflux(m: Mesh, vel: np.ndarray) -> np.ndarray:
+    """Volume flux through each edge's two segments, (E, nz), as the upwind
+    flux of lib/oce_adv_tra_hor.F90:174-252 forms it."""
+    ed_tri = m.get("edge_tri")
+    cr = m.get("edge_cross_dxdy")
+    helem = m.get("helem")
+    lev = m.get("edge_lev")
+    z = np.arange(1, m.nz + 1)[None, :]
+    nu1, nl1, nu2, nl2 = (lev[:, i:i + 1] for i in range(4))
+    nl12, nu12 = np.minimum(nl1, nl2), np.maximum(nu1, nu2)
+    use1 = ((z >= nu1) & (z <= nu12 - 1)) | ((z >= nu12) & (z <= nl12)) | ((z > nl12) & (z <= nl1))
+    use2 = (((nu2 > 0) & (z >= nu2) & (z <= nu12 - 1)) | ((z >= nu12) & (z <= nl12)) | ((z > nl12) & (z <= nl2)))
+    e1 = ed_tri[:, 0]
+    e2 = np.where(ed_tri[:, 1] >= 0, ed_tri[:, 1], 0)
+    v1 = (-(vel[e1, :, 1] * cr[:, 0:1]) + vel[e1, :, 0] * cr[:, 1:2]) * helem[e1]
+    v2 = (vel[e2, :, 1] * cr[:, 2:3] - vel[e2, :, 0] * cr[:, 3:4]) * helem[e2]
+    return np.where(use1, v1, 0.0) + np.where(use2, v2, 0.0)
+
+
+def _node_divergence(m: Mesh, vf: np.ndarray) -> np.ndarray:
+    """Net inflow of a uniform tracer per node and layer, (N, nz)."""
+    edges = m.get("edges")
+    D = np.zeros((m.N, m.nz))
+    np.add.at(D, edges[:, 0], -vf)
+    np.add.at(D, edges[:, 1], vf)
+    return D
+
+
+def diagnose_w(m: Mesh, vel: np.ndarray) -> np.ndarray:
+    """Vertical velocity (N, nl) from the discrete continuity of a uniform
+    tracer: W(z) area(z) = D(z) + W(z+1) area(z+1), W = 0 at the bottom."""
+    D = _node_divergence(m, _edge_vflux(m, vel))
+    area = m.get("area")
+    nlev = m.get("nlevels_nod2D")
+    w = np.zeros((m.N, m.nl))
+    for k in range(m.nz - 1, -1, -1):
+        wet = k < nlev - 1
+        below = w[:, k + 1] * area[:, k + 1]
+        w[:, k] = np.where(wet, (D[:, k] + below) / np.where(area[:, k] > 0, area[:, k], 1.0), 0.0)
+    return w
+
+
+def max_cfl(m: Mesh, vel: np.ndarray, dt: float) -> float:
+    """max over nodes and layers of dt * (upwind outflow) / (areasvol * hnode)."""
+    vf = _edge_vflux(m, vel)
+    edges = m.get("edges")
+    out = np.zeros((m.N, m.nz))
+    np.add.at(out, edges[:, 0], np.maximum(vf, 0.0))
+    np.add.at(out, edges[:, 1], np.maximum(-vf, 0.0))
+    vol = m.get("areasvol")[:, : m.nz] * m.get("hnode")
+    nlev = m.get("nlevels_nod2D")
+    wet = np.arange(m.nz)[None, :] < (nlev - 1)[:, None]
+    return float(np.max(np.where(wet, dt * out / np.where(vol > 0, vol, 1.0), 0.0)))
+
+
+def streamfunction_flow(m: Mesh, rng, dt: float, cfl: float = 0.4, nmodes: int = 8, kmax: int = 8,
+                        efold: float = 500.0, psi_wall_zero: bool = False):
+    """Horizontal velocity (M, nz, 2) = rotated P1 gradient of a random-phase
+    Fourier streamfunction with a depth decay, scaled to the target CFL at dt,
+    and W (N, nl) diagnosed from continuity."""
+    x, y = node_xy(m)
+    psi = np.zeros(m.N)
+    for _ in range(nmodes):
+        kx, ky = rng.integers(1, kmax + 1, size=2)
+        ph = rng.uniform(0, 2 * np.pi)
+        psi += np.sin(2 * np.pi * (kx * x / m.Lx + ky * y / m.Ly) + ph) / np.hypot(kx, ky)
+    if psi_wall_zero and not m.periodic:
+        # closed basin: taper to zero on the walls
+        psi *= np.sin(np.pi * x / m.Lx) * np.sin(np.pi * y / m.Ly)
+    en = m.get("elem_nodes")
+    gs = m.get("gradient_sca")
+    dpx = (gs[:, 0:3] * psi[en]).sum(1)
+    dpy = (gs[:, 3:6] * psi[en]).sum(1)
+    zmid = 0.5 * (m.get("zbar_3d_n")[0, :-1] + m.get("zbar_3d_n")[0, 1:])
+    h = m.get("helem")
+    s = np.exp(zmid / efold)
+    nlevel = m.get("nlevels")
+    wet = np.arange(m.nz)[None, :] < (nlevel - 1)[:, None]
+    full = (s[None, :] * h).sum(1)
+    col = (np.where(wet, s[None, :] * h, 0.0)).sum(1)
+    prof = np.where(wet, s[None, :] * (full / col)[:, None], 0.0)
+    vel = np.zeros((m.M, m.nz, 2))
+    vel[..., 0] = -dpy[:, None] * prof
+    vel[..., 1] = dpx[:, None] * prof
+    c = max_cfl(m, vel, dt)
+    vel *= cfl / c
+    w = diagnose_w(m, vel)
+    return vel, w
+
+
+def gaussian_T(m: Mesh, rng) -> np.ndarray:
+    x, y = node_xy(m)
+    zmid = 0.5 * (m.get("zbar_3d_n")[0, :-1] + m.get("zbar_3d_n")[0, 1:])
+    H = -m.get("zbar_3d_n")[0, -1]
+    r2 = ((x - 0.5 * m.Lx) ** 2 + (y - 0.5 * m.Ly) ** 2) / (2 * (m.Lx / 8) ** 2)
+    zz = (zmid + 0.25 * H) ** 2 / (2 * (0.25 * H) ** 2)
+    return 2.0 + 20.0 * np.exp(-r2[:, None] - zz[None, :]) + rng.normal(0, 0.1, size=(m.N, m.nz))
+
+
+def salinity(m: Mesh, rng) -> np.ndarray:
+    return 35.0 + rng.normal(0, 0.3, size=(m.N, m.nz))
+
+
+def passive_blob(m: Mesh, rng) -> np.ndarray:
+    x, y = node_xy(m)
+    zmid = 0.5 * (m.get("zbar_3d_n")[0, :-1] + m.get("zbar_3d_n")[0, 1:])
+    H = -m.get("zbar_3d_n")[0, -1]
+    cx, cy = rng.uniform(0, m.Lx), rng.uniform(0, m.Ly)
+    sx, sy = rng.uniform(0.05, 0.2) * m.Lx, rng.uniform(0.05, 0.2) * m.Ly
+    cz, sz = -rng.uniform(0, H), rng.uniform(0.1, 0.5) * H
+    dx = np.abs(x - cx)
+    dy = np.abs(y - cy)
+    if m.periodic:
+        dx = np.minimum(dx, m.Lx - dx)
+        dy = np.minimum(dy, m.Ly - dy)
+    return np.exp(-(dx / sx) ** 2 - (dy / sy) ** 2)[:, None] * np.exp(-((zmid - cz) / sz) ** 2)[None, :]
+
+
+def bathymetry_levels(nx: int, ny: int, zbar: np.ndarray, rng, min_layers: int = 8) -> np.ndarray:
+    """nlevels per element (2*(nx-1)*(ny-1)) from a smooth seeded bathymetry:
+    depth between the depth of min_layers layers and the full depth."""
+    nz = len(zbar) - 1
+    xs = np.linspace(0, 1, nx)
+    ys = np.linspace(0, 1, ny)
+    X, Y = np.meshgrid(xs, ys)  # (ny, nx): node (i,j) -> [j, i]
+    f = np.zeros_like(X)
+    for _ in range(6):
+        kx, ky = rng.integers(1, 5, size=2)
+        f += rng.normal() * np.cos(np.pi * kx * X + rng.uniform(0, 6.3)) * np.cos(np.pi * ky * Y + rng.uniform(0, 6.3))
+    f = (f - f.min()) / (f.max() - f.min() + 1e-30)
+    dmin, dmax = -zbar[min_layers], -zbar[-1]
+    depth = dmin + (dmax - dmin) * f
+    # element depth = mean of its three node depths; layers whose top lies above it are wet
+    q = depth[:-1, :-1], depth[:-1, 1:], depth[1:, 1:], depth[1:, :-1]  # (i,j),(i+1,j),(i+1,j+1),(i,j+1)
+    lower = (q[0] + q[2] + q[1]) / 3.0
+    upper = (q[0] + q[3] + q[2]) / 3.0
+    el = np.stack([lower, upper], axis=-1).reshape(-1)  # quad order (j, i), lower then upper
+    tops = -zbar[:-1]
+    nlay = (tops[None, :] < el[:, None]).sum(1)
+    nlay = np.clip(nlay, min_layers, nz)
+    return (nlay + 1).astype(np.int32)

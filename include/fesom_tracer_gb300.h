@@ -1,0 +1,203 @@
+/*
+ * libfesom_tracer_gb300.so -- GB300-native FESOM2 tracer-advection step.
+ *
+ * Two C-ABI layers, both plain pointers and sizes:
+ *
+ *  1. The reference's own C interface (lib/tracer_c_interface.F90), same
+ *     symbol names, argument types and status codes, so a caller of
+ *     libfesom_tracer_Fortran.so can relink against this library. Each
+ *     declaration cites the Fortran function it replaces.
+ *
+ *  2. The fgb_* engine interface: an explicit mesh handle and caller-owned
+ *     device buffers (tracers, velocities, workspace) with a CUDA stream, so
+ *     that hosts such as PyTorch keep the allocation and the stream. It adds
+ *     what the reference interface cannot express: building the analytic
+ *     mesh, choosing schemes, stepping many tracers per launch, the FP32
+ *     form, and the individual stages of the step.
+ *
+ * Status codes: 0 success, -1 error (message on stderr for tracer_*; the
+ * text of the last error from fgb_last_error() for fgb_*).
+ * Array layouts of layer 1 are the reference's Fortran column-major ones.
+ */
+#ifndef FESOM_TRACER_GB300_H
+#define FESOM_TRACER_GB300_H
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ===================================================================== */
+/* 1. Reference interface (lib/tracer_c_interface.F90)                    */
+/* ===================================================================== */
+
+/* lib/tracer_c_interface.F90:46. One GPU, one rank: records the
+ * communicator and returns 0; no MPI is initialised. */
+int tracer_init_mpi(int mpi_comm);
+/* lib/tracer_c_interface.F90:89. Returns 0. */
+int tracer_finalize_mpi(void);
+/* lib/tracer_c_interface.F90:113. Binary restarts are not read by this
+ * library: returns -1 with the reference's message when <dir>/np<npes> is
+ * missing, and -1 ("restart reader not available") otherwise. */
+int tracer_init(const char* restart_dir);
+/* lib/tracer_c_interface.F90:163. One do_oce_adv_tra for tracer 1 plus the
+ * tendency update; del_ttf accumulates across calls as in the reference. */
+int tracer_advect_step(double dt);
+/* lib/tracer_c_interface.F90:228. min, max and plain sum of tracer 1. */
+int tracer_get_stats(double* tmin, double* tmax, double* tsum);
+/* lib/tracer_c_interface.F90:255. nz = nl-1 layers, nn = owned nodes. */
+int tracer_get_size(int* nz, int* nn);
+/* lib/tracer_c_interface.F90:280. Copies tracer 1 into values(nz,nn). */
+int tracer_get_values(double* values, int nz, int nn);
+/* lib/tracer_c_interface.F90:308. Restart writing is not provided: marks
+ * the system uninitialised and returns -1. */
+int tracer_finalize(const char* output_dir);
+/* lib/tracer_c_interface.F90:356. init + nsteps x (step, stats) + finalize. */
+int tracer_run_workflow(const char* restart_dir, int nsteps, double dt);
+/* lib/tracer_c_interface.F90:391. Resets the module state, frees device memory. */
+int tracer_cleanup(void);
+/* lib/tracer_c_interface.F90:415 */
+int tracer_set_mesh_dims(int nl, int nod2D, int edge2D, int elem2D);
+/* lib/tracer_c_interface.F90:441. Sets nodal levels only (as the reference). */
+int tracer_set_levels(const int* nlevels, const int* ulevels, int nod2D);
+/* lib/tracer_c_interface.F90:477. Sets hnode_new only (as the reference). */
+int tracer_set_thickness(const double* hnode, int nl, int nod2D);
+/* lib/tracer_c_interface.F90:510 */
+int tracer_set_partition(int myDim_nod2D, int eDim_nod2D);
+/* lib/tracer_c_interface.F90:539. Defaults UPW1/UPW1/NONE, ph=pv=1. */
+int tracer_allocate_tracers(int num_tracers, int nl, int nod2D, int AB_order);
+/* lib/tracer_c_interface.F90:613. Sets values and valuesAB of one tracer. */
+int tracer_set_values(int tracer_id, const double* values, int nl, int nod2D);
+/* lib/tracer_c_interface.F90:652 */
+int tracer_set_velocity_zero(int nl, int nod2D, int edge2D);
+/* lib/tracer_c_interface.F90:694. uv is stored as given, (nl-1,edge2D,2),
+ * and read by the step as vel(2,nl-1,elem2D) -- the reference reinterprets
+ * the same memory. w_e and w_i are set to zero, as in the reference. */
+int tracer_set_velocity(const double* uv, const double* w, int nl, int nod2D, int edge2D);
+/* lib/tracer_c_interface.F90:749 */
+int tracer_init_complete(void);
+/* lib/tracer_c_interface.F90:769. Restart partitions are not read: -1. */
+int tracer_load_mesh_partition(const char* restart_dir);
+/* lib/tracer_c_interface.F90:830. FESOM ASCII mesh reader: not provided, -1. */
+int tracer_load_mesh_from_files(const char* mesh_path);
+/* lib/tracer_c_interface.F90:875. Layer thicknesses from zbar. */
+int tracer_init_ale_arrays(void);
+/* lib/tracer_c_interface.F90:931. Allocates work arrays (device). */
+int tracer_init_for_advection(void);
+
+/* Extensions of the reference interface (no Fortran counterpart). */
+/* Analytic mesh of lib/analytic_mesh.F90:114 (what the analytic dwarf
+ * src/fesom_analytic.F90:188 builds); replaces loading a mesh. */
+int tracer_generate_analytic_mesh(int nx, int ny, int nl, int periodic);
+/* Advection schemes of one tracer: hor "UPW1"|"MUSCL"|"MFCT", ver
+ * "UPW1"|"QR4C"|"CDIFF"|"PPM", lim "NONE"|"FCT" (T_TRACER_DATA fields,
+ * lib/MOD_TRACER.F90:18-20). */
+int tracer_set_schemes(int tracer_id, const char* hor, const char* ver, const char* lim, double ph,
+                       double pv);
+/* Device form of the step: 0 = FP64 (default), 1 = FP32. */
+int tracer_set_precision(int precision);
+
+/* ===================================================================== */
+/* 2. Engine interface                                                    */
+/* ===================================================================== */
+
+typedef struct fgb_hmesh fgb_hmesh; /* host-side mesh (set-up) */
+typedef struct fgb_mesh fgb_mesh;   /* device-resident mesh */
+
+enum { FGB_HOR_UPW1 = 0, FGB_HOR_MUSCL = 1, FGB_HOR_MFCT = 2 };
+enum { FGB_VER_UPW1 = 0, FGB_VER_QR4C = 1, FGB_VER_CDIFF = 2, FGB_VER_PPM = 3 };
+enum { FGB_LIM_NONE = 0, FGB_LIM_FCT = 1 };
+enum { FGB_FP64 = 0, FGB_FP32 = 1 };
+
+/* Stages of one step (bit mask for fgb_adv_stages). */
+enum {
+  FGB_STAGE_VFLUX = 1,  /* edge volume fluxes from the velocity (per step) */
+  FGB_STAGE_HFLUX = 2,  /* horizontal LO / antidiffusive edge fluxes */
+  FGB_STAGE_LO = 4,     /* FCT low-order solution + vertical antidiffusive flux */
+  FGB_STAGE_RATIO = 8,  /* FCT bounds, sums and limiting factors */
+  FGB_STAGE_UPDATE = 16 /* limiting, flux divergence, tracer update */
+};
+
+const char* fgb_last_error(void);
+int fgb_version(void);
+
+/* Analytic mesh (lib/analytic_mesh.F90:114-829 + geometry). zbar: nl values
+ * or NULL (uniform to depth); elem_nlev: nlevels per element or NULL (flat).
+ * flags = 0 reproduces the reference mesh exactly. FGB_MESH_CLUSTER_FULL
+ * replaces the reference's un-remapped nod_in_elem2D of periodic meshes
+ * (lib/analytic_mesh.F90:675-707) by the full lists; FGB_MESH_ORIENT_LEFT
+ * swaps an edge's nodes where edge_tri(1) lies to the right of
+ * node1 -> node2 (the analytic grid does so for horizontal and vertical
+ * edges, lib/analytic_mesh.F90:386-426; FESOM mesh files keep it left). */
+enum { FGB_MESH_CLUSTER_FULL = 1, FGB_MESH_ORIENT_LEFT = 2 };
+int fgb_hmesh_analytic(int nx, int ny, int nl, double Lx, double Ly, double depth, int periodic, int flags,
+                       const double* zbar, const int* elem_nlev, fgb_hmesh** out);
+void fgb_hmesh_free(fgb_hmesh* h);
+/* out[0..7] = N, E, M, nl, max_nie, edge2D_in, incident-edge entries, cluster entries */
+int fgb_hmesh_sizes(const fgb_hmesh* h, long long* out8);
+/* Copies a named array (0-based indices) into out; returns its element
+ * count (out may be NULL to query), -1 for an unknown name. *kind is set to
+ * 0 for int32, 1 for float64. */
+long long fgb_hmesh_get(const fgb_hmesh* h, const char* name, void* out, int* kind);
+/* Replaces the vertical arrays (N,nl-1) hnode, hnode_new and (M,nl-1)
+ * helem; any may be NULL to keep it. */
+int fgb_hmesh_set_vertical(fgb_hmesh* h, const double* hnode, const double* hnode_new, const double* helem);
+
+/* Uploads the mesh to the current device (FP64 and FP32 geometry). */
+int fgb_mesh_create(const fgb_hmesh* h, fgb_mesh** out);
+void fgb_mesh_free(fgb_mesh* m);
+/* out[0..7] = N, E, M, nl, nz, LZ, LW, fewest layers in a column. Device
+ * arrays are padded: layers to LZ, interfaces to LW (multiples of 4). */
+int fgb_mesh_dims(const fgb_mesh* m, int* out8);
+/* Re-uploads hnode/hnode_new/helem from the host mesh. */
+int fgb_mesh_update_vertical(fgb_mesh* m, const fgb_hmesh* h);
+
+/* Workspace of a step: bytes, and the byte offsets of its arrays
+ * (vf, flo, adfh, lo, adfv, rp, rm). */
+long long fgb_workspace_bytes(const fgb_mesh* m, int precision, int ntracers);
+int fgb_workspace_offsets(const fgb_mesh* m, int precision, int ntracers, long long* out7);
+
+/* One call of the step for a batch of tracers. Device pointers:
+ *   T      (K,N,LZ) values, updated in place (strideT elements apart)
+ *   TA     (K,N,LZ) valuesAB used by the high-order fluxes, or NULL for T
+ *   TAout  optional, receives the new values (copy-AB time level)
+ *   vel    (M,LZ,2) velocity on elements; w, we (N,LW) vertical velocities
+ *   del    optional (K,N,LZ) persistent tendency (reference C-ABI semantics)
+ *   workspace of fgb_workspace_bytes. */
+typedef struct {
+  int precision;
+  int ntracers;
+  int hor, ver, lim;
+  double ph, pv, dt;
+  void* T;
+  long long strideT;
+  const void* TA;
+  long long strideTA;
+  void* TAout;
+  const void* vel;
+  const void* w;
+  const void* we;
+  void* del;
+  void* workspace;
+  long long workspace_bytes;
+} fgb_step_desc;
+
+/* Full step: vflux, hflux, and the FCT (lo, ratio, update) or plain update. */
+int fgb_adv_step(const fgb_mesh* m, const fgb_step_desc* d, void* stream);
+/* Selected stages only (FGB_STAGE_* mask), in pipeline order. */
+int fgb_adv_stages(const fgb_mesh* m, const fgb_step_desc* d, int stage_mask, void* stream);
+
+/* Min, max, plain sum (FP64) and NaN count of values (K,N,LZ) over the
+ * first nz layers of every node (src/fesom_analytic.F90:441-445): out_dev
+ * receives 4 doubles per tracer; scratch of fgb_stats_scratch_bytes. */
+long long fgb_stats_scratch_bytes(const fgb_mesh* m, int ntracers);
+int fgb_tracer_stats(const fgb_mesh* m, int precision, const void* T, long long strideT, int ntracers,
+                     void* scratch, double* out_dev, void* stream);
+
+/* Number of kernels the last fgb_adv_step / fgb_adv_stages call launched. */
+int fgb_last_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

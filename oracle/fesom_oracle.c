@@ -392,6 +392,11 @@ static void find_up_downwind_triangles(omesh* m) {
 
 omesh* om_mesh_analytic(int nx, int ny, int nl, double Lx, double Ly, double max_depth,
                         int periodic, int cluster_full, const double* zbar_in, const int* elem_nlev) {
+  return om_mesh_analytic2(nx, ny, nl, Lx, Ly, max_depth, periodic, cluster_full, 0, zbar_in, elem_nlev);
+}
+
+omesh* om_mesh_analytic2(int nx, int ny, int nl, double Lx, double Ly, double max_depth, int periodic,
+                         int cluster_full, int orient_left, const double* zbar_in, const int* elem_nlev) {
   if (nx < 2 || ny < 2 || nl < 3) return NULL;
   if (periodic && (nx < 3 || ny < 3)) return NULL;
   omesh* m = (omesh*)xcalloc(1, sizeof(omesh));
@@ -556,6 +561,23 @@ omesh* om_mesh_analytic(int nx, int ny, int nl, double Lx, double Ly, double max
       }
     free(en);
     free(ee);
+  }
+
+  if (orient_left) {
+    for (int n = 1; n <= E; ++n) {
+      int a = A2(m->edges, 2, 1, n), b = A2(m->edges, 2, 2, n), el = A2(m->edge_tri, 2, 1, n);
+      const int* v = &A2(m->elem2D_nodes, 3, 1, el);
+      double cx = (A2(m->coord, 2, 1, v[0]) + A2(m->coord, 2, 1, v[1]) + A2(m->coord, 2, 1, v[2])) / 3.0;
+      double cy = (A2(m->coord, 2, 2, v[0]) + A2(m->coord, 2, 2, v[1]) + A2(m->coord, 2, 2, v[2])) / 3.0;
+      double dx0 = A2(m->coord, 2, 1, b) - A2(m->coord, 2, 1, a), dy0 = A2(m->coord, 2, 2, b) - A2(m->coord, 2, 2, a);
+      double s[2] = {cx - A2(m->coord, 2, 1, a), cy - A2(m->coord, 2, 2, a)};
+      wrap_mi(m, s);
+      double sx = s[0], sy = s[1];
+      if (dx0 * sy - dy0 * sx < 0.0) {
+        A2(m->edges, 2, 1, n) = b;
+        A2(m->edges, 2, 2, n) = a;
+      }
+    }
   }
 
   /* 1g. levels, :601-608 (element overrides: see header) */

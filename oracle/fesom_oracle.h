@@ -38,6 +38,12 @@ typedef struct omesh omesh;
  * reference does (lib/analytic_mesh.F90:675-694 runs before the remap at :705). */
 omesh* om_mesh_analytic(int nx, int ny, int nl, double Lx, double Ly, double max_depth,
                         int periodic, int cluster_full, const double* zbar, const int* elem_nlev);
+/* As om_mesh_analytic; orient_left=1 swaps the nodes of every edge whose
+ * edge_tri(1) lies to the right of node1 -> node2 (FESOM mesh-file
+ * orientation; the analytic grid, lib/analytic_mesh.F90:386-426, has it on
+ * the right for horizontal and vertical edges). */
+omesh* om_mesh_analytic2(int nx, int ny, int nl, double Lx, double Ly, double max_depth, int periodic,
+                         int cluster_full, int orient_left, const double* zbar, const int* elem_nlev);
 void om_mesh_free(omesh* m);
 /* sizes: [nod2D, nod2D_total, elem2D, edge2D, edge2D_in, nl, max_nie] */
 void om_mesh_sizes(const omesh* m, int* out7);

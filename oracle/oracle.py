@@ -45,6 +45,10 @@ def lib():
         L.om_mesh_analytic.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                        ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                        _dp, _ip]
+        L.om_mesh_analytic2.restype = ctypes.c_void_p
+        L.om_mesh_analytic2.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_int, _dp, _ip]
         L.om_mesh_free.argtypes = [ctypes.c_void_p]
         L.om_mesh_sizes.argtypes = [ctypes.c_void_p, _ip]
         L.om_mesh_get_int.restype = ctypes.c_long
@@ -85,13 +89,13 @@ class Mesh:
     """An analytic mesh built by the oracle (lib/analytic_mesh.F90)."""
 
     def __init__(self, nx, ny, nl, Lx=100000.0, Ly=100000.0, depth=1000.0, periodic=True,
-                 cluster_full=False, zbar=None, elem_nlev=None):
+                 cluster_full=False, zbar=None, elem_nlev=None, orient_left=False):
         L = lib()
         zb = _f64(zbar) if zbar is not None else None
         en = np.ascontiguousarray(elem_nlev, dtype=np.int32) if elem_nlev is not None else None
         self._zb, self._en = zb, en
-        h = L.om_mesh_analytic(nx, ny, nl, Lx, Ly, depth, int(periodic), int(cluster_full),
-                               _p(zb), _p(en, _ip))
+        h = L.om_mesh_analytic2(nx, ny, nl, Lx, Ly, depth, int(periodic), int(cluster_full),
+                                int(orient_left), _p(zb), _p(en, _ip))
         if not h:
             raise ValueError("invalid analytic mesh parameters")
         self.h = ctypes.c_void_p(h)
