@@ -92,6 +92,21 @@ class TracerAdvection:
         else:
             self.we = self._pad_nodes(we, m.nl, m.LW)
 
+    def load_padded(self, T=None, TA=None, vel=None, w=None, we=None):
+        """Copy device tensors that already have the padded layouts
+        (K,N,LZ), (M,LZ,2), (N,LW)."""
+        if T is not None:
+            self.T.copy_(T)
+        if TA is not None and self.TA is not None:
+            self.TA.copy_(TA)
+        if vel is not None:
+            self.vel.copy_(vel)
+        if w is not None:
+            self.w.copy_(w)
+            self.we = self.w
+        if we is not None:
+            self.we = we.to(self.dtype).contiguous()
+
     # ---- step --------------------------------------------------------------
     def _desc(self, dt):
         d = _lib.StepDesc()

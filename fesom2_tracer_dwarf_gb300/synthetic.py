@@ -68,14 +68,14 @@ def random_flow(m: Mesh, rng, umax: float = 0.3, wmax: float = 2e-3):
     return vel, w
 
 
-def _edge_vflux(m: Mesh, vel: np.ndarray) -> np.ndarray:
+def _edge_vflux(m: Mesh, vel: np.ndarray, helem=None, levels=None) -> np.ndarray:
     """Volume flux through each edge's two segments, (E, nz), as the upwind
     flux of lib/oce_adv_tra_hor.F90:174-252 forms it."""
     ed_tri = m.get("edge_tri")
     cr = m.get("edge_cross_dxdy")
-    helem = m.get("helem")
+    helem = m.get("helem") if helem is None else helem
     lev = m.get("edge_lev")
-    z = np.arange(1, m.nz + 1)[None, :]
+    z = np.arange(1, (m.nz if levels is None else levels) + 1)[None, :]
     nu1, nl1, nu2, nl2 = (lev[:, i:i + 1] for i in range(4))
     nl12, nu12 = np.minimum(nl1, nl2), np.maximum(nu1, nu2)
     use1 = ((z >= nu1) & (z <= nu12 - 1)) | ((z >= nu12) & (z <= nl12)) | ((z > nl12) & (z <= nl1))
@@ -90,7 +90,7 @@ def _edge_vflux(m: Mesh, vel: np.ndarray) -> np.ndarray:
 def _node_divergence(m: Mesh, vf: np.ndarray) -> np.ndarray:
     """Net inflow of a uniform tracer per node and layer, (N, nz)."""
     edges = m.get("edges")
-    D = np.zeros((m.N, m.nz))
+    D = np.zeros((m.N,) + vf.shape[1:])
     np.add.at(D, edges[:, 0], -vf)
     np.add.at(D, edges[:, 1], vf)
     return D
@@ -112,15 +112,15 @@ def diagnose_w(m: Mesh, vel: np.ndarray) -> np.ndarray:
 
 def max_cfl(m: Mesh, vel: np.ndarray, dt: float) -> float:
     """max over nodes and layers of dt * (upwind outflow) / (areasvol * hnode)."""
-    vf = _edge_vflux(m, vel)
-    edges = m.get("edges")
-    out = np.zeros((m.N, m.nz))
-    np.add.at(out, edges[:, 0], np.maximum(vf, 0.0))
-    np.add.at(out, edges[:, 1], np.maximum(-vf, 0.0))
+    out = _node_out(m, _edge_vflux(m, vel))
     vol = m.get("areasvol")[:, : m.nz] * m.get("hnode")
     nlev = m.get("nlevels_nod2D")
     wet = np.arange(m.nz)[None, :] < (nlev - 1)[:, None]
     return float(np.max(np.where(wet, dt * out / np.where(vol > 0, vol, 1.0), 0.0)))
+
+
+def _flat(m: Mesh) -> bool:
+    return bool(np.all(m.get("nlevels") == m.nl)) and bool(np.all(m.get("nlevels_nod2D") == m.nl))
 
 
 def streamfunction_flow(m: Mesh, rng, dt: float, cfl: float = 0.4, nmodes: int = 8, kmax: int = 8,
@@ -141,13 +141,32 @@ def streamfunction_flow(m: Mesh, rng, dt: float, cfl: float = 0.4, nmodes: int =
     gs = m.get("gradient_sca")
     dpx = (gs[:, 0:3] * psi[en]).sum(1)
     dpy = (gs[:, 3:6] * psi[en]).sum(1)
-    zmid = 0.5 * (m.get("zbar_3d_n")[0, :-1] + m.get("zbar_3d_n")[0, 1:])
-    h = m.get("helem")
+    zb = m.get("zbar")
+    zmid = 0.5 * (zb[:-1] + zb[1:])
+    h = zb[:-1] - zb[1:]
     s = np.exp(zmid / efold)
+    if _flat(m):
+        # One 2-D pass: vflux(e, z) = vflux2d(e) * s(z) * h(z), divergence likewise.
+        vel2 = np.zeros((m.M, 1, 2))
+        vel2[:, 0, 0] = -dpy
+        vel2[:, 0, 1] = dpx
+        vf2 = _edge_vflux(m, vel2, helem=np.ones((m.M, 1)), levels=1)[:, 0]
+        out = _node_out(m, vf2)
+        vol2 = m.get("areasvol")[:, 0]
+        scale = cfl / float(np.max(dt * out[:, None] * (s * h)[None, :] / (vol2[:, None] * h[None, :])))
+        vel = np.empty((m.M, m.nz, 2))
+        vel[..., 0] = (-dpy * scale)[:, None] * s[None, :]
+        vel[..., 1] = (dpx * scale)[:, None] * s[None, :]
+        D2 = _node_divergence(m, vf2) * scale
+        area = m.get("area")
+        w = np.zeros((m.N, m.nl))
+        for k in range(m.nz - 1, -1, -1):
+            w[:, k] = (D2 * s[k] * h[k] + w[:, k + 1] * area[:, k + 1]) / area[:, k]
+        return vel, w
     nlevel = m.get("nlevels")
     wet = np.arange(m.nz)[None, :] < (nlevel - 1)[:, None]
-    full = (s[None, :] * h).sum(1)
-    col = (np.where(wet, s[None, :] * h, 0.0)).sum(1)
+    full = (s * h).sum()
+    col = np.where(wet, (s * h)[None, :], 0.0).sum(1)
     prof = np.where(wet, s[None, :] * (full / col)[:, None], 0.0)
     vel = np.zeros((m.M, m.nz, 2))
     vel[..., 0] = -dpy[:, None] * prof
@@ -156,6 +175,14 @@ def streamfunction_flow(m: Mesh, rng, dt: float, cfl: float = 0.4, nmodes: int =
     vel *= cfl / c
     w = diagnose_w(m, vel)
     return vel, w
+
+
+def _node_out(m: Mesh, vf: np.ndarray) -> np.ndarray:
+    edges = m.get("edges")
+    out = np.zeros((m.N,) + vf.shape[1:])
+    np.add.at(out, edges[:, 0], np.maximum(vf, 0.0))
+    np.add.at(out, edges[:, 1], np.maximum(-vf, 0.0))
+    return out
 
 
 def gaussian_T(m: Mesh, rng) -> np.ndarray:
@@ -209,3 +236,82 @@ def bathymetry_levels(nx: int, ny: int, zbar: np.ndarray, rng, min_layers: int =
     nlay = (tops[None, :] < el[:, None]).sum(1)
     nlay = np.clip(nlay, min_layers, nz)
     return (nlay + 1).astype(np.int32)
+
+
+def flat_streamfunction_device(m: Mesh, rng, dt: float, dtype, device, cfl: float = 0.4, nmodes: int = 8,
+                               kmax: int = 8, efold: float = 500.0):
+    """streamfunction_flow for flat meshes, built directly as padded device
+    tensors vel (M, LZ, 2) and w (N, LW) (large benchmark meshes)."""
+    import torch
+
+    assert _flat(m), "flat meshes only"
+    x, y = node_xy(m)
+    psi = np.zeros(m.N)
+    for _ in range(nmodes):
+        kx, ky = rng.integers(1, kmax + 1, size=2)
+        ph = rng.uniform(0, 2 * np.pi)
+        psi += np.sin(2 * np.pi * (kx * x / m.Lx + ky * y / m.Ly) + ph) / np.hypot(kx, ky)
+    en = m.get("elem_nodes")
+    gs = m.get("gradient_sca")
+    dpx = (gs[:, 0:3] * psi[en]).sum(1)
+    dpy = (gs[:, 3:6] * psi[en]).sum(1)
+    zb = m.get("zbar")
+    zmid = 0.5 * (zb[:-1] + zb[1:])
+    h = zb[:-1] - zb[1:]
+    s = np.exp(zmid / efold)
+    vel2 = np.zeros((m.M, 1, 2))
+    vel2[:, 0, 0] = -dpy
+    vel2[:, 0, 1] = dpx
+    vf2 = _edge_vflux(m, vel2, helem=np.ones((m.M, 1)), levels=1)[:, 0]
+    out = _node_out(m, vf2)
+    vol2 = m.get("areasvol")[:, 0]
+    scale = cfl / float(np.max(dt * out[:, None] * s[None, :] / vol2[:, None]))
+    t = lambda a: torch.as_tensor(a, dtype=torch.float64, device=device)
+    vel = torch.zeros(m.M, m.LZ, 2, dtype=dtype, device=device)
+    sz = t(s)
+    vel[:, : m.nz, 0] = (t(-dpy * scale)[:, None] * sz[None, :]).to(dtype)
+    vel[:, : m.nz, 1] = (t(dpx * scale)[:, None] * sz[None, :]).to(dtype)
+    D2 = t(_node_divergence(m, vf2) * scale)
+    area = t(m.get("area"))
+    w = torch.zeros(m.N, m.LW, dtype=torch.float64, device=device)
+    for k in range(m.nz - 1, -1, -1):
+        w[:, k] = (D2 * (s[k] * h[k]) + w[:, k + 1] * area[:, k + 1]) / area[:, k]
+    return vel, w.to(dtype)
+
+
+def tracers_device(m: Mesh, K: int, seed: int, dtype, device):
+    """(K, N, LZ) padded tracers: T (Gaussian blob + noise), S (35 + noise),
+    then passive Gaussian blobs in [0, 1]."""
+    import torch
+
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    x, y = node_xy(m)
+    zb = m.get("zbar")
+    zmid = 0.5 * (zb[:-1] + zb[1:])
+    H = -zb[-1]
+    X = torch.as_tensor(x, dtype=torch.float64, device=device)[:, None]
+    Y = torch.as_tensor(y, dtype=torch.float64, device=device)[:, None]
+    Zm = torch.as_tensor(zmid, dtype=torch.float64, device=device)[None, :]
+    out = torch.zeros(K, m.N, m.LZ, dtype=dtype, device=device)
+    rng = np.random.default_rng(seed)
+    for t in range(K):
+        if t == 0:
+            r2 = ((X - 0.5 * m.Lx) ** 2 + (Y - 0.5 * m.Ly) ** 2) / (2 * (m.Lx / 8) ** 2)
+            zz = (Zm + 0.25 * H) ** 2 / (2 * (0.25 * H) ** 2)
+            v = 2.0 + 20.0 * torch.exp(-r2 - zz)
+            v = v + 0.1 * torch.randn(m.N, m.nz, generator=g, dtype=torch.float64, device=device)
+        elif t == 1:
+            v = 35.0 + 0.3 * torch.randn(m.N, m.nz, generator=g, dtype=torch.float64, device=device)
+        else:
+            cx, cy = rng.uniform(0, m.Lx), rng.uniform(0, m.Ly)
+            sx, sy = rng.uniform(0.05, 0.2) * m.Lx, rng.uniform(0.05, 0.2) * m.Ly
+            cz, sz = -rng.uniform(0, H), rng.uniform(0.1, 0.5) * H
+            dx = (X - cx).abs()
+            dy = (Y - cy).abs()
+            if m.periodic:
+                dx = torch.minimum(dx, m.Lx - dx)
+                dy = torch.minimum(dy, m.Ly - dy)
+            v = torch.exp(-(dx / sx) ** 2 - (dy / sy) ** 2) * torch.exp(-((Zm - cz) / sz) ** 2)
+        out[t, :, : m.nz] = v.to(dtype)
+    return out
