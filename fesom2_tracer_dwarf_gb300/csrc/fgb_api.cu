@@ -168,7 +168,7 @@ long long fgb_hmesh_get(const fgb_hmesh* h, const char* name, void* out, int* ki
       {"nboundary_lay", &m.nboundary_lay}, {"ne_ptr", &m.ne_ptr}, {"ne_code", &m.ne_code},
       {"ne_other", &m.ne_other}, {"ne_lo", &m.ne_lo}, {"ne_hi", &m.ne_hi}, {"cl_ptr", &m.cl_ptr},
       {"cl_node", &m.cl_node}, {"cl_lev", &m.cl_lev}, {"cl_minlev", &m.cl_minlev}, {"edge_lev", &m.edge_lev},
-      {"edge_gm", &m.edge_gm}, {"nie_ptr", &m.nie_ptr}, {"nie_idx", &m.nie_idx}};
+      {"edge_gm", &m.edge_gm}, {"edge_order", &m.edge_order}, {"nie_ptr", &m.nie_ptr}, {"nie_idx", &m.nie_idx}};
   struct { const char* n; const std::vector<double>* v; } dbls[] = {
       {"coord", &m.coord}, {"zbar", &m.zbar}, {"Z", &m.Z}, {"elem_area", &m.elem_area}, {"area", &m.area},
       {"areasvol", &m.areasvol}, {"edge_dxdy", &m.edge_dxdy}, {"edge_cross_dxdy", &m.edge_cross},
@@ -242,6 +242,7 @@ int fgb_mesh_create(const fgb_hmesh* hm, fgb_mesh** out) {
             !upload(mm, h.edge_updn.data(), h.edge_updn.size(), &d.edge_updn) &&
             !upload(mm, h.edge_lev.data(), h.edge_lev.size(), &d.edge_lev) &&
             !upload(mm, h.edge_gm.data(), h.edge_gm.size(), &d.edge_gm) &&
+            !upload(mm, h.edge_order.data(), h.edge_order.size(), &d.edge_order) &&
             !upload_geo<double>(mm, h, d.g64, &mm->hnode64, &mm->hnode_new64, &mm->helem64) &&
             !upload_geo<float>(mm, h, d.g32, &mm->hnode32, &mm->hnode_new32, &mm->helem32);
   if (!ok) {

@@ -46,6 +46,7 @@ struct DMesh {
   const int* edge_updn;   // (E,2)
   const int* edge_lev;    // (E,4)
   const int* edge_gm;     // (E,2)
+  const int* edge_order;  // (E) order in which edge kernels visit the edges
   GeoPtrs<double> g64;
   GeoPtrs<float> g32;
 };
@@ -60,7 +61,6 @@ struct StepPtrs {
   const R* w;       // (N,LW) vertical velocity used by the high-order flux under FCT
   const R* we;      // (N,LW) explicit vertical velocity
   R* vf;            // (E,LZ) volume flux through the edge segments
-  R* flo;           // (K,E,LZ) low-order horizontal flux
   R* adfh;          // (K,E,LZ) antidiffusive (FCT) or high-order horizontal flux
   R* lo;            // (K,N,LZ) low-order solution fct_LO
   R* adfv;          // (K,N,LW) antidiffusive vertical flux
@@ -68,6 +68,7 @@ struct StepPtrs {
   R* rm;            // (K,N,LZ) fct_minus limiting factor
   R* del;           // optional (K,N,LZ) persistent del_ttf
   long long sT, sTA, sE, sN, sW;  // strides between tracers (elements)
+  int K;            // tracers in this launch
   R dt, ph, pv;
 };
 

@@ -530,6 +530,13 @@ void build_tables(HostMesh& m) {
     }
     m.cl_ptr[n + 1] = (int)m.cl_node.size();
   }
+  // Visit order of the edge kernels: by lower node, so that the horizontal,
+  // vertical and diagonal edges of a grid row are swept together.
+  m.edge_order.resize(E);
+  for (int e = 0; e < E; ++e) m.edge_order[e] = e;
+  std::stable_sort(m.edge_order.begin(), m.edge_order.end(), [&](int a, int b) {
+    return std::min(m.edges[2 * a], m.edges[2 * a + 1]) < std::min(m.edges[2 * b], m.edges[2 * b + 1]);
+  });
   // MUSCL gradient windows and edge lengths scaled to metres.
   m.edge_gm.assign((size_t)2 * E, -1);
   m.edge_dxa.assign((size_t)2 * E, 0.0);

@@ -58,6 +58,7 @@ struct HostMesh {
   std::vector<int> edge_lev;          // (E,4) nu1,nl1,nu2,nl2 (1-based layers; nl = nlevels-1)
   std::vector<int> edge_gm;           // (E,2) layer window using the triangle gradients, -1 if none
   std::vector<double> edge_dxa;       // (E,2) edge_dxdy(1)*a, edge_dxdy(2)*r_earth
+  std::vector<int> edge_order;        // (E) edges sorted by their lower node (locality of edge sweeps)
 };
 
 // Analytic mesh of lib/analytic_mesh.F90:114-829 with its geometry.

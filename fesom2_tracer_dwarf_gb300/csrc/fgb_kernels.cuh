@@ -4,7 +4,9 @@
 // Layout: level index fastest, columns padded to LZ layers / LW interfaces.
 // Node-column kernels run one warp per node with the column staged in shared
 // memory; edge kernels run one warp per edge, lanes over layers (coalesced
-// 256-byte rows). The reference's edge scatters (atomics / OpenMP locks) are
+// rows) with two consecutive layers per lane. Node kernels loop over the
+// tracers of a launch KC at a time, so the mesh tables, geometry and edge
+// volume fluxes they load serve all tracers. The reference's edge scatters (atomics / OpenMP locks) are
 // replaced by gathers over each node's incident edges in ascending edge order,
 // which reproduces the reference's per-node summation order exactly.
 //
@@ -99,6 +101,32 @@ __device__ __forceinline__ void elem_grad(const DMesh& m, const GeoPtrs<R>& g, c
   gy = gs[3] * ta + gs[4] * tb + gs[5] * tc;
 }
 
+// A triangle's nodes and gradient coefficients held in registers.
+template <typename R>
+struct Tri {
+  int a, b, c;
+  R x0, x1, x2, y0, y1, y2;
+};
+
+template <typename R>
+__device__ __forceinline__ Tri<R> load_tri(const DMesh& m, const GeoPtrs<R>& g, int el) {
+  Tri<R> q;
+  q.a = m.elem_nodes[3 * el];
+  q.b = m.elem_nodes[3 * el + 1];
+  q.c = m.elem_nodes[3 * el + 2];
+  const R* gs = g.grad_sca + 6 * (size_t)el;
+  q.x0 = gs[0]; q.x1 = gs[1]; q.x2 = gs[2];
+  q.y0 = gs[3]; q.y1 = gs[4]; q.y2 = gs[5];
+  return q;
+}
+
+template <typename R>
+__device__ __forceinline__ void tri_grad(const Tri<R>& q, const R* __restrict__ T, size_t LZ, int k, R& gx, R& gy) {
+  const R ta = T[q.a * LZ + k], tb = T[q.b * LZ + k], tc = T[q.c * LZ + k];
+  gx = q.x0 * ta + q.x1 * tb + q.x2 * tc;
+  gy = q.y0 * ta + q.y1 * tb + q.y2 * tc;
+}
+
 // Area-weighted mean of the element gradients around a node at layer z
 // (lib/oce_muscl_adv.F90:393-410).
 template <typename R>
@@ -120,81 +148,153 @@ __device__ __forceinline__ void node_mean_grad(const DMesh& m, const GeoPtrs<R>&
   gy = ty / tvol;
 }
 
+// Two consecutive layers per lane: vector loads and stores of R pairs.
+template <typename R>
+struct V2T;
+template <>
+struct V2T<float> {
+  using T = float2;
+};
+template <>
+struct V2T<double> {
+  using T = double2;
+};
+template <typename R>
+using vec2 = typename V2T<R>::T;
+template <typename R>
+__device__ __forceinline__ vec2<R> ld2(const R* p) {
+  return *reinterpret_cast<const vec2<R>*>(p);
+}
+template <typename R>
+__device__ __forceinline__ void st2(R* p, R a, R b) {
+  vec2<R> v;
+  v.x = a;
+  v.y = b;
+  *reinterpret_cast<vec2<R>*>(p) = v;
+}
+
+// High-order horizontal flux of one layer: upwind (adv_tra_hor_upw1,
+// lib/oce_adv_tra_hor.F90:218-220) or the MUSCL/MFCT edge reconstruction
+// (lib/oce_adv_tra_hor.F90:454-497, :748-790); c1, c2 are the c_lo masks.
+template <typename R, int HOR>
+__device__ __forceinline__ R ho_flux(R v, R vp, R vm, R ta1, R ta2, R g1, R g2, R g3, R g4, R ex, R ey, R c1, R c2,
+                                     R ph) {
+  if (HOR == 0) return -(R(0.5) * (ta1 * vp + ta2 * vm));
+  R Tm2, Tm1;
+  if (HOR == 1) {
+    Tm2 = ta2 - ((R(2) * (ta2 - ta1) + ex * g2 + ey * g4) / R(6)) * c2;
+    Tm1 = ta1 + ((R(2) * (ta2 - ta1) + ex * g1 + ey * g3) / R(6)) * c1;
+  } else {
+    Tm2 = ta2 - (R(2) * (ta2 - ta1) + ex * g2 + ey * g4) / R(6);
+    Tm1 = ta1 + (R(2) * (ta2 - ta1) + ex * g1 + ey * g3) / R(6);
+  }
+  const R cHO = vp * Tm1 + vm * Tm2;
+  return -((R(0.5) * (R(1) - ph)) * cHO) - ((v * ph) * R(0.5)) * (Tm1 + Tm2);
+}
+
 // ---------------------------------------------------------------------------
-// Horizontal edge fluxes. FCT: writes the low-order flux (adv_tra_hor_upw1 on
-// T) and the antidiffusive flux HO(T_AB) - LO; otherwise the HO flux.
-// HOR: 0 UPW1, 1 MUSCL (with the nboundary_lay mask c_lo), 2 MFCT.
+// Horizontal edge fluxes of all K tracers. FCT: the antidiffusive flux
+// HO(T_AB) - LO(T) (adv_tra_hor_* with o_init_zero=.false. after
+// adv_tra_hor_upw1, lib/oce_adv_tra_driver.F90:95,244-255); otherwise the HO
+// flux. HOR: 0 UPW1, 1 MUSCL (with the nboundary_lay mask c_lo), 2 MFCT.
+// One warp per edge, two layers per lane. Edges are visited in edge_order
+// (the three edge families interleaved by node) for cache locality; results
+// are stored at the edge's own index.
 // ---------------------------------------------------------------------------
 template <typename R, int HOR, bool FCT>
-__global__ void __launch_bounds__(256) k_hflux(DMesh m, StepPtrs<R> a) {
+__global__ void __launch_bounds__(256, 3) k_hflux(DMesh m, StepPtrs<R> a) {
   const int lane = threadIdx.x & (kWarp - 1);
-  const int e = blockIdx.x * (blockDim.x / kWarp) + (threadIdx.x / kWarp);
-  if (e >= m.E) return;
-  const int t = blockIdx.y;
+  const int w = blockIdx.x * (blockDim.x / kWarp) + (threadIdx.x / kWarp);
+  if (w >= m.E) return;
+  const int e = m.edge_order ? m.edge_order[w] : w;
   const GeoPtrs<R>& g = GeoSel<R>::get(m);
-  const R* __restrict__ T = a.T + t * a.sT;
-  const R* __restrict__ TA = a.TA + t * a.sTA;
-  R* __restrict__ flo = FCT ? a.flo + t * a.sE : nullptr;
-  R* __restrict__ adf = a.adfh + t * a.sE;
   const size_t LZ = m.LZ;
   const int n1 = m.edge_nodes[2 * e], n2 = m.edge_nodes[2 * e + 1];
   const int nu1 = m.edge_lev[4 * e], nl1 = m.edge_lev[4 * e + 1];
   const int nu2 = m.edge_lev[4 * e + 2], nl2 = m.edge_lev[4 * e + 3];
-  int up = -1, dn = -1, gm0 = -1, gm1 = -1, nb1 = 0, nb2 = 0;
+  int gm0 = -1, gm1 = -1, nb1 = 0, nb2 = 0;
   R ex = R(0), ey = R(0);
+  Tri<R> tu{}, td{};
   if (HOR != 0) {
-    up = m.edge_updn[2 * e];
-    dn = m.edge_updn[2 * e + 1];
     gm0 = m.edge_gm[2 * e];
     gm1 = m.edge_gm[2 * e + 1];
     ex = g.edge_dxa[2 * e];
     ey = g.edge_dxa[2 * e + 1];
     nb1 = m.nbl[n1];
     nb2 = m.nbl[n2];
+    if (gm0 >= 0) {
+      tu = load_tri(m, g, m.edge_updn[2 * e]);
+      td = load_tri(m, g, m.edge_updn[2 * e + 1]);
+    }
   }
   const R ph = a.ph;
-  for (int k = lane; k < m.nz; k += kWarp) {
-    const int z = k + 1;
-    const int seg = edge_seg(z, nu1, nl1, nu2, nl2);
-    if (seg == 0) {
-      if (FCT) flo[e * LZ + k] = R(0);
-      adf[e * LZ + k] = R(0);
+  const bool ta_sep = a.TA != a.T;
+  for (int p = lane; 2 * p < m.LZ; p += kWarp) {
+    const int k0 = 2 * p;
+    const int z0 = k0 + 1, z1 = k0 + 2;
+    const size_t ek = (size_t)e * LZ + k0;
+    const bool a0 = k0 < m.nz && edge_seg(z0, nu1, nl1, nu2, nl2) != 0;
+    const bool a1 = k0 + 1 < m.nz && edge_seg(z1, nu1, nl1, nu2, nl2) != 0;
+    if (!a0 && !a1) {
+      for (int t = 0; t < a.K; ++t) st2(a.adfh + t * a.sE + ek, R(0), R(0));
       continue;
     }
-    const R v = a.vf[e * LZ + k];
-    const R vp = v + rabs(v), vm = v - rabs(v);
-    R lo = R(0);
-    if (FCT) {
-      lo = -(R(0.5) * (T[n1 * LZ + k] * vp + T[n2 * LZ + k] * vm));
-      flo[e * LZ + k] = lo;
-    }
-    const R ta1 = TA[n1 * LZ + k], ta2 = TA[n2 * LZ + k];
-    R ho;
-    if (HOR == 0) {
-      ho = -(R(0.5) * (ta1 * vp + ta2 * vm));
-    } else {
-      R g1, g2, g3, g4;
-      if (gm0 >= 0 && z >= gm0 && z <= gm1 - 1) {
-        elem_grad(m, g, TA, up, k, g1, g3);
-        elem_grad(m, g, TA, dn, k, g2, g4);
-      } else {
-        node_mean_grad(m, g, TA, n1, k, g1, g3);
-        node_mean_grad(m, g, TA, n2, k, g2, g4);
+    const vec2<R> vv = ld2(a.vf + ek);
+    const R v0 = vv.x, v1 = vv.y;
+    const R vp0 = v0 + rabs(v0), vm0 = v0 - rabs(v0), vp1 = v1 + rabs(v1), vm1 = v1 - rabs(v1);
+    const bool tri0 = gm0 >= 0 && z0 >= gm0 && z0 <= gm1 - 1;
+    const bool tri1 = gm0 >= 0 && z1 >= gm0 && z1 <= gm1 - 1;
+    const R c10 = (nb1 - z0 >= 0) ? R(1) : R(0), c11 = (nb1 - z1 >= 0) ? R(1) : R(0);
+    const R c20 = (nb2 - z0 >= 0) ? R(1) : R(0), c21 = (nb2 - z1 >= 0) ? R(1) : R(0);
+    for (int t = 0; t < a.K; ++t) {
+      const R* __restrict__ T = a.T + t * a.sT;
+      const R* __restrict__ TA = ta_sep ? a.TA + t * a.sTA : T;
+      const vec2<R> s1 = ld2(TA + n1 * LZ + k0), s2 = ld2(TA + n2 * LZ + k0);
+      R lo0 = R(0), lo1 = R(0);
+      if (FCT) {
+        const vec2<R> r1 = ta_sep ? ld2(T + n1 * LZ + k0) : s1;
+        const vec2<R> r2 = ta_sep ? ld2(T + n2 * LZ + k0) : s2;
+        lo0 = -(R(0.5) * (r1.x * vp0 + r2.x * vm0));
+        lo1 = -(R(0.5) * (r1.y * vp1 + r2.y * vm1));
       }
-      R Tm2, Tm1;
-      if (HOR == 1) {
-        const R c1 = (nb1 - z >= 0) ? R(1) : R(0);
-        const R c2 = (nb2 - z >= 0) ? R(1) : R(0);
-        Tm2 = ta2 - ((R(2) * (ta2 - ta1) + ex * g2 + ey * g4) / R(6)) * c2;
-        Tm1 = ta1 + ((R(2) * (ta2 - ta1) + ex * g1 + ey * g3) / R(6)) * c1;
-      } else {
-        Tm2 = ta2 - (R(2) * (ta2 - ta1) + ex * g2 + ey * g4) / R(6);
-        Tm1 = ta1 + (R(2) * (ta2 - ta1) + ex * g1 + ey * g3) / R(6);
+      R g10 = R(0), g20 = R(0), g30 = R(0), g40 = R(0), g11 = R(0), g21 = R(0), g31 = R(0), g41 = R(0);
+      if (HOR != 0) {
+        if (tri0 && tri1) {
+          const vec2<R> ua = ld2(TA + tu.a * LZ + k0), ub = ld2(TA + tu.b * LZ + k0), uc = ld2(TA + tu.c * LZ + k0);
+          const vec2<R> da = ld2(TA + td.a * LZ + k0), db = ld2(TA + td.b * LZ + k0), dc = ld2(TA + td.c * LZ + k0);
+          g10 = tu.x0 * ua.x + tu.x1 * ub.x + tu.x2 * uc.x;
+          g30 = tu.y0 * ua.x + tu.y1 * ub.x + tu.y2 * uc.x;
+          g11 = tu.x0 * ua.y + tu.x1 * ub.y + tu.x2 * uc.y;
+          g31 = tu.y0 * ua.y + tu.y1 * ub.y + tu.y2 * uc.y;
+          g20 = td.x0 * da.x + td.x1 * db.x + td.x2 * dc.x;
+          g40 = td.y0 * da.x + td.y1 * db.x + td.y2 * dc.x;
+          g21 = td.x0 * da.y + td.x1 * db.y + td.x2 * dc.y;
+          g41 = td.y0 * da.y + td.y1 * db.y + td.y2 * dc.y;
+        } else {
+          if (a0) {
+            if (tri0) {
+              tri_grad(tu, TA, LZ, k0, g10, g30);
+              tri_grad(td, TA, LZ, k0, g20, g40);
+            } else {
+              node_mean_grad(m, g, TA, n1, k0, g10, g30);
+              node_mean_grad(m, g, TA, n2, k0, g20, g40);
+            }
+          }
+          if (a1) {
+            if (tri1) {
+              tri_grad(tu, TA, LZ, k0 + 1, g11, g31);
+              tri_grad(td, TA, LZ, k0 + 1, g21, g41);
+            } else {
+              node_mean_grad(m, g, TA, n1, k0 + 1, g11, g31);
+              node_mean_grad(m, g, TA, n2, k0 + 1, g21, g41);
+            }
+          }
+        }
       }
-      const R cHO = vp * Tm1 + vm * Tm2;
-      ho = -((R(0.5) * (R(1) - ph)) * cHO) - ((v * ph) * R(0.5)) * (Tm1 + Tm2);
+      const R h0 = ho_flux<R, HOR>(v0, vp0, vm0, s1.x, s2.x, g10, g20, g30, g40, ex, ey, c10, c20, ph);
+      const R h1 = ho_flux<R, HOR>(v1, vp1, vm1, s1.y, s2.y, g11, g21, g31, g41, ex, ey, c11, c21, ph);
+      st2(a.adfh + t * a.sE + ek, a0 ? (FCT ? h0 - lo0 : h0) : R(0), a1 ? (FCT ? h1 - lo1 : h1) : R(0));
     }
-    adf[e * LZ + k] = FCT ? ho - lo : ho;
   }
 }
 
@@ -376,27 +476,75 @@ __device__ __forceinline__ void column_ver_flux(Col<R>& c, R* tvbuf, const R* fo
 }
 
 // ---------------------------------------------------------------------------
-// FCT stage 1 (node columns): low-order solution fct_LO
-// (lib/oce_adv_tra_driver.F90:91-235) and the vertical antidiffusive flux
-// HO(T_AB, w) - LO(T, w_e).
+// Node-column kernels. One warp per node, two layers per lane; tracers are
+// processed KC at a time. The node's incident edges (ascending edge index,
+// the reference's scatter order) and its FCT cluster are staged once in
+// shared memory; gathers run edge-outer, tracer-inner, so every edge's
+// metadata is read once and the loads of all KC tracers are in flight
+// together. Per-(tracer, layer) summation order is the reference's.
 // ---------------------------------------------------------------------------
-template <typename R, int VER>
+struct Nbr {
+  int e, role, other, lo, hi;
+};
+constexpr int kMaxDeg = 16;  // incident edges staged per node; more are read from global memory
+constexpr int kMaxCl = 24;   // cluster nodes staged per node
+
+__device__ __forceinline__ Nbr nbr_global(const DMesh& m, int j) {
+  const int code = m.ne_code[j];
+  return Nbr{code >> 1, code & 1, m.ne_other[j], m.ne_lo[j], m.ne_hi[j]};
+}
+
+struct NbrList {
+  const Nbr* s;
+  int j0, deg;
+  __device__ __forceinline__ Nbr get(const DMesh& m, int j) const {
+    return deg <= kMaxDeg ? s[j] : nbr_global(m, j0 + j);
+  }
+};
+
+__device__ __forceinline__ NbrList stage_nbrs(const DMesh& m, int n, Nbr* s, int lane) {
+  NbrList L{s, m.ne_ptr[n], m.ne_ptr[n + 1] - m.ne_ptr[n]};
+  if (L.deg <= kMaxDeg)
+    for (int j = lane; j < L.deg; j += kWarp) s[j] = nbr_global(m, L.j0 + j);
+  return L;
+}
+
+// Shared memory of one warp: `slices` columns of LW values, the edge list and
+// `extra_bytes` more.
+template <typename R>
+__host__ __device__ constexpr size_t warp_smem(int slices, int LW, int extra_bytes) {
+  return ((size_t)slices * LW * sizeof(R) + kMaxDeg * sizeof(Nbr) + extra_bytes + 15) / 16 * 16;
+}
+__host__ __device__ constexpr int lo_slices(int KC) { return 7 + 4 * KC; }
+__host__ __device__ constexpr int ratio_slices(int KC) { return 3 * KC; }
+__host__ __device__ constexpr int upd_slices(int KC) { return 3 * KC; }
+__host__ __device__ constexpr int nofct_slices(int KC) { return 7 + 3 * KC; }
+constexpr int kClBytes = kMaxCl * 2 * (int)sizeof(int);
+
+// ---------------------------------------------------------------------------
+// FCT stage 1: low-order solution fct_LO (lib/oce_adv_tra_driver.F90:91-235)
+// and the vertical antidiffusive flux HO(T_AB, w) - LO(T, w_e). The low-order
+// horizontal edge fluxes are formed here from T and the edge volume fluxes,
+// with the expression adv_tra_hor_upw1 uses (lib/oce_adv_tra_hor.F90:218-220).
+// ---------------------------------------------------------------------------
+template <typename R, int VER, int KC>
 __global__ void k_fct_lo(DMesh m, StepPtrs<R> a) {
-  extern __shared__ unsigned char smem_raw[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kWarp - 1), wib = threadIdx.x / kWarp;
   const int n = blockIdx.x * (blockDim.x / kWarp) + wib;
   if (n >= m.N) return;
-  const int t = blockIdx.y;
   const GeoPtrs<R>& g = GeoSel<R>::get(m);
   const size_t LZ = m.LZ, LW = m.LW;
   const int nl = m.nl, nz = m.nz;
-  ColSmem<R> sm{reinterpret_cast<R*>(smem_raw) + (size_t)wib * 10 * LW, (int)LW};
-  R *sT = sm.slice(0), *sTA = sm.slice(1), *sW = sm.slice(2), *sWE = sm.slice(3), *sA = sm.slice(4);
-  R *sHn = sm.slice(5), *sHnn = sm.slice(6), *sFlo = sm.slice(7), *sX = sm.slice(8), *sZ = sm.slice(9);
-  const R* __restrict__ T = a.T + t * a.sT + n * LZ;
-  const R* __restrict__ TA = a.TA + t * a.sTA + n * LZ;
-  stage(sT, T, nz, lane);
-  stage(sTA, TA, nz, lane);
+  unsigned char* base = smem_raw + (size_t)wib * warp_smem<R>(lo_slices(KC), m.LW, 0);
+  R* sl = reinterpret_cast<R*>(base);
+  R *sW = sl, *sWE = sl + LW, *sA = sl + 2 * LW, *sHn = sl + 3 * LW, *sHnn = sl + 4 * LW, *sX = sl + 5 * LW;
+  R* sZ = sl + 6 * LW;
+  R* sT = sl + 7 * LW;                 // KC columns
+  R* sTA = sT + (size_t)KC * LW;       // KC columns (T_AB when it is a separate field)
+  R* sFv = sTA + (size_t)KC * LW;      // KC columns of vertical fluxes
+  R* sTv = sFv + (size_t)KC * LW;      // KC columns of PPM edge values
+  const NbrList nb = stage_nbrs(m, n, reinterpret_cast<Nbr*>(base + lo_slices(KC) * LW * sizeof(R)), lane);
   stage(sW, a.w + n * LW, nl, lane);
   stage(sWE, a.we + n * LW, nl, lane);
   stage(sA, g.area + n * LW, nl, lane);
@@ -408,202 +556,321 @@ __global__ void k_fct_lo(DMesh m, StepPtrs<R> a) {
     stage(sZ, g.Z3 + n * LZ, nz, lane);
     stage(sX, g.zbar3 + n * LW, nl, lane);
   }
-  __syncwarp();
   const int nzmin = m.ulev[n], nzmax = m.nlev[n];
-  // LO vertical flux: adv_tra_ver_upw1(we, ttf) with init zero.
-  Col<R> clo{sT, sWE, sA, sHn, sHnn, sZ, sX, nullptr};
-  column_ver_flux<R, 0>(clo, nullptr, nullptr, sFlo, nl, nzmin, nzmax, R(1), a.dt, lane);
-  // LO solution (lib/oce_adv_tra_driver.F90:202-209)
-  R* __restrict__ lo = a.lo + t * a.sN + n * LZ;
-  const R* __restrict__ flo = a.flo + t * a.sE;
+  const bool ta_sep = a.TA != a.T;
   const R dt = a.dt;
-  for (int k = lane; k < nz; k += kWarp) {
-    const int z = k + 1;
-    R acc = R(0);
-    for (int j = m.ne_ptr[n]; j < m.ne_ptr[n + 1]; ++j) {
-      if (z < m.ne_lo[j] || z > m.ne_hi[j]) continue;
-      const int code = m.ne_code[j];
-      const R f = flo[(size_t)(code >> 1) * LZ + k];
-      acc = (code & 1) ? acc - f : acc + f;
+  for (int t0 = 0; t0 < a.K; t0 += KC) {
+#pragma unroll
+    for (int i = 0; i < KC; ++i) {
+      stage(sT + i * LW, a.T + (t0 + i) * a.sT + n * LZ, nz, lane);
+      if (ta_sep) stage(sTA + i * LW, a.TA + (t0 + i) * a.sTA + n * LZ, nz, lane);
     }
-    R v = acc;
-    if (z >= nzmin && z <= nzmax - 1)
-      v = (sT[k] * g.hnode[n * LZ + k] + ((acc + (sFlo[k] - sFlo[k + 1])) * dt) / g.areasvol[n * LZ + k]) /
-          g.hnode_new[n * LZ + k];
-    lo[k] = v;
-  }
-  __syncwarp();  // every lane has read the LO fluxes before they are overwritten
-  // HO vertical flux on T_AB with w; adf_v = HO - LO ("X - flux").
-  Col<R> cho{sTA, sW, sA, sHn, sHnn, sZ, sX, nullptr};
-  R* tvbuf = sm.slice(9);  // PPM edge values reuse the Z_3d_n slice (QR4C only)
-  R* __restrict__ adfv = a.adfv + t * a.sW + n * LW;
-  column_ver_flux<R, VER>(cho, tvbuf, sFlo, sFlo, nl, nzmin, nzmax, a.pv, dt, lane);
-  for (int iz = lane; iz < (int)LW; iz += kWarp) adfv[iz] = iz < nl ? sFlo[iz] : R(0);
-}
-
-// ---------------------------------------------------------------------------
-// FCT stage 2 (node columns): bounds a1-a3, antidiffusive sums b1 and the
-// limiting factors b2 (lib/oce_adv_tra_fct.F90:98-374).
-// ---------------------------------------------------------------------------
-template <typename R>
-__global__ void k_fct_ratio(DMesh m, StepPtrs<R> a) {
-  extern __shared__ unsigned char smem_raw[];
-  const int lane = threadIdx.x & (kWarp - 1), wib = threadIdx.x / kWarp;
-  const int n = blockIdx.x * (blockDim.x / kWarp) + wib;
-  if (n >= m.N) return;
-  const int t = blockIdx.y;
-  const GeoPtrs<R>& g = GeoSel<R>::get(m);
-  const size_t LZ = m.LZ, LW = m.LW;
-  const int nz = m.nz;
-  R* smax = reinterpret_cast<R*>(smem_raw) + (size_t)wib * 3 * LW;
-  R* smin = smax + LW;
-  R* sadv = smin + LW;
-  const R* __restrict__ T = a.T + t * a.sT;
-  const R* __restrict__ LO = a.lo + t * a.sN;
-  const int nzmin = m.ulev[n], nzmax = m.nlev[n];
-  const int c0 = m.cl_ptr[n], c1 = m.cl_ptr[n + 1], minlev = m.cl_minlev[n];
-  const R big = R(1e3);
-  for (int k = lane; k < nz; k += kWarp) {
-    const int z = k + 1;
-    R mx = -big, mn = big;
-    bool any = z > minlev;  // some element of the cluster lacks layer z: AUX = -/+1e3
-    for (int j = c0; j < c1; ++j) {
-      if (z > m.cl_lev[j]) continue;
-      const size_t v = (size_t)m.cl_node[j] * LZ + k;
-      const R lv = LO[v], tv = T[v];
-      const R hi = rmax(lv, tv), lw = rmin(lv, tv);
-      if (!any) {
-        mx = hi;
-        mn = lw;
-        any = true;
-      } else {
-        mx = rmax(mx, hi);
-        mn = rmin(mn, lw);
+    __syncwarp();
+    // LO vertical flux: adv_tra_ver_upw1(we, ttf) with init zero.
+    for (int i = 0; i < KC; ++i) {
+      Col<R> clo{sT + i * LW, sWE, sA, sHn, sHnn, sZ, sX, nullptr};
+      column_ver_flux<R, 0>(clo, nullptr, nullptr, sFv + i * LW, nl, nzmin, nzmax, R(1), dt, lane);
+    }
+    for (int p = lane; 2 * p < m.LZ; p += kWarp) {
+      const int k0 = 2 * p, z0 = k0 + 1, z1 = k0 + 2;
+      R acc0[KC], acc1[KC];
+#pragma unroll
+      for (int i = 0; i < KC; ++i) acc0[i] = acc1[i] = R(0);
+      for (int j = 0; j < nb.deg; ++j) {
+        const Nbr q = nb.get(m, j);
+        const bool a0 = z0 >= q.lo && z0 <= q.hi, a1 = z1 >= q.lo && z1 <= q.hi;
+        const vec2<R> vv = ld2(a.vf + (size_t)q.e * LZ + k0);
+        const R vp0 = vv.x + rabs(vv.x), vm0 = vv.x - rabs(vv.x);
+        const R vp1 = vv.y + rabs(vv.y), vm1 = vv.y - rabs(vv.y);
+#pragma unroll
+        for (int i = 0; i < KC; ++i) {
+          const vec2<R> to = ld2(a.T + (t0 + i) * a.sT + (size_t)q.other * LZ + k0);
+          const R tn0 = sT[i * LW + k0], tn1 = sT[i * LW + k0 + 1];
+          if (q.role) {  // this node is the edge's second node
+            if (a0) acc0[i] = acc0[i] - (-(R(0.5) * (to.x * vp0 + tn0 * vm0)));
+            if (a1) acc1[i] = acc1[i] - (-(R(0.5) * (to.y * vp1 + tn1 * vm1)));
+          } else {
+            if (a0) acc0[i] = acc0[i] + (-(R(0.5) * (tn0 * vp0 + to.x * vm0)));
+            if (a1) acc1[i] = acc1[i] + (-(R(0.5) * (tn1 * vp1 + to.y * vm1)));
+          }
+        }
+      }
+      const vec2<R> hn = ld2(g.hnode + n * LZ + k0), hnn = ld2(g.hnode_new + n * LZ + k0);
+      const vec2<R> av = ld2(g.areasvol + n * LZ + k0);
+      const bool w0 = z0 >= nzmin && z0 <= nzmax - 1, w1 = z1 >= nzmin && z1 <= nzmax - 1;
+#pragma unroll
+      for (int i = 0; i < KC; ++i) {
+        const R* Ti = sT + i * LW;
+        const R* Fi = sFv + i * LW;
+        R l0 = acc0[i], l1 = acc1[i];
+        if (w0) l0 = (Ti[k0] * hn.x + ((acc0[i] + (Fi[k0] - Fi[k0 + 1])) * dt) / av.x) / hnn.x;
+        if (w1) l1 = (Ti[k0 + 1] * hn.y + ((acc1[i] + (Fi[k0 + 1] - Fi[k0 + 2])) * dt) / av.y) / hnn.y;
+        st2(a.lo + (t0 + i) * a.sN + n * LZ + k0, l0, l1);
       }
     }
-    smax[k] = mx;
-    smin[k] = mn;
-  }
-  stage(sadv, a.adfv + t * a.sW + n * LW, m.nl, lane);
-  __syncwarp();
-  const R* __restrict__ adfh = a.adfh + t * a.sE;
-  R* __restrict__ rp = a.rp + t * a.sN + n * LZ;
-  R* __restrict__ rm = a.rm + t * a.sN + n * LZ;
-  const R dt = a.dt;
-  for (int k = lane; k < nz; k += kWarp) {
-    const int z = k + 1;
-    if (z < nzmin || z > nzmax - 1) continue;
-    const R lo = LO[n * LZ + k];
-    R bmax, bmin;
-    if (z == nzmax - 1 || z == nzmin) {
-      bmax = smax[k] - lo;
-      bmin = smin[k] - lo;
-    } else {
-      bmax = rmax(rmax(smax[k - 1], smax[k]), smax[k + 1]) - lo;
-      bmin = rmin(rmin(smin[k - 1], smin[k]), smin[k + 1]) - lo;
+    __syncwarp();  // every lane has read the LO fluxes before they are overwritten
+    // HO vertical flux on T_AB with w; adf_v = HO - LO ("X - flux").
+    for (int i = 0; i < KC; ++i) {
+      Col<R> cho{(ta_sep ? sTA : sT) + i * LW, sW, sA, sHn, sHnn, sZ, sX, nullptr};
+      column_ver_flux<R, VER>(cho, sTv + i * LW, sFv + i * LW, sFv + i * LW, nl, nzmin, nzmax, a.pv, dt, lane);
+      R* __restrict__ adfv = a.adfv + (t0 + i) * a.sW + n * LW;
+      for (int iz = lane; iz < (int)LW; iz += kWarp) adfv[iz] = iz < nl ? sFv[i * LW + iz] : R(0);
     }
-    R plus = R(0) + (rmax(R(0), sadv[k]) + rmax(R(0), -sadv[k + 1]));
-    R minus = R(0) + (rmin(R(0), sadv[k]) + rmin(R(0), -sadv[k + 1]));
-    for (int j = m.ne_ptr[n]; j < m.ne_ptr[n + 1]; ++j) {
-      if (z < m.ne_lo[j] || z > m.ne_hi[j]) continue;
-      const int code = m.ne_code[j];
-      R f = adfh[(size_t)(code >> 1) * LZ + k];
-      if (code & 1) f = -f;
-      plus = plus + rmax(R(0), f);
-      minus = minus + rmin(R(0), f);
-    }
-    const R av = g.areasvol[n * LZ + k];
-    R flux = (plus * dt) / av + R(1e-16);
-    rp[k] = rmin(R(1), bmax / flux);
-    flux = (minus * dt) / av - R(1e-16);
-    rm[k] = rmin(R(1), bmin / flux);
+    __syncwarp();
   }
 }
 
 // ---------------------------------------------------------------------------
-// FCT stage 3 (node columns): limiting b3 (lib/oce_adv_tra_fct.F90:396-471),
-// flux divergence (oce_tra_adv_flux2dtracer with use_lo,
-// lib/oce_adv_tra_driver.F90:298-450) and the caller's tendency update
-// (src/fesom_analytic.F90:419-437 or lib/tracer_c_interface.F90:194-214).
+// FCT stage 2: bounds a1-a3, antidiffusive sums b1 and the limiting factors
+// b2 (lib/oce_adv_tra_fct.F90:98-374). The cluster bound is the maximum over
+// the cluster's elements of the maximum over their nodes; max is exact, so
+// the distinct nodes with the deepest layer reaching them give the same value.
 // ---------------------------------------------------------------------------
-template <typename R>
-__global__ void k_fct_update(DMesh m, StepPtrs<R> a) {
-  extern __shared__ unsigned char smem_raw[];
+template <typename R, int KC>
+__global__ void k_fct_ratio(DMesh m, StepPtrs<R> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kWarp - 1), wib = threadIdx.x / kWarp;
   const int n = blockIdx.x * (blockDim.x / kWarp) + wib;
   if (n >= m.N) return;
-  const int t = blockIdx.y;
+  const GeoPtrs<R>& g = GeoSel<R>::get(m);
+  const size_t LZ = m.LZ, LW = m.LW;
+  unsigned char* base = smem_raw + (size_t)wib * warp_smem<R>(ratio_slices(KC), m.LW, kClBytes);
+  R* smax = reinterpret_cast<R*>(base);
+  R* smin = smax + (size_t)KC * LW;
+  R* sadv = smin + (size_t)KC * LW;
+  const NbrList nb = stage_nbrs(m, n, reinterpret_cast<Nbr*>(base + ratio_slices(KC) * LW * sizeof(R)), lane);
+  int* scl = reinterpret_cast<int*>(base + ratio_slices(KC) * LW * sizeof(R) + kMaxDeg * sizeof(Nbr));
+  const int c0 = m.cl_ptr[n], ncl = m.cl_ptr[n + 1] - c0, minlev = m.cl_minlev[n];
+  const bool cl_staged = ncl <= kMaxCl;
+  if (cl_staged)
+    for (int j = lane; j < ncl; j += kWarp) {
+      scl[2 * j] = m.cl_node[c0 + j];
+      scl[2 * j + 1] = m.cl_lev[c0 + j];
+    }
+  const int nzmin = m.ulev[n], nzmax = m.nlev[n];
+  const R big = R(1e3), dt = a.dt;
+  const R inf = R(INFINITY);
+  for (int t0 = 0; t0 < a.K; t0 += KC) {
+#pragma unroll
+    for (int i = 0; i < KC; ++i) stage(sadv + i * LW, a.adfv + (t0 + i) * a.sW + n * LW, m.nl, lane);
+    __syncwarp();
+    for (int p = lane; 2 * p < m.LZ; p += kWarp) {
+      const int k0 = 2 * p, z0 = k0 + 1, z1 = k0 + 2;
+      // AUX = -/+1e3 of elements without the layer joins the bound (lib/oce_adv_tra_fct.F90:139-145)
+      const R mx0i = z0 > minlev ? -big : -inf, mx1i = z1 > minlev ? -big : -inf;
+      R mx0[KC], mx1[KC], mn0[KC], mn1[KC];
+#pragma unroll
+      for (int i = 0; i < KC; ++i) {
+        mx0[i] = mx0i;
+        mx1[i] = mx1i;
+        mn0[i] = -mx0i;
+        mn1[i] = -mx1i;
+      }
+      for (int j = 0; j < ncl; ++j) {
+        const int node = cl_staged ? scl[2 * j] : m.cl_node[c0 + j];
+        const int lev = cl_staged ? scl[2 * j + 1] : m.cl_lev[c0 + j];
+        const bool a0 = z0 <= lev, a1 = z1 <= lev;
+#pragma unroll
+        for (int i = 0; i < KC; ++i) {
+          const size_t v = (size_t)node * LZ + k0;
+          const vec2<R> lv = ld2(a.lo + (t0 + i) * a.sN + v), tv = ld2(a.T + (t0 + i) * a.sT + v);
+          if (a0) {
+            mx0[i] = rmax(mx0[i], rmax(lv.x, tv.x));
+            mn0[i] = rmin(mn0[i], rmin(lv.x, tv.x));
+          }
+          if (a1) {
+            mx1[i] = rmax(mx1[i], rmax(lv.y, tv.y));
+            mn1[i] = rmin(mn1[i], rmin(lv.y, tv.y));
+          }
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < KC; ++i) {
+        smax[i * LW + k0] = mx0[i];
+        smax[i * LW + k0 + 1] = mx1[i];
+        smin[i * LW + k0] = mn0[i];
+        smin[i * LW + k0 + 1] = mn1[i];
+      }
+    }
+    __syncwarp();
+    for (int p = lane; 2 * p < m.LZ; p += kWarp) {
+      const int k0 = 2 * p;
+      R pl0[KC], pl1[KC], mi0[KC], mi1[KC];
+#pragma unroll
+      for (int i = 0; i < KC; ++i) {
+        const R* ad = sadv + i * LW;
+        pl0[i] = R(0) + (rmax(R(0), ad[k0]) + rmax(R(0), -ad[k0 + 1]));
+        mi0[i] = R(0) + (rmin(R(0), ad[k0]) + rmin(R(0), -ad[k0 + 1]));
+        pl1[i] = R(0) + (rmax(R(0), ad[k0 + 1]) + rmax(R(0), -ad[k0 + 2]));
+        mi1[i] = R(0) + (rmin(R(0), ad[k0 + 1]) + rmin(R(0), -ad[k0 + 2]));
+      }
+      const int z0 = k0 + 1, z1 = k0 + 2;
+      for (int j = 0; j < nb.deg; ++j) {
+        const Nbr q = nb.get(m, j);
+        const bool a0 = z0 >= q.lo && z0 <= q.hi, a1 = z1 >= q.lo && z1 <= q.hi;
+#pragma unroll
+        for (int i = 0; i < KC; ++i) {
+          vec2<R> f = ld2(a.adfh + (t0 + i) * a.sE + (size_t)q.e * LZ + k0);
+          if (q.role) {
+            f.x = -f.x;
+            f.y = -f.y;
+          }
+          if (a0) {
+            pl0[i] = pl0[i] + rmax(R(0), f.x);
+            mi0[i] = mi0[i] + rmin(R(0), f.x);
+          }
+          if (a1) {
+            pl1[i] = pl1[i] + rmax(R(0), f.y);
+            mi1[i] = mi1[i] + rmin(R(0), f.y);
+          }
+        }
+      }
+      const vec2<R> av = ld2(g.areasvol + n * LZ + k0);
+#pragma unroll
+      for (int i = 0; i < KC; ++i) {
+        const R* mxs = smax + i * LW;
+        const R* mns = smin + i * LW;
+        const vec2<R> lo = ld2(a.lo + (t0 + i) * a.sN + n * LZ + k0);
+        R out_p[2] = {R(0), R(0)}, out_m[2] = {R(0), R(0)};
+#pragma unroll
+        for (int l = 0; l < 2; ++l) {
+          const int k = k0 + l, z = k + 1;
+          if (z < nzmin || z > nzmax - 1) continue;
+          const R lov = l ? lo.y : lo.x;
+          R bmax, bmin;
+          if (z == nzmax - 1 || z == nzmin) {
+            bmax = mxs[k] - lov;
+            bmin = mns[k] - lov;
+          } else {
+            bmax = rmax(rmax(mxs[k - 1], mxs[k]), mxs[k + 1]) - lov;
+            bmin = rmin(rmin(mns[k - 1], mns[k]), mns[k + 1]) - lov;
+          }
+          const R avk = l ? av.y : av.x;
+          R flux = ((l ? pl1[i] : pl0[i]) * dt) / avk + R(1e-16);
+          out_p[l] = rmin(R(1), bmax / flux);
+          flux = ((l ? mi1[i] : mi0[i]) * dt) / avk - R(1e-16);
+          out_m[l] = rmin(R(1), bmin / flux);
+        }
+        st2(a.rp + (t0 + i) * a.sN + n * LZ + k0, out_p[0], out_p[1]);
+        st2(a.rm + (t0 + i) * a.sN + n * LZ + k0, out_m[0], out_m[1]);
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FCT stage 3: limiting b3 (lib/oce_adv_tra_fct.F90:396-471), flux divergence
+// (oce_tra_adv_flux2dtracer with use_lo, lib/oce_adv_tra_driver.F90:298-450)
+// and the caller's tendency update (src/fesom_analytic.F90:419-437 or, with a
+// persistent del_ttf, lib/tracer_c_interface.F90:194-214).
+// ---------------------------------------------------------------------------
+template <typename R, int KC>
+__global__ void k_fct_update(DMesh m, StepPtrs<R> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & (kWarp - 1), wib = threadIdx.x / kWarp;
+  const int n = blockIdx.x * (blockDim.x / kWarp) + wib;
+  if (n >= m.N) return;
   const GeoPtrs<R>& g = GeoSel<R>::get(m);
   const size_t LZ = m.LZ, LW = m.LW;
   const int nz = m.nz, nl = m.nl;
-  R* sLv = reinterpret_cast<R*>(smem_raw) + (size_t)wib * 3 * LW;
-  R* sRp = sLv + LW;
-  R* sRm = sRp + LW;
-  const R* __restrict__ rp = a.rp + t * a.sN;
-  const R* __restrict__ rm = a.rm + t * a.sN;
-  stage(sRp, rp + n * LZ, nz, lane);
-  stage(sRm, rm + n * LZ, nz, lane);
-  const R* __restrict__ adfv = a.adfv + t * a.sW + n * LW;
-  __syncwarp();
+  unsigned char* base = smem_raw + (size_t)wib * warp_smem<R>(upd_slices(KC), m.LW, 0);
+  R* sLv = reinterpret_cast<R*>(base);
+  R* sRp = sLv + (size_t)KC * LW;
+  R* sRm = sRp + (size_t)KC * LW;
+  const NbrList nb = stage_nbrs(m, n, reinterpret_cast<Nbr*>(base + upd_slices(KC) * LW * sizeof(R)), lane);
   const int nzmin = m.ulev[n], nzmax = m.nlev[n];
-  for (int iz = lane; iz < nl; iz += kWarp) {
-    const int z = iz + 1;
-    R f = adfv[iz];
-    if (z == nzmin) {
-      R ae = R(1);
-      ae = (f >= R(0)) ? rmin(ae, sRp[iz]) : rmin(ae, sRm[iz]);
-      f = ae * f;
-    } else if (z > nzmin && z <= nzmax - 1) {
-      R ae = R(1);
-      if (f >= R(0)) {
-        ae = rmin(ae, sRm[iz - 1]);
-        ae = rmin(ae, sRp[iz]);
-      } else {
-        ae = rmin(ae, sRp[iz - 1]);
-        ae = rmin(ae, sRm[iz]);
-      }
-      f = ae * f;
-    }
-    sLv[iz] = f;
-  }
-  __syncwarp();
-  R* __restrict__ T = a.T + t * a.sT + n * LZ;
-  const R* __restrict__ LO = a.lo + t * a.sN + n * LZ;
-  const R* __restrict__ adfh = a.adfh + t * a.sE;
-  R* __restrict__ del = a.del ? a.del + t * a.sN + n * LZ : nullptr;
-  R* __restrict__ TAo = a.TAout ? a.TAout + t * a.sTA + n * LZ : nullptr;
   const R dt = a.dt;
-  for (int k = lane; k < nz; k += kWarp) {
-    const int z = k + 1;
-    if (z < nzmin || z > nzmax - 1) continue;
-    const R av = g.areasvol[n * LZ + k];
-    const R Tn = T[k];
-    R dv = (R(0) - Tn * g.hnode[n * LZ + k]) + LO[k] * g.hnode_new[n * LZ + k];
-    dv = dv + ((sLv[k] - sLv[k + 1]) * dt) / av;
-    R dh = R(0);
-    const R rpn = sRp[k], rmn = sRm[k];
-    for (int j = m.ne_ptr[n]; j < m.ne_ptr[n + 1]; ++j) {
-      if (z < m.ne_lo[j] || z > m.ne_hi[j]) continue;
-      const int code = m.ne_code[j];
-      const R f = adfh[(size_t)(code >> 1) * LZ + k];
-      const size_t o = (size_t)m.ne_other[j] * LZ + k;
-      R ae = R(1);
-      if (code & 1) {  // this node is the edge's second node
-        if (f >= R(0)) { ae = rmin(ae, rp[o]); ae = rmin(ae, rmn); }
-        else { ae = rmin(ae, rm[o]); ae = rmin(ae, rpn); }
-        dh = dh - ((ae * f) * dt) / av;
-      } else {
-        if (f >= R(0)) { ae = rmin(ae, rpn); ae = rmin(ae, rm[o]); }
-        else { ae = rmin(ae, rmn); ae = rmin(ae, rp[o]); }
-        dh = dh + ((ae * f) * dt) / av;
+  for (int t0 = 0; t0 < a.K; t0 += KC) {
+#pragma unroll
+    for (int i = 0; i < KC; ++i) {
+      stage(sRp + i * LW, a.rp + (t0 + i) * a.sN + n * LZ, nz, lane);
+      stage(sRm + i * LW, a.rm + (t0 + i) * a.sN + n * LZ, nz, lane);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < KC; ++i) {
+      const R* __restrict__ adfv = a.adfv + (t0 + i) * a.sW + n * LW;
+      const R* Rp = sRp + i * LW;
+      const R* Rm = sRm + i * LW;
+      for (int iz = lane; iz < nl; iz += kWarp) {
+        const int z = iz + 1;
+        R f = adfv[iz];
+        if (z == nzmin) {
+          R ae = R(1);
+          ae = (f >= R(0)) ? rmin(ae, Rp[iz]) : rmin(ae, Rm[iz]);
+          f = ae * f;
+        } else if (z > nzmin && z <= nzmax - 1) {
+          R ae = R(1);
+          if (f >= R(0)) {
+            ae = rmin(ae, Rm[iz - 1]);
+            ae = rmin(ae, Rp[iz]);
+          } else {
+            ae = rmin(ae, Rp[iz - 1]);
+            ae = rmin(ae, Rm[iz]);
+          }
+          f = ae * f;
+        }
+        sLv[i * LW + iz] = f;
       }
     }
-    R d = del ? del[k] : R(0);
-    d = d + dh + dv;
-    if (del) del[k] = d;
-    const R tn = Tn + d / g.hnode_new[n * LZ + k];
-    T[k] = tn;
-    if (TAo) TAo[k] = tn;
+    __syncwarp();
+    for (int p = lane; 2 * p < m.LZ; p += kWarp) {
+      const int k0 = 2 * p, z0 = k0 + 1, z1 = k0 + 2;
+      const vec2<R> av = ld2(g.areasvol + n * LZ + k0);
+      R dh0[KC], dh1[KC];
+#pragma unroll
+      for (int i = 0; i < KC; ++i) dh0[i] = dh1[i] = R(0);
+      for (int j = 0; j < nb.deg; ++j) {
+        const Nbr q = nb.get(m, j);
+        const bool a0 = z0 >= q.lo && z0 <= q.hi, a1 = z1 >= q.lo && z1 <= q.hi;
+        const size_t o = (size_t)q.other * LZ + k0;
+#pragma unroll
+        for (int i = 0; i < KC; ++i) {
+          const vec2<R> f = ld2(a.adfh + (t0 + i) * a.sE + (size_t)q.e * LZ + k0);
+          const vec2<R> rpo = ld2(a.rp + (t0 + i) * a.sN + o), rmo = ld2(a.rm + (t0 + i) * a.sN + o);
+          const R rpn0 = sRp[i * LW + k0], rpn1 = sRp[i * LW + k0 + 1];
+          const R rmn0 = sRm[i * LW + k0], rmn1 = sRm[i * LW + k0 + 1];
+          R ae0 = R(1), ae1 = R(1);
+          if (q.role) {  // this node is the edge's second node
+            if (f.x >= R(0)) { ae0 = rmin(ae0, rpo.x); ae0 = rmin(ae0, rmn0); }
+            else { ae0 = rmin(ae0, rmo.x); ae0 = rmin(ae0, rpn0); }
+            if (f.y >= R(0)) { ae1 = rmin(ae1, rpo.y); ae1 = rmin(ae1, rmn1); }
+            else { ae1 = rmin(ae1, rmo.y); ae1 = rmin(ae1, rpn1); }
+            if (a0) dh0[i] = dh0[i] - ((ae0 * f.x) * dt) / av.x;
+            if (a1) dh1[i] = dh1[i] - ((ae1 * f.y) * dt) / av.y;
+          } else {
+            if (f.x >= R(0)) { ae0 = rmin(ae0, rpn0); ae0 = rmin(ae0, rmo.x); }
+            else { ae0 = rmin(ae0, rmn0); ae0 = rmin(ae0, rpo.x); }
+            if (f.y >= R(0)) { ae1 = rmin(ae1, rpn1); ae1 = rmin(ae1, rmo.y); }
+            else { ae1 = rmin(ae1, rmn1); ae1 = rmin(ae1, rpo.y); }
+            if (a0) dh0[i] = dh0[i] + ((ae0 * f.x) * dt) / av.x;
+            if (a1) dh1[i] = dh1[i] + ((ae1 * f.y) * dt) / av.y;
+          }
+        }
+      }
+      const vec2<R> hn = ld2(g.hnode + n * LZ + k0), hnn = ld2(g.hnode_new + n * LZ + k0);
+      const bool w0 = z0 >= nzmin && z0 <= nzmax - 1, w1 = z1 >= nzmin && z1 <= nzmax - 1;
+#pragma unroll
+      for (int i = 0; i < KC; ++i) {
+        R* __restrict__ T = a.T + (t0 + i) * a.sT + n * LZ + k0;
+        const vec2<R> Tn = ld2(T);
+        const vec2<R> lo = ld2(a.lo + (t0 + i) * a.sN + n * LZ + k0);
+        const R* Lv = sLv + i * LW;
+        R* del = a.del ? a.del + (t0 + i) * a.sN + n * LZ + k0 : nullptr;
+        const vec2<R> d0 = del ? ld2(del) : vec2<R>{R(0), R(0)};
+        R dv0 = (R(0) - Tn.x * hn.x) + lo.x * hnn.x;
+        dv0 = dv0 + ((Lv[k0] - Lv[k0 + 1]) * dt) / av.x;
+        R dv1 = (R(0) - Tn.y * hn.y) + lo.y * hnn.y;
+        dv1 = dv1 + ((Lv[k0 + 1] - Lv[k0 + 2]) * dt) / av.y;
+        const R e0 = d0.x + dh0[i] + dv0, e1 = d0.y + dh1[i] + dv1;
+        const R n0 = w0 ? Tn.x + e0 / hnn.x : Tn.x, n1v = w1 ? Tn.y + e1 / hnn.y : Tn.y;
+        st2(T, n0, n1v);
+        if (del) st2(del, w0 ? e0 : d0.x, w1 ? e1 : d0.y);
+        if (a.TAout) st2(a.TAout + (t0 + i) * a.sTA + n * LZ + k0, n0, n1v);
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -611,20 +878,22 @@ __global__ void k_fct_update(DMesh m, StepPtrs<R> a) {
 // Without a limiter: vertical HO flux on T_AB with w_e, flux divergence
 // (oce_tra_adv_flux2dtracer) and the tendency update in one pass.
 // ---------------------------------------------------------------------------
-template <typename R, int VER>
+template <typename R, int VER, int KC>
 __global__ void k_nofct_update(DMesh m, StepPtrs<R> a) {
-  extern __shared__ unsigned char smem_raw[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kWarp - 1), wib = threadIdx.x / kWarp;
   const int n = blockIdx.x * (blockDim.x / kWarp) + wib;
   if (n >= m.N) return;
-  const int t = blockIdx.y;
   const GeoPtrs<R>& g = GeoSel<R>::get(m);
   const size_t LZ = m.LZ, LW = m.LW;
   const int nl = m.nl, nz = m.nz;
-  ColSmem<R> sm{reinterpret_cast<R*>(smem_raw) + (size_t)wib * 10 * LW, (int)LW};
-  R *sTA = sm.slice(1), *sW = sm.slice(2), *sA = sm.slice(4);
-  R *sHn = sm.slice(5), *sHnn = sm.slice(6), *sF = sm.slice(7), *sX = sm.slice(8), *sZ = sm.slice(9);
-  stage(sTA, a.TA + t * a.sTA + n * LZ, nz, lane);
+  unsigned char* base = smem_raw + (size_t)wib * warp_smem<R>(nofct_slices(KC), m.LW, 0);
+  R* sl = reinterpret_cast<R*>(base);
+  R *sW = sl, *sA = sl + LW, *sHn = sl + 2 * LW, *sHnn = sl + 3 * LW, *sX = sl + 4 * LW, *sZ = sl + 5 * LW;
+  R* sTA = sl + 7 * LW;              // KC columns
+  R* sF = sTA + (size_t)KC * LW;     // KC columns
+  R* sTv = sF + (size_t)KC * LW;     // KC columns
+  const NbrList nb = stage_nbrs(m, n, reinterpret_cast<Nbr*>(base + nofct_slices(KC) * LW * sizeof(R)), lane);
   stage(sW, a.we + n * LW, nl, lane);
   stage(sA, g.area + n * LW, nl, lane);
   if (VER == 3) {
@@ -635,33 +904,56 @@ __global__ void k_nofct_update(DMesh m, StepPtrs<R> a) {
     stage(sZ, g.Z3 + n * LZ, nz, lane);
     stage(sX, g.zbar3 + n * LW, nl, lane);
   }
-  __syncwarp();
   const int nzmin = m.ulev[n], nzmax = m.nlev[n];
-  Col<R> c{sTA, sW, sA, sHn, sHnn, sZ, sX, nullptr};
-  column_ver_flux<R, VER>(c, sm.slice(VER == 3 ? 9 : 0), nullptr, sF, nl, nzmin, nzmax, a.pv, a.dt, lane);
-  R* __restrict__ T = a.T + t * a.sT + n * LZ;
-  const R* __restrict__ fh = a.adfh + t * a.sE;
-  R* __restrict__ del = a.del ? a.del + t * a.sN + n * LZ : nullptr;
-  R* __restrict__ TAo = a.TAout ? a.TAout + t * a.sTA + n * LZ : nullptr;
   const R dt = a.dt;
-  for (int k = lane; k < nz; k += kWarp) {
-    const int z = k + 1;
-    if (z < nzmin || z > nzmax - 1) continue;
-    const R av = g.areasvol[n * LZ + k];
-    const R dv = R(0) + ((sF[k] - sF[k + 1]) * dt) / av;
-    R dh = R(0);
-    for (int j = m.ne_ptr[n]; j < m.ne_ptr[n + 1]; ++j) {
-      if (z < m.ne_lo[j] || z > m.ne_hi[j]) continue;
-      const int code = m.ne_code[j];
-      const R f = fh[(size_t)(code >> 1) * LZ + k];
-      dh = (code & 1) ? dh - (f * dt) / av : dh + (f * dt) / av;
+  for (int t0 = 0; t0 < a.K; t0 += KC) {
+#pragma unroll
+    for (int i = 0; i < KC; ++i) stage(sTA + i * LW, a.TA + (t0 + i) * a.sTA + n * LZ, nz, lane);
+    __syncwarp();
+    for (int i = 0; i < KC; ++i) {
+      Col<R> c{sTA + i * LW, sW, sA, sHn, sHnn, sZ, sX, nullptr};
+      column_ver_flux<R, VER>(c, sTv + i * LW, nullptr, sF + i * LW, nl, nzmin, nzmax, a.pv, dt, lane);
     }
-    R d = del ? del[k] : R(0);
-    d = d + dh + dv;
-    if (del) del[k] = d;
-    const R tn = T[k] + d / g.hnode_new[n * LZ + k];
-    T[k] = tn;
-    if (TAo) TAo[k] = tn;
+    for (int p = lane; 2 * p < m.LZ; p += kWarp) {
+      const int k0 = 2 * p, z0 = k0 + 1, z1 = k0 + 2;
+      const vec2<R> av = ld2(g.areasvol + n * LZ + k0);
+      R dh0[KC], dh1[KC];
+#pragma unroll
+      for (int i = 0; i < KC; ++i) dh0[i] = dh1[i] = R(0);
+      for (int j = 0; j < nb.deg; ++j) {
+        const Nbr q = nb.get(m, j);
+        const bool a0 = z0 >= q.lo && z0 <= q.hi, a1 = z1 >= q.lo && z1 <= q.hi;
+#pragma unroll
+        for (int i = 0; i < KC; ++i) {
+          const vec2<R> f = ld2(a.adfh + (t0 + i) * a.sE + (size_t)q.e * LZ + k0);
+          if (q.role) {
+            if (a0) dh0[i] = dh0[i] - (f.x * dt) / av.x;
+            if (a1) dh1[i] = dh1[i] - (f.y * dt) / av.y;
+          } else {
+            if (a0) dh0[i] = dh0[i] + (f.x * dt) / av.x;
+            if (a1) dh1[i] = dh1[i] + (f.y * dt) / av.y;
+          }
+        }
+      }
+      const vec2<R> hnn = ld2(g.hnode_new + n * LZ + k0);
+      const bool w0 = z0 >= nzmin && z0 <= nzmax - 1, w1 = z1 >= nzmin && z1 <= nzmax - 1;
+#pragma unroll
+      for (int i = 0; i < KC; ++i) {
+        const R* F = sF + i * LW;
+        R* __restrict__ T = a.T + (t0 + i) * a.sT + n * LZ + k0;
+        const vec2<R> Tn = ld2(T);
+        R* del = a.del ? a.del + (t0 + i) * a.sN + n * LZ + k0 : nullptr;
+        const vec2<R> d0 = del ? ld2(del) : vec2<R>{R(0), R(0)};
+        const R dv0 = R(0) + ((F[k0] - F[k0 + 1]) * dt) / av.x;
+        const R dv1 = R(0) + ((F[k0 + 1] - F[k0 + 2]) * dt) / av.y;
+        const R e0 = d0.x + dh0[i] + dv0, e1 = d0.y + dh1[i] + dv1;
+        const R n0 = w0 ? Tn.x + e0 / hnn.x : Tn.x, n1v = w1 ? Tn.y + e1 / hnn.y : Tn.y;
+        st2(T, n0, n1v);
+        if (del) st2(del, w0 ? e0 : d0.x, w1 ? e1 : d0.y);
+        if (a.TAout) st2(a.TAout + (t0 + i) * a.sTA + n * LZ + k0, n0, n1v);
+      }
+    }
+    __syncwarp();
   }
 }
 

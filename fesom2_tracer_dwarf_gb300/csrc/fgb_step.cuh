@@ -22,7 +22,7 @@ WorkspaceLayout workspace_layout(const DMesh& m, int K) {
   auto al = [](long long b) { return (b + 255) / 256 * 256; };
   long long off = 0;
   w.off[0] = off; off += al(E * LZ * s);          // vf
-  w.off[1] = off; off += al((long long)K * E * LZ * s);  // flo
+  w.off[1] = off;                                         // (unused slot)
   w.off[2] = off; off += al((long long)K * E * LZ * s);  // adfh
   w.off[3] = off; off += al((long long)K * N * LZ * s);  // lo
   w.off[4] = off; off += al((long long)K * N * LW * s);  // adfv
@@ -33,24 +33,69 @@ WorkspaceLayout workspace_layout(const DMesh& m, int K) {
 }
 
 template <typename R, int HOR>
-void launch_hflux(const DMesh& m, const StepPtrs<R>& a, bool fct, int K, cudaStream_t s) {
-  dim3 grid((m.E + kEdgeWarps - 1) / kEdgeWarps, K), block(kEdgeWarps * kWarp);
+void launch_hflux(const DMesh& m, const StepPtrs<R>& a, bool fct, cudaStream_t s) {
+  dim3 grid((m.E + kEdgeWarps - 1) / kEdgeWarps), block(kEdgeWarps * kWarp);
   if (fct) k_hflux<R, HOR, true><<<grid, block, 0, s>>>(m, a);
   else k_hflux<R, HOR, false><<<grid, block, 0, s>>>(m, a);
 }
 
-template <typename R, int VER>
-void launch_lo(const DMesh& m, const StepPtrs<R>& a, int K, cudaStream_t s) {
-  dim3 grid((m.N + kNodeWarps - 1) / kNodeWarps, K), block(kNodeWarps * kWarp);
-  size_t sm = (size_t)kNodeWarps * 10 * m.LW * sizeof(R);
-  k_fct_lo<R, VER><<<grid, block, sm, s>>>(m, a);
+// Dynamic shared memory above the 48 KB default needs an opt-in per kernel.
+template <typename F>
+void allow_smem(F* kernel, size_t bytes) {
+  if (bytes > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
-template <typename R, int VER>
-void launch_nofct(const DMesh& m, const StepPtrs<R>& a, int K, cudaStream_t s) {
-  dim3 grid((m.N + kNodeWarps - 1) / kNodeWarps, K), block(kNodeWarps * kWarp);
-  size_t sm = (size_t)kNodeWarps * 10 * m.LW * sizeof(R);
-  k_nofct_update<R, VER><<<grid, block, sm, s>>>(m, a);
+template <typename R, int VER, int KC>
+void launch_lo(const DMesh& m, const StepPtrs<R>& a, cudaStream_t s) {
+  dim3 grid((m.N + kNodeWarps - 1) / kNodeWarps), block(kNodeWarps * kWarp);
+  const size_t sm = kNodeWarps * warp_smem<R>(lo_slices(KC), m.LW, 0);
+  allow_smem(k_fct_lo<R, VER, KC>, sm);
+  k_fct_lo<R, VER, KC><<<grid, block, sm, s>>>(m, a);
+}
+
+template <typename R, int KC>
+void launch_ratio_update(const DMesh& m, const StepPtrs<R>& a, int mask, cudaStream_t s, int* launches) {
+  dim3 grid((m.N + kNodeWarps - 1) / kNodeWarps), block(kNodeWarps * kWarp);
+  if (mask & FGB_STAGE_RATIO) {
+    const size_t sm = kNodeWarps * warp_smem<R>(ratio_slices(KC), m.LW, kClBytes);
+    allow_smem(k_fct_ratio<R, KC>, sm);
+    k_fct_ratio<R, KC><<<grid, block, sm, s>>>(m, a);
+    ++*launches;
+  }
+  if (mask & FGB_STAGE_UPDATE) {
+    const size_t sm = kNodeWarps * warp_smem<R>(upd_slices(KC), m.LW, 0);
+    allow_smem(k_fct_update<R, KC>, sm);
+    k_fct_update<R, KC><<<grid, block, sm, s>>>(m, a);
+    ++*launches;
+  }
+}
+
+template <typename R, int VER, int KC>
+void launch_nofct(const DMesh& m, const StepPtrs<R>& a, cudaStream_t s) {
+  dim3 grid((m.N + kNodeWarps - 1) / kNodeWarps), block(kNodeWarps * kWarp);
+  const size_t sm = kNodeWarps * warp_smem<R>(nofct_slices(KC), m.LW, 0);
+  allow_smem(k_nofct_update<R, VER, KC>, sm);
+  k_nofct_update<R, VER, KC><<<grid, block, sm, s>>>(m, a);
+}
+
+template <typename R, int KC>
+void launch_lo_ver(const DMesh& m, const StepPtrs<R>& a, int ver, cudaStream_t s) {
+  switch (ver) {
+    case FGB_VER_QR4C: launch_lo<R, 1, KC>(m, a, s); break;
+    case FGB_VER_CDIFF: launch_lo<R, 2, KC>(m, a, s); break;
+    case FGB_VER_PPM: launch_lo<R, 3, KC>(m, a, s); break;
+    default: launch_lo<R, 0, KC>(m, a, s); break;
+  }
+}
+
+template <typename R, int KC>
+void launch_nofct_ver(const DMesh& m, const StepPtrs<R>& a, int ver, cudaStream_t s) {
+  switch (ver) {
+    case FGB_VER_QR4C: launch_nofct<R, 1, KC>(m, a, s); break;
+    case FGB_VER_CDIFF: launch_nofct<R, 2, KC>(m, a, s); break;
+    case FGB_VER_PPM: launch_nofct<R, 3, KC>(m, a, s); break;
+    default: launch_nofct<R, 0, KC>(m, a, s); break;
+  }
 }
 
 template <typename R>
@@ -78,7 +123,6 @@ int launch_stages(const DMesh& m, const fgb_step_desc& d, int mask, cudaStream_t
   a.w = static_cast<const R*>(d.w);
   a.we = static_cast<const R*>(d.we);
   a.vf = reinterpret_cast<R*>(ws + wl.off[0]);
-  a.flo = reinterpret_cast<R*>(ws + wl.off[1]);
   a.adfh = reinterpret_cast<R*>(ws + wl.off[2]);
   a.lo = reinterpret_cast<R*>(ws + wl.off[3]);
   a.adfv = reinterpret_cast<R*>(ws + wl.off[4]);
@@ -93,6 +137,7 @@ int launch_stages(const DMesh& m, const fgb_step_desc& d, int mask, cudaStream_t
   a.dt = (R)d.dt;
   a.ph = (R)d.ph;
   a.pv = (R)d.pv;
+  a.K = K;
   const bool fct = d.lim == FGB_LIM_FCT;
   int launches = 0;
   if (mask & FGB_STAGE_VFLUX) {
@@ -101,37 +146,27 @@ int launch_stages(const DMesh& m, const fgb_step_desc& d, int mask, cudaStream_t
     ++launches;
   }
   if (mask & FGB_STAGE_HFLUX) {
-    if (d.hor == FGB_HOR_UPW1) launch_hflux<R, 0>(m, a, fct, K, s);
-    else if (d.hor == FGB_HOR_MUSCL) launch_hflux<R, 1>(m, a, fct, K, s);
-    else launch_hflux<R, 2>(m, a, fct, K, s);
+    if (d.hor == FGB_HOR_UPW1) launch_hflux<R, 0>(m, a, fct, s);
+    else if (d.hor == FGB_HOR_MUSCL) launch_hflux<R, 1>(m, a, fct, s);
+    else launch_hflux<R, 2>(m, a, fct, s);
     ++launches;
   }
-  dim3 ngrid((m.N + kNodeWarps - 1) / kNodeWarps, K), nblock(kNodeWarps * kWarp);
+  // Tracers per node-kernel chunk: 4, 2 or 1, a divisor of K.
+  const int KC = (K % 4 == 0) ? 4 : ((K % 2 == 0) ? 2 : 1);
   if (fct) {
     if (mask & FGB_STAGE_LO) {
-      switch (d.ver) {
-        case FGB_VER_QR4C: launch_lo<R, 1>(m, a, K, s); break;
-        case FGB_VER_CDIFF: launch_lo<R, 2>(m, a, K, s); break;
-        case FGB_VER_PPM: launch_lo<R, 3>(m, a, K, s); break;
-        default: launch_lo<R, 0>(m, a, K, s); break;
-      }
+      if (KC == 4) launch_lo_ver<R, 4>(m, a, d.ver, s);
+      else if (KC == 2) launch_lo_ver<R, 2>(m, a, d.ver, s);
+      else launch_lo_ver<R, 1>(m, a, d.ver, s);
       ++launches;
     }
-    if (mask & FGB_STAGE_RATIO) {
-      k_fct_ratio<R><<<ngrid, nblock, (size_t)kNodeWarps * 3 * m.LW * sizeof(R), s>>>(m, a);
-      ++launches;
-    }
-    if (mask & FGB_STAGE_UPDATE) {
-      k_fct_update<R><<<ngrid, nblock, (size_t)kNodeWarps * 3 * m.LW * sizeof(R), s>>>(m, a);
-      ++launches;
-    }
+    if (KC == 4) launch_ratio_update<R, 4>(m, a, mask, s, &launches);
+    else if (KC == 2) launch_ratio_update<R, 2>(m, a, mask, s, &launches);
+    else launch_ratio_update<R, 1>(m, a, mask, s, &launches);
   } else if (mask & FGB_STAGE_UPDATE) {
-    switch (d.ver) {
-      case FGB_VER_QR4C: launch_nofct<R, 1>(m, a, K, s); break;
-      case FGB_VER_CDIFF: launch_nofct<R, 2>(m, a, K, s); break;
-      case FGB_VER_PPM: launch_nofct<R, 3>(m, a, K, s); break;
-      default: launch_nofct<R, 0>(m, a, K, s); break;
-    }
+    if (KC == 4) launch_nofct_ver<R, 4>(m, a, d.ver, s);
+    else if (KC == 2) launch_nofct_ver<R, 2>(m, a, d.ver, s);
+    else launch_nofct_ver<R, 1>(m, a, d.ver, s);
     ++launches;
   }
   *nlaunch = launches;

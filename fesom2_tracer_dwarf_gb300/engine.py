@@ -140,14 +140,14 @@ class TracerAdvection:
         return self.T[:, :, : m.nz].double().cpu().numpy()
 
     def workspace_view(self, name: str):
-        """A view of one workspace array: vf, flo, adfh, lo, adfv, rp, rm."""
+        """A view of one workspace array: vf, adfh, lo, adfv, rp, rm."""
         m = self.mesh
         L = _lib.load()
         offs = (ctypes.c_longlong * 7)()
         _lib.check(L.fgb_workspace_offsets(m.handle, _PREC[self.precision], self.K, offs), "offsets")
-        names = ["vf", "flo", "adfh", "lo", "adfv", "rp", "rm"]
+        names = ["vf", "(unused)", "adfh", "lo", "adfv", "rp", "rm"]
         i = names.index(name)
-        shape = {"vf": (m.E, m.LZ), "flo": (self.K, m.E, m.LZ), "adfh": (self.K, m.E, m.LZ),
+        shape = {"vf": (m.E, m.LZ), "adfh": (self.K, m.E, m.LZ),
                  "lo": (self.K, m.N, m.LZ), "adfv": (self.K, m.N, m.LW), "rp": (self.K, m.N, m.LZ),
                  "rm": (self.K, m.N, m.LZ)}[name]
         n = int(np.prod(shape))

@@ -153,7 +153,7 @@ int fgb_mesh_dims(const fgb_mesh* m, int* out8);
 int fgb_mesh_update_vertical(fgb_mesh* m, const fgb_hmesh* h);
 
 /* Workspace of a step: bytes, and the byte offsets of its arrays
- * (vf, flo, adfh, lo, adfv, rp, rm). */
+ * (vf, an unused slot, adfh, lo, adfv, rp, rm). */
 long long fgb_workspace_bytes(const fgb_mesh* m, int precision, int ntracers);
 int fgb_workspace_offsets(const fgb_mesh* m, int precision, int ntracers, long long* out7);
 
