@@ -40,6 +40,16 @@ __device__ __forceinline__ R rmax(R a, R b) { return a > b ? a : b; }
 template <typename R>
 __device__ __forceinline__ R rabs(R a) { return fabs(a); }
 
+// Division: correctly rounded in the FP64 form (bit parity with the CPU
+// restatement), the fast single-precision reciprocal form (about 2 ulp) in
+// the FP32 form.
+template <typename R>
+__device__ __forceinline__ R fdiv(R a, R b);
+template <>
+__device__ __forceinline__ double fdiv<double>(double a, double b) { return a / b; }
+template <>
+__device__ __forceinline__ float fdiv<float>(float a, float b) { return __fdividef(a, b); }
+
 // Layer membership of the horizontal-flux segments A-E of
 // lib/oce_adv_tra_hor.F90:171-252 (1-based layer z): which elements' volume
 // fluxes contribute at z. Returns 0 (inactive), 1, 2 or 3 (both).
@@ -144,8 +154,8 @@ __device__ __forceinline__ void node_mean_grad(const DMesh& m, const GeoPtrs<R>&
     tx = tx + ex * ar;
     ty = ty + ey * ar;
   }
-  gx = tx / tvol;
-  gy = ty / tvol;
+  gx = fdiv(tx, tvol);
+  gy = fdiv(ty, tvol);
 }
 
 // Two consecutive layers per lane: vector loads and stores of R pairs.
@@ -182,11 +192,11 @@ __device__ __forceinline__ R ho_flux(R v, R vp, R vm, R ta1, R ta2, R g1, R g2, 
   if (HOR == 0) return -(R(0.5) * (ta1 * vp + ta2 * vm));
   R Tm2, Tm1;
   if (HOR == 1) {
-    Tm2 = ta2 - ((R(2) * (ta2 - ta1) + ex * g2 + ey * g4) / R(6)) * c2;
-    Tm1 = ta1 + ((R(2) * (ta2 - ta1) + ex * g1 + ey * g3) / R(6)) * c1;
+    Tm2 = ta2 - fdiv(R(2) * (ta2 - ta1) + ex * g2 + ey * g4, R(6)) * c2;
+    Tm1 = ta1 + fdiv(R(2) * (ta2 - ta1) + ex * g1 + ey * g3, R(6)) * c1;
   } else {
-    Tm2 = ta2 - (R(2) * (ta2 - ta1) + ex * g2 + ey * g4) / R(6);
-    Tm1 = ta1 + (R(2) * (ta2 - ta1) + ex * g1 + ey * g3) / R(6);
+    Tm2 = ta2 - fdiv(R(2) * (ta2 - ta1) + ex * g2 + ey * g4, R(6));
+    Tm1 = ta1 + fdiv(R(2) * (ta2 - ta1) + ex * g1 + ey * g3, R(6));
   }
   const R cHO = vp * Tm1 + vm * Tm2;
   return -((R(0.5) * (R(1) - ph)) * cHO) - ((v * ph) * R(0.5)) * (Tm1 + Tm2);
@@ -202,7 +212,7 @@ __device__ __forceinline__ R ho_flux(R v, R vp, R vm, R ta1, R ta2, R g1, R g2, 
 // are stored at the edge's own index.
 // ---------------------------------------------------------------------------
 template <typename R, int HOR, bool FCT>
-__global__ void __launch_bounds__(256, 3) k_hflux(DMesh m, StepPtrs<R> a) {
+__global__ void __launch_bounds__(256, (sizeof(R) == 4 ? 3 : 2)) k_hflux(DMesh m, StepPtrs<R> a) {
   const int lane = threadIdx.x & (kWarp - 1);
   const int w = blockIdx.x * (blockDim.x / kWarp) + (threadIdx.x / kWarp);
   if (w >= m.E) return;
@@ -337,12 +347,12 @@ __device__ __forceinline__ R ver_qr4c(const Col<R>& c, int z, int nzmin, int nzm
   }
   const R T0 = c.T[z - 1], Tm1 = c.T[z - 2], Tm2 = c.T[z - 3], Tp1 = c.T[z];
   const R Z0 = c.Z[z - 1], Zm1 = c.Z[z - 2], Zm2 = c.Z[z - 3], Zp1 = c.Z[z];
-  const R qc = (Tm1 - T0) / (Zm1 - Z0);
-  const R qu = (T0 - Tp1) / (Z0 - Zp1);
-  const R qd = (Tm2 - Tm1) / (Zm2 - Zm1);
+  const R qc = fdiv(Tm1 - T0, Zm1 - Z0);
+  const R qu = fdiv(T0 - Tp1, Z0 - Zp1);
+  const R qd = fdiv(Tm2 - Tm1, Zm2 - Zm1);
   const R zb = c.zb[z - 1];
-  const R tm1 = T0 + ((R(2) * qc + qu) * (zb - Z0)) / R(3);
-  const R tm2 = Tm1 + ((R(2) * qc + qd) * (zb - Zm1)) / R(3);
+  const R tm1 = T0 + fdiv((R(2) * qc + qu) * (zb - Z0), R(3));
+  const R tm2 = Tm1 + fdiv((R(2) * qc + qd) * (zb - Zm1), R(3));
   const R tm = (W + rabs(W)) * tm1 + (W - rabs(W)) * tm2;
   return (-((R(0.5) * (R(1) - num_ord)) * tm) - (num_ord * (R(0.5) * (tm1 + tm2))) * W) * c.area[z - 1] - fold;
 }
@@ -367,10 +377,10 @@ __device__ __forceinline__ R ppm_tv(const Col<R>& c, int z, int nzmin, int nzmax
     const int nz = z - 1;  // layer whose upper neighbour interface is z
     const R dzjm1 = c.hnn[nz - 2], dzj = c.hnn[nz - 1], dzjp1 = c.hnn[nz], dzjp2 = c.hnn[nz + 1];
     const R Tm = T[nz - 2], T0 = T[nz - 1], Tp = T[nz], Tpp = T[nz + 1];
-    R deltaj = (dzj / (dzjm1 + dzj + dzjp1)) *
-               (((R(2) * dzjm1 + dzj) / (dzjp1 + dzj)) * (Tp - T0) + ((dzj + R(2) * dzjp1) / (dzjm1 + dzj)) * (T0 - Tm));
-    R deltajp1 = (dzjp1 / (dzj + dzjp1 + dzjp2)) *
-                 (((R(2) * dzj + dzjp1) / (dzjp2 + dzjp1)) * (Tpp - Tp) + ((dzjp1 + R(2) * dzjp2) / (dzj + dzjp1)) * (Tp - T0));
+    R deltaj = fdiv(dzj, dzjm1 + dzj + dzjp1) *
+               (fdiv(R(2) * dzjm1 + dzj, dzjp1 + dzj) * (Tp - T0) + fdiv(dzj + R(2) * dzjp1, dzjm1 + dzj) * (T0 - Tm));
+    R deltajp1 = fdiv(dzjp1, dzj + dzjp1 + dzjp2) *
+                 (fdiv(R(2) * dzj + dzjp1, dzjp2 + dzjp1) * (Tpp - Tp) + fdiv(dzjp1 + R(2) * dzjp2, dzj + dzjp1) * (Tp - T0));
     if ((Tp - T0) * (T0 - Tm) > R(0))
       deltaj = rmin(rmin(rabs(deltaj), R(2) * rabs(Tp - T0)), R(2) * rabs(T0 - Tm)) * copysign(R(1), deltaj);
     else
@@ -379,11 +389,11 @@ __device__ __forceinline__ R ppm_tv(const Col<R>& c, int z, int nzmin, int nzmax
       deltajp1 = rmin(rmin(rabs(deltajp1), R(2) * rabs(Tpp - Tp)), R(2) * rabs(Tp - T0)) * copysign(R(1), deltajp1);
     else
       deltajp1 = R(0);
-    const R inner1 = (((R(2) * dzjp1) * dzj) / (dzj + dzjp1)) *
-                     ((dzjm1 + dzj) / (R(2) * dzj + dzjp1) - (dzjp2 + dzjp1) / (R(2) * dzjp1 + dzj)) * (Tp - T0);
-    const R inner2 = ((dzj * (dzjm1 + dzj)) / (R(2) * dzj + dzjp1)) * deltajp1;
-    const R inner3 = ((dzjp1 * (dzjp1 + dzjp2)) / (dzj + R(2) * dzjp1)) * deltaj;
-    return (T0 + (dzj / (dzj + dzjp1)) * (Tp - T0)) + (R(1) / (dzjm1 + dzj + dzjp1 + dzjp2)) * (inner1 - inner2 + inner3);
+    const R inner1 = fdiv((R(2) * dzjp1) * dzj, dzj + dzjp1) *
+                     (fdiv(dzjm1 + dzj, R(2) * dzj + dzjp1) - fdiv(dzjp2 + dzjp1, R(2) * dzjp1 + dzj)) * (Tp - T0);
+    const R inner2 = fdiv(dzj * (dzjm1 + dzj), R(2) * dzj + dzjp1) * deltajp1;
+    const R inner3 = fdiv(dzjp1 * (dzjp1 + dzjp2), dzj + R(2) * dzjp1) * deltaj;
+    return (T0 + fdiv(dzj, dzj + dzjp1) * (Tp - T0)) + fdiv(R(1), dzjm1 + dzj + dzjp1 + dzjp2) * (inner1 - inner2 + inner3);
   }
   if (z == nzmax) return T[nzmax - 2];
   if (z == nzmax - 1) {
@@ -404,19 +414,19 @@ __device__ __forceinline__ R ppm_layer(const Col<R>& c, int nz, bool upper, R dt
     aL = T0;
     aR = T0;
   }
-  if ((aR - aL) * (T0 - R(0.5) * (aL + aR)) > ((aR - aL) * (aR - aL)) / R(6)) aL = R(3) * T0 - R(2) * aR;
-  if ((aR - aL) * (T0 - R(0.5) * (aR + aL)) < -(((aR - aL) * (aR - aL)) / R(6))) aR = R(3) * T0 - R(2) * aL;
+  if ((aR - aL) * (T0 - R(0.5) * (aL + aR)) > fdiv((aR - aL) * (aR - aL), R(6))) aL = R(3) * T0 - R(2) * aR;
+  if ((aR - aL) * (T0 - R(0.5) * (aR + aL)) < -fdiv((aR - aL) * (aR - aL), R(6))) aR = R(3) * T0 - R(2) * aL;
   const R dzj = c.hn[nz - 1];
   const R aj = R(6) * (T0 - R(0.5) * (aL + aR));
   if (upper) {
     const R W = c.W[nz - 1];
-    const R x = rmin((W * dt) / dzj, R(1));
-    R tv = -aL - (R(0.5) * x) * ((aR - aL) + (R(1) - (R(2) / R(3)) * x) * aj);
+    const R x = rmin(fdiv(W * dt, dzj), R(1));
+    R tv = -aL - (R(0.5) * x) * ((aR - aL) + (R(1) - fdiv(R(2), R(3)) * x) * aj);
     return (tv * c.area[nz - 1]) * W;
   }
   const R W = c.W[nz];
-  const R x = rmin(-((W * dt) / dzj), R(1));
-  R tv = -aR + (R(0.5) * x) * ((aR - aL) - (R(1) - (R(2) / R(3)) * x) * aj);
+  const R x = rmin(-fdiv(W * dt, dzj), R(1));
+  R tv = -aR + (R(0.5) * x) * ((aR - aL) - (R(1) - fdiv(R(2), R(3)) * x) * aj);
   return (tv * c.area[nz]) * W;
 }
 
@@ -528,7 +538,7 @@ constexpr int kClBytes = kMaxCl * 2 * (int)sizeof(int);
 // with the expression adv_tra_hor_upw1 uses (lib/oce_adv_tra_hor.F90:218-220).
 // ---------------------------------------------------------------------------
 template <typename R, int VER, int KC>
-__global__ void k_fct_lo(DMesh m, StepPtrs<R> a) {
+__global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_fct_lo(DMesh m, StepPtrs<R> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kWarp - 1), wib = threadIdx.x / kWarp;
   const int n = blockIdx.x * (blockDim.x / kWarp) + wib;
@@ -603,8 +613,8 @@ __global__ void k_fct_lo(DMesh m, StepPtrs<R> a) {
         const R* Ti = sT + i * LW;
         const R* Fi = sFv + i * LW;
         R l0 = acc0[i], l1 = acc1[i];
-        if (w0) l0 = (Ti[k0] * hn.x + ((acc0[i] + (Fi[k0] - Fi[k0 + 1])) * dt) / av.x) / hnn.x;
-        if (w1) l1 = (Ti[k0 + 1] * hn.y + ((acc1[i] + (Fi[k0 + 1] - Fi[k0 + 2])) * dt) / av.y) / hnn.y;
+        if (w0) l0 = fdiv(Ti[k0] * hn.x + fdiv((acc0[i] + (Fi[k0] - Fi[k0 + 1])) * dt, av.x), hnn.x);
+        if (w1) l1 = fdiv(Ti[k0 + 1] * hn.y + fdiv((acc1[i] + (Fi[k0 + 1] - Fi[k0 + 2])) * dt, av.y), hnn.y);
         st2(a.lo + (t0 + i) * a.sN + n * LZ + k0, l0, l1);
       }
     }
@@ -627,7 +637,7 @@ __global__ void k_fct_lo(DMesh m, StepPtrs<R> a) {
 // the distinct nodes with the deepest layer reaching them give the same value.
 // ---------------------------------------------------------------------------
 template <typename R, int KC>
-__global__ void k_fct_ratio(DMesh m, StepPtrs<R> a) {
+__global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_fct_ratio(DMesh m, StepPtrs<R> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kWarp - 1), wib = threadIdx.x / kWarp;
   const int n = blockIdx.x * (blockDim.x / kWarp) + wib;
@@ -746,10 +756,10 @@ __global__ void k_fct_ratio(DMesh m, StepPtrs<R> a) {
             bmin = rmin(rmin(mns[k - 1], mns[k]), mns[k + 1]) - lov;
           }
           const R avk = l ? av.y : av.x;
-          R flux = ((l ? pl1[i] : pl0[i]) * dt) / avk + R(1e-16);
-          out_p[l] = rmin(R(1), bmax / flux);
-          flux = ((l ? mi1[i] : mi0[i]) * dt) / avk - R(1e-16);
-          out_m[l] = rmin(R(1), bmin / flux);
+          R flux = fdiv((l ? pl1[i] : pl0[i]) * dt, avk) + R(1e-16);
+          out_p[l] = rmin(R(1), fdiv(bmax, flux));
+          flux = fdiv((l ? mi1[i] : mi0[i]) * dt, avk) - R(1e-16);
+          out_m[l] = rmin(R(1), fdiv(bmin, flux));
         }
         st2(a.rp + (t0 + i) * a.sN + n * LZ + k0, out_p[0], out_p[1]);
         st2(a.rm + (t0 + i) * a.sN + n * LZ + k0, out_m[0], out_m[1]);
@@ -766,7 +776,7 @@ __global__ void k_fct_ratio(DMesh m, StepPtrs<R> a) {
 // persistent del_ttf, lib/tracer_c_interface.F90:194-214).
 // ---------------------------------------------------------------------------
 template <typename R, int KC>
-__global__ void k_fct_update(DMesh m, StepPtrs<R> a) {
+__global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_fct_update(DMesh m, StepPtrs<R> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kWarp - 1), wib = threadIdx.x / kWarp;
   const int n = blockIdx.x * (blockDim.x / kWarp) + wib;
@@ -837,15 +847,15 @@ __global__ void k_fct_update(DMesh m, StepPtrs<R> a) {
             else { ae0 = rmin(ae0, rmo.x); ae0 = rmin(ae0, rpn0); }
             if (f.y >= R(0)) { ae1 = rmin(ae1, rpo.y); ae1 = rmin(ae1, rmn1); }
             else { ae1 = rmin(ae1, rmo.y); ae1 = rmin(ae1, rpn1); }
-            if (a0) dh0[i] = dh0[i] - ((ae0 * f.x) * dt) / av.x;
-            if (a1) dh1[i] = dh1[i] - ((ae1 * f.y) * dt) / av.y;
+            if (a0) dh0[i] = dh0[i] - fdiv((ae0 * f.x) * dt, av.x);
+            if (a1) dh1[i] = dh1[i] - fdiv((ae1 * f.y) * dt, av.y);
           } else {
             if (f.x >= R(0)) { ae0 = rmin(ae0, rpn0); ae0 = rmin(ae0, rmo.x); }
             else { ae0 = rmin(ae0, rmn0); ae0 = rmin(ae0, rpo.x); }
             if (f.y >= R(0)) { ae1 = rmin(ae1, rpn1); ae1 = rmin(ae1, rmo.y); }
             else { ae1 = rmin(ae1, rmn1); ae1 = rmin(ae1, rpo.y); }
-            if (a0) dh0[i] = dh0[i] + ((ae0 * f.x) * dt) / av.x;
-            if (a1) dh1[i] = dh1[i] + ((ae1 * f.y) * dt) / av.y;
+            if (a0) dh0[i] = dh0[i] + fdiv((ae0 * f.x) * dt, av.x);
+            if (a1) dh1[i] = dh1[i] + fdiv((ae1 * f.y) * dt, av.y);
           }
         }
       }
@@ -860,11 +870,11 @@ __global__ void k_fct_update(DMesh m, StepPtrs<R> a) {
         R* del = a.del ? a.del + (t0 + i) * a.sN + n * LZ + k0 : nullptr;
         const vec2<R> d0 = del ? ld2(del) : vec2<R>{R(0), R(0)};
         R dv0 = (R(0) - Tn.x * hn.x) + lo.x * hnn.x;
-        dv0 = dv0 + ((Lv[k0] - Lv[k0 + 1]) * dt) / av.x;
+        dv0 = dv0 + fdiv((Lv[k0] - Lv[k0 + 1]) * dt, av.x);
         R dv1 = (R(0) - Tn.y * hn.y) + lo.y * hnn.y;
-        dv1 = dv1 + ((Lv[k0 + 1] - Lv[k0 + 2]) * dt) / av.y;
+        dv1 = dv1 + fdiv((Lv[k0 + 1] - Lv[k0 + 2]) * dt, av.y);
         const R e0 = d0.x + dh0[i] + dv0, e1 = d0.y + dh1[i] + dv1;
-        const R n0 = w0 ? Tn.x + e0 / hnn.x : Tn.x, n1v = w1 ? Tn.y + e1 / hnn.y : Tn.y;
+        const R n0 = w0 ? Tn.x + fdiv(e0, hnn.x) : Tn.x, n1v = w1 ? Tn.y + fdiv(e1, hnn.y) : Tn.y;
         st2(T, n0, n1v);
         if (del) st2(del, w0 ? e0 : d0.x, w1 ? e1 : d0.y);
         if (a.TAout) st2(a.TAout + (t0 + i) * a.sTA + n * LZ + k0, n0, n1v);
@@ -879,7 +889,7 @@ __global__ void k_fct_update(DMesh m, StepPtrs<R> a) {
 // (oce_tra_adv_flux2dtracer) and the tendency update in one pass.
 // ---------------------------------------------------------------------------
 template <typename R, int VER, int KC>
-__global__ void k_nofct_update(DMesh m, StepPtrs<R> a) {
+__global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_nofct_update(DMesh m, StepPtrs<R> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kWarp - 1), wib = threadIdx.x / kWarp;
   const int n = blockIdx.x * (blockDim.x / kWarp) + wib;
@@ -927,11 +937,11 @@ __global__ void k_nofct_update(DMesh m, StepPtrs<R> a) {
         for (int i = 0; i < KC; ++i) {
           const vec2<R> f = ld2(a.adfh + (t0 + i) * a.sE + (size_t)q.e * LZ + k0);
           if (q.role) {
-            if (a0) dh0[i] = dh0[i] - (f.x * dt) / av.x;
-            if (a1) dh1[i] = dh1[i] - (f.y * dt) / av.y;
+            if (a0) dh0[i] = dh0[i] - fdiv(f.x * dt, av.x);
+            if (a1) dh1[i] = dh1[i] - fdiv(f.y * dt, av.y);
           } else {
-            if (a0) dh0[i] = dh0[i] + (f.x * dt) / av.x;
-            if (a1) dh1[i] = dh1[i] + (f.y * dt) / av.y;
+            if (a0) dh0[i] = dh0[i] + fdiv(f.x * dt, av.x);
+            if (a1) dh1[i] = dh1[i] + fdiv(f.y * dt, av.y);
           }
         }
       }
@@ -944,10 +954,10 @@ __global__ void k_nofct_update(DMesh m, StepPtrs<R> a) {
         const vec2<R> Tn = ld2(T);
         R* del = a.del ? a.del + (t0 + i) * a.sN + n * LZ + k0 : nullptr;
         const vec2<R> d0 = del ? ld2(del) : vec2<R>{R(0), R(0)};
-        const R dv0 = R(0) + ((F[k0] - F[k0 + 1]) * dt) / av.x;
-        const R dv1 = R(0) + ((F[k0 + 1] - F[k0 + 2]) * dt) / av.y;
+        const R dv0 = R(0) + fdiv((F[k0] - F[k0 + 1]) * dt, av.x);
+        const R dv1 = R(0) + fdiv((F[k0 + 1] - F[k0 + 2]) * dt, av.y);
         const R e0 = d0.x + dh0[i] + dv0, e1 = d0.y + dh1[i] + dv1;
-        const R n0 = w0 ? Tn.x + e0 / hnn.x : Tn.x, n1v = w1 ? Tn.y + e1 / hnn.y : Tn.y;
+        const R n0 = w0 ? Tn.x + fdiv(e0, hnn.x) : Tn.x, n1v = w1 ? Tn.y + fdiv(e1, hnn.y) : Tn.y;
         st2(T, n0, n1v);
         if (del) st2(del, w0 ? e0 : d0.x, w1 ? e1 : d0.y);
         if (a.TAout) st2(a.TAout + (t0 + i) * a.sTA + n * LZ + k0, n0, n1v);
