@@ -197,6 +197,26 @@ int fgb_tracer_stats(const fgb_mesh* m, int precision, const void* T, long long 
 /* Number of kernels the last fgb_adv_step / fgb_adv_stages call launched. */
 int fgb_last_launch_count(void);
 
+/* No counterpart in the reference: a variant of fgb_adv_step for callers that
+ * cannot allocate device memory -- for example a host model whose framework
+ * owns all GPU memory through its own pool allocator and must not see
+ * cudaMalloc called behind its back. It allocates nothing: the step's scratch
+ * is a file-scope device array of FGB_STATIC_WORKSPACE_BYTES (64 MiB) that
+ * every GPU loading this library holds until the process exits; d->workspace
+ * is ignored. The caller still passes T, TA, vel, w and we.
+ * - Meshes whose fgb_workspace_bytes(m, precision, ntracers) exceeds
+ *   FGB_STATIC_WORKSPACE_BYTES are rejected with -1 and a message.
+ * - The first call on a device looks up the array's device address
+ *   (cudaGetSymbolAddress) with that device current; make that first call
+ *   before any stream capture.
+ * - Every call shares the one array and overwrites it; nothing in it needs to
+ *   start at zero (each call writes every scratch value before reading it).
+ *   Calls that overlap on the GPU (concurrent streams, or two threads) race on
+ *   it: serialise them. */
+#define FGB_STATIC_WORKSPACE_BYTES (64LL * 1024 * 1024)
+long long fgb_static_workspace_bytes(void);
+int fgb_adv_step_static(const fgb_mesh* m, const fgb_step_desc* d, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
