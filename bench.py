@@ -122,12 +122,15 @@ def stage_bytes(m, K, s, ver, fct=True, copy_ab=True):
     el = m.M / m.N
     colgeo = 5 + (2 if ver == "QR4C" else 0)  # w, area, hnode, hnode_new, areasvol (+ Z_3d_n, zbar_3d_n)
     b = {
-        "vflux": cells * s * (2 * el + el + e),                          # vel(2 comps), helem -> vf
-        "hflux": cells * s * (e + K * (1 + ta + (2 * e if fct else e))),  # vf, T[,TA] -> flo, adfh
-        "lo": cells * s * (colgeo + K * (1 + ta + e + 2)),                # geometry, flo, T[,TA] -> LO, adfv
-        "ratio": cells * s * (1 + K * (2 + 1 + e + 2)),                   # areasvol; LO, T, adfv, adfh -> R+, R-
-        "update": cells * s * (3 + K * (2 + 1 + e + 1 + 1 + 1)),          # geometry; R+-, adfv, adfh, LO, T -> T
+        "vflux": cells * s * (2 * el + el + e),                    # vel (2 comps), helem -> vf
+        "hflux": cells * s * (e + K * (1 + ta + e)),                # vf, T[,TA] -> adfh
     }
+    if fct:
+        b["lo"] = cells * s * (colgeo + e + K * (1 + ta + 2))        # geometry, vf, T[,TA] -> LO, adfv
+        b["ratio"] = cells * s * (1 + K * (2 + 1 + e + 2))          # areasvol; LO, T, adfv, adfh -> R+, R-
+        b["update"] = cells * s * (3 + K * (2 + 1 + e + 1 + 2))     # geometry; R+-, adfv, adfh, LO, T -> T
+    else:
+        b["update"] = cells * s * (colgeo + K * (ta + 1 + e + 2))   # geometry; T_AB, adfh, T -> T
     return b
 
 
