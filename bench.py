@@ -290,6 +290,11 @@ def run_gpu(args):
     cfg = WORKLOADS[args.workload]
     m, eng, T0 = build_case(cfg, cfg["precision"], device)
     cells = m.N * m.nz * cfg["K"]
+    tuned = None
+    if not args.no_tune:
+        from fesom2_tracer_dwarf_gb300 import autotune
+
+        tuned = autotune.tune(eng, cfg["dt"], reps=3)
     with ClockSampler(local) as clk:
         total_ms, per, launches = time_engine(eng, T0, cfg["dt"], args.steps, args.warmup, barrier)
     clocks = clk.summary()
@@ -322,7 +327,8 @@ def run_gpu(args):
                    "nodes": m.N, "edges": m.E, "elements": m.M, "tracers": cfg["K"],
                    "schemes": f"{cfg['hor']}/{cfg['ver']}/{cfg['lim']}", "form": cfg["precision"], "dt_s": cfg["dt"],
                    "tracer_cells_per_step": cells, "l2": "inputs larger than L2 (no flush)",
-                   "parallelism": f"replicas x{world}"},
+                   "parallelism": f"replicas x{world}",
+                   "launch_cfg": tuned["cfg"] if tuned else "default"},
         "stage_ms": {k: round(v, 4) for k, v in per.items()},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
@@ -339,6 +345,8 @@ def run_gpu(args):
         del eng, T0
         torch.cuda.empty_cache()
         m64, e64, T64 = build_case(cfg, "fp64", device)
+        if not args.no_tune:
+            autotune.tune(e64, cfg["dt"], reps=1)
         n64 = max(2, min(args.steps, args.fp64_steps))
         tot64, per64, l64 = time_engine(e64, T64, cfg["dt"], n64, min(args.warmup, 2), barrier)
         ms64 = tot64 / n64
@@ -407,6 +415,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="use the default launch configuration")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3

@@ -47,6 +47,7 @@ class StepDesc(ctypes.Structure):
         ("del_", _vp),
         ("workspace", _vp),
         ("workspace_bytes", ctypes.c_longlong),
+        ("cfg", ctypes.c_int * 8),
     ]
 
 

@@ -64,8 +64,7 @@ struct StepPtrs {
   R* adfh;          // (K,E,LZ) antidiffusive (FCT) or high-order horizontal flux
   R* lo;            // (K,N,LZ) low-order solution fct_LO
   R* adfv;          // (K,N,LW) antidiffusive vertical flux
-  R* rp;            // (K,N,LZ) fct_plus limiting factor
-  R* rm;            // (K,N,LZ) fct_minus limiting factor
+  R* rpm;           // (K,N,LZ,2) limiting factors fct_plus, fct_minus interleaved per layer
   R* del;           // optional (K,N,LZ) persistent del_ttf
   long long sT, sTA, sE, sN, sW;  // strides between tracers (elements)
   int K;            // tracers in this launch

@@ -183,6 +183,27 @@ __device__ __forceinline__ void st2(R* p, R a, R b) {
   *reinterpret_cast<vec2<R>*>(p) = v;
 }
 
+// Four values per lane (two layers of an interleaved pair array).
+template <typename R>
+struct Q4 {
+  R a, b, c, d;
+};
+__device__ __forceinline__ Q4<float> ld4(const float* p) {
+  const float4 v = *reinterpret_cast<const float4*>(p);
+  return Q4<float>{v.x, v.y, v.z, v.w};
+}
+__device__ __forceinline__ Q4<double> ld4(const double* p) {
+  const double2 u = *reinterpret_cast<const double2*>(p), v = *reinterpret_cast<const double2*>(p + 2);
+  return Q4<double>{u.x, u.y, v.x, v.y};
+}
+__device__ __forceinline__ void st4(float* p, float a, float b, float c, float d) {
+  *reinterpret_cast<float4*>(p) = make_float4(a, b, c, d);
+}
+__device__ __forceinline__ void st4(double* p, double a, double b, double c, double d) {
+  *reinterpret_cast<double2*>(p) = make_double2(a, b);
+  *reinterpret_cast<double2*>(p + 2) = make_double2(c, d);
+}
+
 // High-order horizontal flux of one layer: upwind (adv_tra_hor_upw1,
 // lib/oce_adv_tra_hor.F90:218-220) or the MUSCL/MFCT edge reconstruction
 // (lib/oce_adv_tra_hor.F90:454-497, :748-790); c1, c2 are the c_lo masks.
@@ -270,8 +291,13 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 ? 3 : 2)) k_hflux(DMesh m
       R g10 = R(0), g20 = R(0), g30 = R(0), g40 = R(0), g11 = R(0), g21 = R(0), g31 = R(0), g41 = R(0);
       if (HOR != 0) {
         if (tri0 && tri1) {
-          const vec2<R> ua = ld2(TA + tu.a * LZ + k0), ub = ld2(TA + tu.b * LZ + k0), uc = ld2(TA + tu.c * LZ + k0);
-          const vec2<R> da = ld2(TA + td.a * LZ + k0), db = ld2(TA + td.b * LZ + k0), dc = ld2(TA + td.c * LZ + k0);
+          // the upwind triangle holds node 1 and the downwind one node 2: reuse those columns
+          const vec2<R> ua = tu.a == n1 ? s1 : ld2(TA + tu.a * LZ + k0);
+          const vec2<R> ub = tu.b == n1 ? s1 : ld2(TA + tu.b * LZ + k0);
+          const vec2<R> uc = tu.c == n1 ? s1 : ld2(TA + tu.c * LZ + k0);
+          const vec2<R> da = td.a == n2 ? s2 : ld2(TA + td.a * LZ + k0);
+          const vec2<R> db = td.b == n2 ? s2 : ld2(TA + td.b * LZ + k0);
+          const vec2<R> dc = td.c == n2 ? s2 : ld2(TA + td.c * LZ + k0);
           g10 = tu.x0 * ua.x + tu.x1 * ub.x + tu.x2 * uc.x;
           g30 = tu.y0 * ua.x + tu.y1 * ub.x + tu.y2 * uc.x;
           g11 = tu.x0 * ua.y + tu.x1 * ub.y + tu.x2 * uc.y;
@@ -586,6 +612,7 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_fct_lo(DMesh 
       R acc0[KC], acc1[KC];
 #pragma unroll
       for (int i = 0; i < KC; ++i) acc0[i] = acc1[i] = R(0);
+#pragma unroll 2
       for (int j = 0; j < nb.deg; ++j) {
         const Nbr q = nb.get(m, j);
         const bool a0 = z0 >= q.lo && z0 <= q.hi, a1 = z1 >= q.lo && z1 <= q.hi;
@@ -676,6 +703,7 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_fct_ratio(DMe
         mn0[i] = -mx0i;
         mn1[i] = -mx1i;
       }
+#pragma unroll 2
       for (int j = 0; j < ncl; ++j) {
         const int node = cl_staged ? scl[2 * j] : m.cl_node[c0 + j];
         const int lev = cl_staged ? scl[2 * j + 1] : m.cl_lev[c0 + j];
@@ -715,6 +743,7 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_fct_ratio(DMe
         mi1[i] = R(0) + (rmin(R(0), ad[k0 + 1]) + rmin(R(0), -ad[k0 + 2]));
       }
       const int z0 = k0 + 1, z1 = k0 + 2;
+#pragma unroll 2
       for (int j = 0; j < nb.deg; ++j) {
         const Nbr q = nb.get(m, j);
         const bool a0 = z0 >= q.lo && z0 <= q.hi, a1 = z1 >= q.lo && z1 <= q.hi;
@@ -761,8 +790,7 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_fct_ratio(DMe
           flux = fdiv((l ? mi1[i] : mi0[i]) * dt, avk) - R(1e-16);
           out_m[l] = rmin(R(1), fdiv(bmin, flux));
         }
-        st2(a.rp + (t0 + i) * a.sN + n * LZ + k0, out_p[0], out_p[1]);
-        st2(a.rm + (t0 + i) * a.sN + n * LZ + k0, out_m[0], out_m[1]);
+        st4(a.rpm + 2 * ((t0 + i) * a.sN + n * LZ + k0), out_p[0], out_m[0], out_p[1], out_m[1]);
       }
     }
     __syncwarp();
@@ -794,8 +822,11 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_fct_update(DM
   for (int t0 = 0; t0 < a.K; t0 += KC) {
 #pragma unroll
     for (int i = 0; i < KC; ++i) {
-      stage(sRp + i * LW, a.rp + (t0 + i) * a.sN + n * LZ, nz, lane);
-      stage(sRm + i * LW, a.rm + (t0 + i) * a.sN + n * LZ, nz, lane);
+      const R* src = a.rpm + 2 * ((t0 + i) * a.sN + n * LZ);
+      for (int k = lane; k < nz; k += kWarp) {
+        sRp[i * LW + k] = src[2 * k];
+        sRm[i * LW + k] = src[2 * k + 1];
+      }
     }
     __syncwarp();
 #pragma unroll
@@ -831,6 +862,7 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_fct_update(DM
       R dh0[KC], dh1[KC];
 #pragma unroll
       for (int i = 0; i < KC; ++i) dh0[i] = dh1[i] = R(0);
+#pragma unroll 2
       for (int j = 0; j < nb.deg; ++j) {
         const Nbr q = nb.get(m, j);
         const bool a0 = z0 >= q.lo && z0 <= q.hi, a1 = z1 >= q.lo && z1 <= q.hi;
@@ -838,7 +870,8 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_fct_update(DM
 #pragma unroll
         for (int i = 0; i < KC; ++i) {
           const vec2<R> f = ld2(a.adfh + (t0 + i) * a.sE + (size_t)q.e * LZ + k0);
-          const vec2<R> rpo = ld2(a.rp + (t0 + i) * a.sN + o), rmo = ld2(a.rm + (t0 + i) * a.sN + o);
+          const Q4<R> ro = ld4(a.rpm + 2 * ((t0 + i) * a.sN + o));
+          const vec2<R> rpo{ro.a, ro.c}, rmo{ro.b, ro.d};
           const R rpn0 = sRp[i * LW + k0], rpn1 = sRp[i * LW + k0 + 1];
           const R rmn0 = sRm[i * LW + k0], rmn1 = sRm[i * LW + k0 + 1];
           R ae0 = R(1), ae1 = R(1);
@@ -930,6 +963,7 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_nofct_update(
       R dh0[KC], dh1[KC];
 #pragma unroll
       for (int i = 0; i < KC; ++i) dh0[i] = dh1[i] = R(0);
+#pragma unroll 2
       for (int j = 0; j < nb.deg; ++j) {
         const Nbr q = nb.get(m, j);
         const bool a0 = z0 >= q.lo && z0 <= q.hi, a1 = z1 >= q.lo && z1 <= q.hi;

@@ -12,8 +12,9 @@
 
 namespace fgb {
 
-constexpr int kEdgeWarps = 8;  // edges per 256-thread block
-constexpr int kNodeWarps = 4;  // node columns per 128-thread block
+constexpr int kEdgeWarps = 8;  // default edges per block
+constexpr int kNodeWarps = 4;  // default node columns per block (the kernels' launch bound)
+
 
 template <typename R>
 WorkspaceLayout workspace_layout(const DMesh& m, int K) {
@@ -26,15 +27,15 @@ WorkspaceLayout workspace_layout(const DMesh& m, int K) {
   w.off[2] = off; off += al((long long)K * E * LZ * s);  // adfh
   w.off[3] = off; off += al((long long)K * N * LZ * s);  // lo
   w.off[4] = off; off += al((long long)K * N * LW * s);  // adfv
-  w.off[5] = off; off += al((long long)K * N * LZ * s);  // rp
-  w.off[6] = off; off += al((long long)K * N * LZ * s);  // rm
+  w.off[5] = off; off += al(2LL * K * N * LZ * s);       // R+, R- interleaved
+  w.off[6] = w.off[5];                                    // (same array)
   w.total = off;
   return w;
 }
 
 template <typename R, int HOR>
-void launch_hflux(const DMesh& m, const StepPtrs<R>& a, bool fct, cudaStream_t s) {
-  dim3 grid((m.E + kEdgeWarps - 1) / kEdgeWarps), block(kEdgeWarps * kWarp);
+void launch_hflux(const DMesh& m, const StepPtrs<R>& a, bool fct, int ew, cudaStream_t s) {
+  dim3 grid((m.E + ew - 1) / ew), block(ew * kWarp);
   if (fct) k_hflux<R, HOR, true><<<grid, block, 0, s>>>(m, a);
   else k_hflux<R, HOR, false><<<grid, block, 0, s>>>(m, a);
 }
@@ -46,56 +47,62 @@ void allow_smem(F* kernel, size_t bytes) {
 }
 
 template <typename R, int VER, int KC>
-void launch_lo(const DMesh& m, const StepPtrs<R>& a, cudaStream_t s) {
-  dim3 grid((m.N + kNodeWarps - 1) / kNodeWarps), block(kNodeWarps * kWarp);
-  const size_t sm = kNodeWarps * warp_smem<R>(lo_slices(KC), m.LW, 0);
+void launch_lo(const DMesh& m, const StepPtrs<R>& a, int nw, cudaStream_t s) {
+  dim3 grid((m.N + nw - 1) / nw), block(nw * kWarp);
+  const size_t sm = nw * warp_smem<R>(lo_slices(KC), m.LW, 0);
   allow_smem(k_fct_lo<R, VER, KC>, sm);
   k_fct_lo<R, VER, KC><<<grid, block, sm, s>>>(m, a);
 }
 
 template <typename R, int KC>
-void launch_ratio_update(const DMesh& m, const StepPtrs<R>& a, int mask, cudaStream_t s, int* launches) {
-  dim3 grid((m.N + kNodeWarps - 1) / kNodeWarps), block(kNodeWarps * kWarp);
-  if (mask & FGB_STAGE_RATIO) {
-    const size_t sm = kNodeWarps * warp_smem<R>(ratio_slices(KC), m.LW, kClBytes);
-    allow_smem(k_fct_ratio<R, KC>, sm);
-    k_fct_ratio<R, KC><<<grid, block, sm, s>>>(m, a);
-    ++*launches;
-  }
-  if (mask & FGB_STAGE_UPDATE) {
-    const size_t sm = kNodeWarps * warp_smem<R>(upd_slices(KC), m.LW, 0);
-    allow_smem(k_fct_update<R, KC>, sm);
-    k_fct_update<R, KC><<<grid, block, sm, s>>>(m, a);
-    ++*launches;
-  }
+void launch_ratio(const DMesh& m, const StepPtrs<R>& a, int nw, cudaStream_t s) {
+  dim3 grid((m.N + nw - 1) / nw), block(nw * kWarp);
+  const size_t sm = nw * warp_smem<R>(ratio_slices(KC), m.LW, kClBytes);
+  allow_smem(k_fct_ratio<R, KC>, sm);
+  k_fct_ratio<R, KC><<<grid, block, sm, s>>>(m, a);
+}
+
+template <typename R, int KC>
+void launch_update(const DMesh& m, const StepPtrs<R>& a, int nw, cudaStream_t s) {
+  dim3 grid((m.N + nw - 1) / nw), block(nw * kWarp);
+  const size_t sm = nw * warp_smem<R>(upd_slices(KC), m.LW, 0);
+  allow_smem(k_fct_update<R, KC>, sm);
+  k_fct_update<R, KC><<<grid, block, sm, s>>>(m, a);
 }
 
 template <typename R, int VER, int KC>
-void launch_nofct(const DMesh& m, const StepPtrs<R>& a, cudaStream_t s) {
-  dim3 grid((m.N + kNodeWarps - 1) / kNodeWarps), block(kNodeWarps * kWarp);
-  const size_t sm = kNodeWarps * warp_smem<R>(nofct_slices(KC), m.LW, 0);
+void launch_nofct(const DMesh& m, const StepPtrs<R>& a, int nw, cudaStream_t s) {
+  dim3 grid((m.N + nw - 1) / nw), block(nw * kWarp);
+  const size_t sm = nw * warp_smem<R>(nofct_slices(KC), m.LW, 0);
   allow_smem(k_nofct_update<R, VER, KC>, sm);
   k_nofct_update<R, VER, KC><<<grid, block, sm, s>>>(m, a);
 }
 
 template <typename R, int KC>
-void launch_lo_ver(const DMesh& m, const StepPtrs<R>& a, int ver, cudaStream_t s) {
+void launch_lo_ver(const DMesh& m, const StepPtrs<R>& a, int ver, int nw, cudaStream_t s) {
   switch (ver) {
-    case FGB_VER_QR4C: launch_lo<R, 1, KC>(m, a, s); break;
-    case FGB_VER_CDIFF: launch_lo<R, 2, KC>(m, a, s); break;
-    case FGB_VER_PPM: launch_lo<R, 3, KC>(m, a, s); break;
-    default: launch_lo<R, 0, KC>(m, a, s); break;
+    case FGB_VER_QR4C: launch_lo<R, 1, KC>(m, a, nw, s); break;
+    case FGB_VER_CDIFF: launch_lo<R, 2, KC>(m, a, nw, s); break;
+    case FGB_VER_PPM: launch_lo<R, 3, KC>(m, a, nw, s); break;
+    default: launch_lo<R, 0, KC>(m, a, nw, s); break;
   }
 }
 
 template <typename R, int KC>
-void launch_nofct_ver(const DMesh& m, const StepPtrs<R>& a, int ver, cudaStream_t s) {
+void launch_nofct_ver(const DMesh& m, const StepPtrs<R>& a, int ver, int nw, cudaStream_t s) {
   switch (ver) {
-    case FGB_VER_QR4C: launch_nofct<R, 1, KC>(m, a, s); break;
-    case FGB_VER_CDIFF: launch_nofct<R, 2, KC>(m, a, s); break;
-    case FGB_VER_PPM: launch_nofct<R, 3, KC>(m, a, s); break;
-    default: launch_nofct<R, 0, KC>(m, a, s); break;
+    case FGB_VER_QR4C: launch_nofct<R, 1, KC>(m, a, nw, s); break;
+    case FGB_VER_CDIFF: launch_nofct<R, 2, KC>(m, a, nw, s); break;
+    case FGB_VER_PPM: launch_nofct<R, 3, KC>(m, a, nw, s); break;
+    default: launch_nofct<R, 0, KC>(m, a, nw, s); break;
   }
+}
+
+// Tracers per node-kernel chunk: the requested value if it divides K, else the
+// largest of 4, 2, 1 that does.
+inline int pick_kc(int K, int want) {
+  if ((want == 1 || want == 2 || want == 4) && K % want == 0) return want;
+  return (K % 4 == 0) ? 4 : ((K % 2 == 0) ? 2 : 1);
 }
 
 template <typename R>
@@ -126,8 +133,7 @@ int launch_stages(const DMesh& m, const fgb_step_desc& d, int mask, cudaStream_t
   a.adfh = reinterpret_cast<R*>(ws + wl.off[2]);
   a.lo = reinterpret_cast<R*>(ws + wl.off[3]);
   a.adfv = reinterpret_cast<R*>(ws + wl.off[4]);
-  a.rp = reinterpret_cast<R*>(ws + wl.off[5]);
-  a.rm = reinterpret_cast<R*>(ws + wl.off[6]);
+  a.rpm = reinterpret_cast<R*>(ws + wl.off[5]);
   a.del = static_cast<R*>(d.del);
   a.sT = d.strideT;
   a.sTA = d.TA ? d.strideTA : d.strideT;
@@ -139,6 +145,14 @@ int launch_stages(const DMesh& m, const fgb_step_desc& d, int mask, cudaStream_t
   a.pv = (R)d.pv;
   a.K = K;
   const bool fct = d.lim == FGB_LIM_FCT;
+  auto pick_w = [](int want, int a, int b, int c, int def) {
+    return (want == a || want == b || want == c) ? want : def;
+  };
+  const int ew = pick_w(d.cfg[0], 2, 4, 8, kEdgeWarps);
+  const int nw_lo = pick_w(d.cfg[1], 1, 2, 4, kNodeWarps);
+  const int nw_ratio = pick_w(d.cfg[2], 1, 2, 4, kNodeWarps);
+  const int nw_upd = pick_w(d.cfg[3], 1, 2, 4, kNodeWarps);
+  const int kc_lo = pick_kc(K, d.cfg[4]), kc_ratio = pick_kc(K, d.cfg[5]), kc_upd = pick_kc(K, d.cfg[6]);
   int launches = 0;
   if (mask & FGB_STAGE_VFLUX) {
     dim3 grid((m.E + kEdgeWarps - 1) / kEdgeWarps), block(kEdgeWarps * kWarp);
@@ -146,27 +160,34 @@ int launch_stages(const DMesh& m, const fgb_step_desc& d, int mask, cudaStream_t
     ++launches;
   }
   if (mask & FGB_STAGE_HFLUX) {
-    if (d.hor == FGB_HOR_UPW1) launch_hflux<R, 0>(m, a, fct, s);
-    else if (d.hor == FGB_HOR_MUSCL) launch_hflux<R, 1>(m, a, fct, s);
-    else launch_hflux<R, 2>(m, a, fct, s);
+    if (d.hor == FGB_HOR_UPW1) launch_hflux<R, 0>(m, a, fct, ew, s);
+    else if (d.hor == FGB_HOR_MUSCL) launch_hflux<R, 1>(m, a, fct, ew, s);
+    else launch_hflux<R, 2>(m, a, fct, ew, s);
     ++launches;
   }
-  // Tracers per node-kernel chunk: 4, 2 or 1, a divisor of K.
-  const int KC = (K % 4 == 0) ? 4 : ((K % 2 == 0) ? 2 : 1);
   if (fct) {
     if (mask & FGB_STAGE_LO) {
-      if (KC == 4) launch_lo_ver<R, 4>(m, a, d.ver, s);
-      else if (KC == 2) launch_lo_ver<R, 2>(m, a, d.ver, s);
-      else launch_lo_ver<R, 1>(m, a, d.ver, s);
+      if (kc_lo == 4) launch_lo_ver<R, 4>(m, a, d.ver, nw_lo, s);
+      else if (kc_lo == 2) launch_lo_ver<R, 2>(m, a, d.ver, nw_lo, s);
+      else launch_lo_ver<R, 1>(m, a, d.ver, nw_lo, s);
       ++launches;
     }
-    if (KC == 4) launch_ratio_update<R, 4>(m, a, mask, s, &launches);
-    else if (KC == 2) launch_ratio_update<R, 2>(m, a, mask, s, &launches);
-    else launch_ratio_update<R, 1>(m, a, mask, s, &launches);
+    if (mask & FGB_STAGE_RATIO) {
+      if (kc_ratio == 4) launch_ratio<R, 4>(m, a, nw_ratio, s);
+      else if (kc_ratio == 2) launch_ratio<R, 2>(m, a, nw_ratio, s);
+      else launch_ratio<R, 1>(m, a, nw_ratio, s);
+      ++launches;
+    }
+    if (mask & FGB_STAGE_UPDATE) {
+      if (kc_upd == 4) launch_update<R, 4>(m, a, nw_upd, s);
+      else if (kc_upd == 2) launch_update<R, 2>(m, a, nw_upd, s);
+      else launch_update<R, 1>(m, a, nw_upd, s);
+      ++launches;
+    }
   } else if (mask & FGB_STAGE_UPDATE) {
-    if (KC == 4) launch_nofct_ver<R, 4>(m, a, d.ver, s);
-    else if (KC == 2) launch_nofct_ver<R, 2>(m, a, d.ver, s);
-    else launch_nofct_ver<R, 1>(m, a, d.ver, s);
+    if (kc_upd == 4) launch_nofct_ver<R, 4>(m, a, d.ver, nw_upd, s);
+    else if (kc_upd == 2) launch_nofct_ver<R, 2>(m, a, d.ver, nw_upd, s);
+    else launch_nofct_ver<R, 1>(m, a, d.ver, nw_upd, s);
     ++launches;
   }
   *nlaunch = launches;

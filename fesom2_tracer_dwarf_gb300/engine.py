@@ -58,6 +58,20 @@ class TracerAdvection:
                                           device=self.device)
         self._stats_out = torch.zeros(self.K, 4, dtype=torch.float64, device=self.device)
         self.launches = 0
+        self.cfg = [0] * 8  # launch configuration, see set_launch
+
+    def set_launch(self, cfg):
+        """Launch configuration (fgb_step_desc.cfg): a list of up to 8 ints or a
+        dict with keys edge_warps, node_warps (lo, ratio, update), chunk (lo,
+        ratio, update). Zeros pick the library defaults; results do not depend on it."""
+        if isinstance(cfg, dict):
+            nw = list(cfg.get("node_warps", (0, 0, 0)))
+            kc = list(cfg.get("chunk", (0, 0, 0)))
+            cfg = [int(cfg.get("edge_warps", 0)), *nw, *kc, 0]
+        cfg = [int(c) for c in cfg] + [0] * (8 - len(cfg))
+        if len(cfg) != 8:
+            raise ValueError("a launch configuration has 8 entries")
+        self.cfg = cfg
 
     # ---- configuration -----------------------------------------------------
     def set_schemes(self, hor="UPW1", ver="UPW1", lim="NONE", ph=1.0, pv=1.0):
@@ -124,6 +138,8 @@ class TracerAdvection:
         d.del_ = None
         d.workspace = self.workspace.data_ptr()
         d.workspace_bytes = self.workspace.numel()
+        for i, c in enumerate(self.cfg):
+            d.cfg[i] = c
         return d
 
     def step(self, dt: float, nsteps: int = 1, stages: int = _lib.STAGE_ALL):
@@ -140,19 +156,23 @@ class TracerAdvection:
         return self.T[:, :, : m.nz].double().cpu().numpy()
 
     def workspace_view(self, name: str):
-        """A view of one workspace array: vf, adfh, lo, adfv, rp, rm."""
+        """A view of one workspace array: vf (E,LZ), adfh (K,E,LZ), lo (K,N,LZ),
+        adfv (K,N,LW), rp / rm (K,N,LZ; stored interleaved)."""
         m = self.mesh
         L = _lib.load()
         offs = (ctypes.c_longlong * 7)()
         _lib.check(L.fgb_workspace_offsets(m.handle, _PREC[self.precision], self.K, offs), "offsets")
-        names = ["vf", "(unused)", "adfh", "lo", "adfv", "rp", "rm"]
-        i = names.index(name)
-        shape = {"vf": (m.E, m.LZ), "adfh": (self.K, m.E, m.LZ),
-                 "lo": (self.K, m.N, m.LZ), "adfv": (self.K, m.N, m.LW), "rp": (self.K, m.N, m.LZ),
-                 "rm": (self.K, m.N, m.LZ)}[name]
+        slot = {"vf": 0, "adfh": 2, "lo": 3, "adfv": 4, "rp": 5, "rm": 5}[name]
+        shape = {"vf": (m.E, m.LZ), "adfh": (self.K, m.E, m.LZ), "lo": (self.K, m.N, m.LZ),
+                 "adfv": (self.K, m.N, m.LW), "rp": (self.K, m.N, m.LZ, 2), "rm": (self.K, m.N, m.LZ, 2)}[name]
         n = int(np.prod(shape))
         es = self.T.element_size()
-        return self.workspace[offs[i]: offs[i] + n * es].view(self.dtype).view(shape)
+        v = self.workspace[offs[slot]: offs[slot] + n * es].view(self.dtype).view(shape)
+        if name == "rp":
+            return v[..., 0]
+        if name == "rm":
+            return v[..., 1]
+        return v
 
     def stats(self) -> np.ndarray:
         """(K, 4): min, max, plain sum, NaN count over all layers of the owned nodes."""

@@ -153,7 +153,8 @@ int fgb_mesh_dims(const fgb_mesh* m, int* out8);
 int fgb_mesh_update_vertical(fgb_mesh* m, const fgb_hmesh* h);
 
 /* Workspace of a step: bytes, and the byte offsets of its arrays
- * (vf, an unused slot, adfh, lo, adfv, rp, rm). */
+ * (vf, an unused slot, adfh, lo, adfv, R+/R- interleaved per layer, the
+ * same again). */
 long long fgb_workspace_bytes(const fgb_mesh* m, int precision, int ntracers);
 int fgb_workspace_offsets(const fgb_mesh* m, int precision, int ntracers, long long* out7);
 
@@ -180,6 +181,14 @@ typedef struct {
   void* del;
   void* workspace;
   long long workspace_bytes;
+  /* Launch configuration; 0 picks the default. Results do not depend on it.
+   * cfg[0]     warps (edges) per block of the edge-flux kernel: 2, 4, 8 (default 8)
+   * cfg[1..3]  warps (node columns) per block of the LO, ratio and update
+   *            kernels: 1, 2, 4 (default 4)
+   * cfg[4..6]  tracers per chunk of the same three kernels: 1, 2, 4, used when
+   *            it divides ntracers (default: the largest of 4, 2, 1 that does)
+   * cfg[7]     reserved, 0 */
+  int cfg[8];
 } fgb_step_desc;
 
 /* Full step: vflux, hflux, and the FCT (lo, ratio, update) or plain update. */
