@@ -177,7 +177,8 @@ def build_case(cfg, precision, device, seed=20260301):
     T0 = synthetic.tracers_device(m, cfg["K"], seed, dtype, device)
     eng = TracerAdvection(m, cfg["K"], precision, cfg["hor"], cfg["ver"], cfg["lim"], copy_ab=True, device=device)
     eng.load_padded(T=T0, vel=vel, w=w)
-    return m, eng, T0
+    del T0
+    return m, eng, eng.T.clone()  # initial values in the engine's tracer layout
 
 
 def time_engine(eng, T0, dt, steps, warmup, dist_barrier, per_stage=True):

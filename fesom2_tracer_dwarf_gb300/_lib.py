@@ -47,6 +47,7 @@ class StepDesc(ctypes.Structure):
         ("del_", _vp),
         ("workspace", _vp),
         ("workspace_bytes", ctypes.c_longlong),
+        ("tracer_vec", ctypes.c_int),
         ("cfg", ctypes.c_int * 8),
     ]
 
@@ -65,7 +66,7 @@ ENGINE_SYMBOLS = [
     "fgb_last_error", "fgb_version", "fgb_hmesh_analytic", "fgb_hmesh_free", "fgb_hmesh_sizes", "fgb_hmesh_get",
     "fgb_hmesh_set_vertical", "fgb_mesh_create", "fgb_mesh_free", "fgb_mesh_dims", "fgb_mesh_update_vertical",
     "fgb_workspace_bytes", "fgb_workspace_offsets", "fgb_adv_step", "fgb_adv_stages", "fgb_stats_scratch_bytes",
-    "fgb_tracer_stats", "fgb_last_launch_count", "fgb_static_workspace_bytes", "fgb_adv_step_static",
+    "fgb_tracer_stats", "fgb_tracer_stats_grouped", "fgb_last_launch_count", "fgb_static_workspace_bytes", "fgb_adv_step_static",
 ]
 
 _lib = None
@@ -106,6 +107,8 @@ def load(build_if_missing: bool = True):
         "fgb_adv_step_static": (ctypes.c_int, [_vp, ctypes.POINTER(StepDesc), _vp]),
         "fgb_tracer_stats": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_longlong, ctypes.c_int, _vp, _vp,
                                             _vp]),
+        "fgb_tracer_stats_grouped": (ctypes.c_int, [_vp, _vp, ctypes.c_longlong, ctypes.c_int, ctypes.c_int, _vp,
+                                                    _vp, _vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -37,11 +37,14 @@ def chunk_candidates(K: int):
     return [c for c in CHUNKS if K % c == 0]
 
 
-def stage_candidates(stage: str, K: int):
-    """Candidate knob values per tuned stage: a list of dicts of cfg index -> value."""
+def stage_candidates(stage: str, K: int, precision: str = "fp64"):
+    """Candidate knob values per tuned stage: a list of dicts of cfg index -> value.
+    The FP32 form works one tracer group at a time, so only its block sizes vary."""
     if stage == "hflux":
         return [{0: w} for w in EDGE_WARPS]
     slot = {"lo": 0, "ratio": 1, "update": 2}[stage]
+    if precision == "fp32":
+        return [{1 + slot: w} for w in NODE_WARPS]
     return [{1 + slot: w, 4 + slot: c} for w, c in product(NODE_WARPS, chunk_candidates(K))]
 
 
@@ -113,7 +116,7 @@ def tune(engine, dt: float = 1.0, reps: int = 5, cache_path: str | None = None, 
     best_ms = {}
     for name, mask in stages:
         best = None
-        for cand in stage_candidates(name, engine.K):
+        for cand in stage_candidates(name, engine.K, engine.precision):
             trial = list(cfg)
             for i, v in cand.items():
                 trial[i] = v

@@ -221,7 +221,40 @@ int fgb_mesh_create(const fgb_hmesh* hm, fgb_mesh** out) {
   for (int n = 0; n < h.N; ++n) minl = std::min(minl, h.nlev_nod[n] - h.ulev_nod[n]);
   d.min_layers = minl;
   std::vector<int> elem_nlev(h.nlevels);
-  bool ok = !upload(mm, h.nlev_nod.data(), h.nlev_nod.size(), &d.nlev) &&
+  // FP32 MUSCL tables: triangle weights ((dx, dy) . grad_sca) / 6 of the edge
+  // node and the two other vertices of the up- and downwind triangles.
+  std::vector<int> ftri((size_t)4 * h.E, 0);
+  std::vector<float> fwu((size_t)4 * h.E, 0.f), fwd((size_t)4 * h.E, 0.f);
+  d.fast_tri_ok = 1;
+  for (int e = 0; e < h.E; ++e) {
+    const int n1 = h.edges[2 * e], n2 = h.edges[2 * e + 1];
+    const int tu = h.edge_updn[2 * e], td = h.edge_updn[2 * e + 1];
+    int* o = &ftri[(size_t)4 * e];
+    o[0] = o[1] = n1;
+    o[2] = o[3] = n2;
+    if (tu < 0 || td < 0) continue;
+    const double ex = h.edge_dxa[2 * e], ey = h.edge_dxa[2 * e + 1];
+    auto fill = [&](int el, int node, int* oo, float* w) {
+      int k = 0;
+      bool found = false;
+      for (int j = 0; j < 3; ++j) {
+        const int v = h.elem_nodes[3 * el + j];
+        const double wv = (ex * h.grad_sca[6 * (size_t)el + j] + ey * h.grad_sca[6 * (size_t)el + 3 + j]) / 6.0;
+        if (v == node && !found) {
+          w[0] = (float)wv;
+          found = true;
+        } else if (k < 2) {
+          oo[k] = v;
+          w[1 + k] = (float)wv;
+          ++k;
+        }
+      }
+      return found;
+    };
+    if (!fill(tu, n1, o, &fwu[(size_t)4 * e]) || !fill(td, n2, o + 2, &fwd[(size_t)4 * e])) d.fast_tri_ok = 0;
+  }
+  bool ok = !upload(mm, ftri.data(), ftri.size(), &d.f_tri) && !upload(mm, fwu.data(), fwu.size(), &d.f_wu) &&
+            !upload(mm, fwd.data(), fwd.size(), &d.f_wd) &&!upload(mm, h.nlev_nod.data(), h.nlev_nod.size(), &d.nlev) &&
             !upload(mm, h.ulev_nod.data(), h.ulev_nod.size(), &d.ulev) &&
             !upload(mm, h.nboundary_lay.data(), h.nboundary_lay.size(), &d.nbl) &&
             !upload(mm, h.ne_ptr.data(), h.ne_ptr.size(), &d.ne_ptr) &&
@@ -322,17 +355,19 @@ namespace {
 constexpr int kStatBlocks = 1024;
 constexpr int kStatThreads = 256;
 
+// Tracer t of a batch in groups of KV (KV = 1: one tracer per stride).
 template <typename R>
-__global__ void k_stats_partial(const R* __restrict__ T, long long sT, int N, int nz, int LZ, double* __restrict__ part) {
+__global__ void k_stats_partial(const R* __restrict__ T, long long sT, int KV, int N, int nz, int LZ,
+                                double* __restrict__ part) {
   const int t = blockIdx.y;
-  const R* base = T + t * sT;
+  const R* base = T + (t / KV) * sT + t % KV;
   const long long total = (long long)N * nz;
   const long long per = (total + gridDim.x - 1) / gridDim.x;
   const long long lo = blockIdx.x * per, hi = min(total, lo + per);
   double mn = INFINITY, mx = -INFINITY, sm = 0.0, nan = 0.0;
   for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
     const long long n = i / nz, k = i - n * nz;
-    const double v = (double)base[n * LZ + k];
+    const double v = (double)base[(n * LZ + k) * KV];
     if (v != v) { nan += 1.0; continue; }
     mn = fmin(mn, v);
     mx = fmax(mx, v);
@@ -382,11 +417,28 @@ int fgb_tracer_stats(const fgb_mesh* m, int precision, const void* T, long long 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   dim3 grid(kStatBlocks, ntracers);
   if (precision == FGB_FP32)
-    k_stats_partial<float><<<grid, kStatThreads, 0, s>>>(static_cast<const float*>(T), strideT, m->d.N, m->d.nz,
+    k_stats_partial<float><<<grid, kStatThreads, 0, s>>>(static_cast<const float*>(T), strideT, 1, m->d.N, m->d.nz,
                                                          m->d.LZ, static_cast<double*>(scratch));
   else
-    k_stats_partial<double><<<grid, kStatThreads, 0, s>>>(static_cast<const double*>(T), strideT, m->d.N, m->d.nz,
-                                                          m->d.LZ, static_cast<double*>(scratch));
+    k_stats_partial<double><<<grid, kStatThreads, 0, s>>>(static_cast<const double*>(T), strideT, 1, m->d.N,
+                                                          m->d.nz, m->d.LZ, static_cast<double*>(scratch));
+  k_stats_final<<<ntracers, 32, 0, s>>>(static_cast<const double*>(scratch), kStatBlocks, out_dev);
+  cudaError_t ce = cudaGetLastError();
+  if (ce != cudaSuccess) { set_error(std::string("stats launch failed: ") + cudaGetErrorString(ce)); return -1; }
+  return 0;
+}
+
+int fgb_tracer_stats_grouped(const fgb_mesh* m, const float* T, long long strideT, int ntracers, int tracer_vec,
+                             void* scratch, double* out_dev, void* stream) {
+  const int KV = tracer_vec <= 1 ? 1 : tracer_vec;
+  if (!m || !T || !scratch || !out_dev || ntracers < 1 || (KV != 2 && KV != 4 && KV != 1) || ntracers % KV) {
+    set_error("bad argument");
+    return -1;
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  dim3 grid(kStatBlocks, ntracers);
+  k_stats_partial<float><<<grid, kStatThreads, 0, s>>>(T, strideT, KV, m->d.N, m->d.nz, m->d.LZ,
+                                                       static_cast<double*>(scratch));
   k_stats_final<<<ntracers, 32, 0, s>>>(static_cast<const double*>(scratch), kStatBlocks, out_dev);
   cudaError_t ce = cudaGetLastError();
   if (ce != cudaSuccess) { set_error(std::string("stats launch failed: ") + cudaGetErrorString(ce)); return -1; }

@@ -47,6 +47,13 @@ struct DMesh {
   const int* edge_lev;    // (E,4)
   const int* edge_gm;     // (E,2)
   const int* edge_order;  // (E) order in which edge kernels visit the edges
+  // FP32 form, MUSCL/MFCT: per edge the two other vertices of the upwind and
+  // downwind triangles (E,4) and the triangles' edge-direction weights (E,4)
+  // each; valid when fast_tri_ok (each triangle holds its edge node).
+  const int* f_tri;
+  const float* f_wu;
+  const float* f_wd;
+  int fast_tri_ok;
   GeoPtrs<double> g64;
   GeoPtrs<float> g32;
 };
@@ -70,5 +77,32 @@ struct StepPtrs {
   int K;            // tracers in this launch
   R dt, ph, pv;
 };
+
+namespace fast {
+// Pointers of one launch. Group g of a per-tracer array starts at
+// base + g * stride (floats); offsets inside a group are in units of KV floats.
+struct FastPtrs {
+  float* T;
+  const float* TA;
+  float* TAout;
+  const float* vel;  // (M,LZ,2)
+  const float* w;    // (N,LW)
+  const float* we;   // (N,LW)
+  float* vf;         // (E,LZ)
+  float* adfh;       // (G,E,LZ,KV)
+  float* lo;         // (G,N,LZ,KV)
+  float* adfv;       // (G,N,LW,KV)
+  float* rpm;        // (G,N,LZ,2,KV): R+ then R- per layer
+  float* del;        // optional (G,N,LZ,KV)
+  long long gT, gTA, gE, gN, gW;  // group strides (floats)
+  int G;
+  float dt, ph, pv;
+};
+
+// Launch shape of one FP32 call.
+struct LaunchArgs {
+  int mask, edge_warps, nw_lo, nw_ratio, nw_upd, hor, ver, fct;
+};
+}  // namespace fast
 
 }  // namespace fgb

@@ -1,0 +1,1019 @@
+// FP32 form of the tracer-advection step (do_oce_adv_tra,
+// lib/oce_adv_tra_driver.F90:23-294, and the caller's tendency update) on the
+// tracer-grouped layout.
+//
+// Layout: tracers are stored in groups of KV (1, 2 or 4) that are contiguous
+// per node-layer: value (t, n, k) lives at
+//   T[(t / KV) * strideT + (n * LZ + k) * KV + t % KV],
+// so one 16-byte load brings the four tracers of a node-layer. The edge and
+// node work arrays of the step use the same grouping. With KV = 1 this is the
+// per-tracer layout of the FP64 form.
+//
+// Work decomposition: one warp per edge (edge fluxes) or per node column
+// (node kernels); lane l handles layers l and l + 32 of each 64-layer pass,
+// so every warp load is one contiguous row. What does not depend on the
+// tracer is computed once per layer or interface and applied to the KV
+// tracers of a group: the PPM and QR4C interface coefficients, the MUSCL
+// edge weights (precomputed per edge at mesh upload), the upwind coefficients
+// of the low-order edge fluxes and the dt / area factors of the flux
+// divergence. Arithmetic is regrouped accordingly, so results agree with the
+// reference order to FP32 rounding, not bit for bit. The active-layer tests of
+// the edge gathers are dropped: the edge volume fluxes and the antidiffusive
+// fluxes are stored as exact zeros outside an edge's layers, so those terms
+// add zero; tracer values at stored layers below a node's bottom must
+// therefore be finite.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+
+#include "fgb_device.hpp"
+
+namespace fgb {
+namespace fast {
+
+constexpr int kW = 32;
+constexpr int kSlices = 2;              // layers per lane per pass
+constexpr int kPass = kW * kSlices;     // layers per pass
+constexpr int kMaxDegF = 16;            // incident edges staged per node
+constexpr int kMaxClF = 24;             // cluster nodes staged per node
+
+// ---------------------------------------------------------------------------
+// KV tracer values of one node-layer (or edge-layer, or interface).
+// ---------------------------------------------------------------------------
+template <int KV>
+struct alignas(4 * KV) V {
+  float v[KV];
+};
+
+template <int KV>
+__device__ __forceinline__ V<KV> ld(const float* __restrict__ base, unsigned i) {
+  return reinterpret_cast<const V<KV>*>(base)[i];
+}
+template <int KV>
+__device__ __forceinline__ void st(float* base, unsigned i, const V<KV>& a) {
+  reinterpret_cast<V<KV>*>(base)[i] = a;
+}
+template <int KV>
+__device__ __forceinline__ V<KV> splat(float s) {
+  V<KV> r;
+#pragma unroll
+  for (int j = 0; j < KV; ++j) r.v[j] = s;
+  return r;
+}
+
+// Element-wise arithmetic; pairs of tracers use the packed FP32x2 instructions.
+#define FGB_F2(x, j) make_float2((x).v[j], (x).v[(j) + 1])
+template <int KV>
+__device__ __forceinline__ V<KV> add(const V<KV>& a, const V<KV>& b) {
+  V<KV> r;
+  if constexpr (KV % 2 == 0) {
+#pragma unroll
+    for (int j = 0; j < KV; j += 2) {
+      const float2 t = __fadd2_rn(FGB_F2(a, j), FGB_F2(b, j));
+      r.v[j] = t.x;
+      r.v[j + 1] = t.y;
+    }
+  } else {
+    r.v[0] = __fadd_rn(a.v[0], b.v[0]);
+  }
+  return r;
+}
+template <int KV>
+__device__ __forceinline__ V<KV> sub(const V<KV>& a, const V<KV>& b) {
+  V<KV> r;
+  if constexpr (KV % 2 == 0) {
+#pragma unroll
+    for (int j = 0; j < KV; j += 2) {
+      const float2 t = __fadd2_rn(FGB_F2(a, j), make_float2(-b.v[j], -b.v[j + 1]));
+      r.v[j] = t.x;
+      r.v[j + 1] = t.y;
+    }
+  } else {
+    r.v[0] = __fsub_rn(a.v[0], b.v[0]);
+  }
+  return r;
+}
+template <int KV>
+__device__ __forceinline__ V<KV> mul(const V<KV>& a, const V<KV>& b) {
+  V<KV> r;
+  if constexpr (KV % 2 == 0) {
+#pragma unroll
+    for (int j = 0; j < KV; j += 2) {
+      const float2 t = __fmul2_rn(FGB_F2(a, j), FGB_F2(b, j));
+      r.v[j] = t.x;
+      r.v[j + 1] = t.y;
+    }
+  } else {
+    r.v[0] = __fmul_rn(a.v[0], b.v[0]);
+  }
+  return r;
+}
+// a * b + c
+template <int KV>
+__device__ __forceinline__ V<KV> fma(const V<KV>& a, const V<KV>& b, const V<KV>& c) {
+  V<KV> r;
+  if constexpr (KV % 2 == 0) {
+#pragma unroll
+    for (int j = 0; j < KV; j += 2) {
+      const float2 t = __ffma2_rn(FGB_F2(a, j), FGB_F2(b, j), FGB_F2(c, j));
+      r.v[j] = t.x;
+      r.v[j + 1] = t.y;
+    }
+  } else {
+    r.v[0] = __fmaf_rn(a.v[0], b.v[0], c.v[0]);
+  }
+  return r;
+}
+// a * s + c with a scalar s
+template <int KV>
+__device__ __forceinline__ V<KV> fmas(const V<KV>& a, float s, const V<KV>& c) {
+  return fma(a, splat<KV>(s), c);
+}
+template <int KV>
+__device__ __forceinline__ V<KV> muls(const V<KV>& a, float s) {
+  return mul(a, splat<KV>(s));
+}
+#undef FGB_F2
+
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+  float d;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+  float d;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+
+// ---------------------------------------------------------------------------
+// Volume flux through each edge segment (lib/oce_adv_tra_hor.F90:174,194,
+// 215-216). With ulevels = 1 the segments reduce to: element 1 contributes at
+// layers 1..nl1, element 2 at layers 1..nl2.
+// ---------------------------------------------------------------------------
+static __global__ void __launch_bounds__(256) kf_vflux(DMesh m, const float* __restrict__ vel, float* __restrict__ vf) {
+  const int lane = threadIdx.x & (kW - 1);
+  const int e = blockIdx.x * (blockDim.x / kW) + (threadIdx.x / kW);
+  if (e >= m.E) return;
+  const GeoPtrs<float>& g = m.g32;
+  const int nl1 = m.edge_lev[4 * e + 1], nl2 = m.edge_lev[4 * e + 3];
+  const int el1 = m.edge_tri[2 * e], el2 = m.edge_tri[2 * e + 1];
+  const float4 cr = reinterpret_cast<const float4*>(g.edge_cross)[e];
+  const unsigned LZ = m.LZ;
+  const float2* __restrict__ uv = reinterpret_cast<const float2*>(vel);
+  for (unsigned k = lane; k < LZ; k += kW) {
+    const int z = (int)k + 1;
+    float v = 0.f;
+    if (z <= nl1) {
+      const float2 u = uv[el1 * LZ + k];
+      v = (-(u.y * cr.x) + u.x * cr.y) * g.helem[el1 * LZ + k];
+    }
+    if (z <= nl2) {
+      const float2 u = uv[el2 * LZ + k];
+      v = v + (u.y * cr.z - u.x * cr.w) * g.helem[el2 * LZ + k];
+    }
+    vf[e * LZ + k] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Horizontal edge fluxes of all tracer groups (FCT: HO(T_AB) - LO(T), else
+// HO). HOR: 0 UPW1 (lib/oce_adv_tra_hor.F90:218-220), 1 MUSCL
+// (:454-497, with the nboundary_lay mask), 2 MFCT (:748-790).
+//
+// MUSCL reconstruction at node 1 with the upwind triangle's gradient g_u:
+//   Tm1 = T1 + c1 * (2 (T2 - T1) + (dx, dy) . g_u) / 6
+//       = T1 + c1 * ((T2 - T1) / 3 + sum_v w_v T_v),
+// the weights w_v = ((dx, dy) . grad_sca_v) / 6 of the triangle's vertices
+// taken from the per-edge table; likewise Tm2 from the downwind triangle.
+// Layers outside the triangles' common window use the area-weighted mean
+// gradient of the elements around each node (lib/oce_muscl_adv.F90:393-410).
+// ---------------------------------------------------------------------------
+template <int KV>
+__device__ __forceinline__ void node_grad(const DMesh& m, const float* __restrict__ TA, int n, unsigned k,
+                                          V<KV>& gx, V<KV>& gy) {
+  const GeoPtrs<float>& g = m.g32;
+  const unsigned LZ = m.LZ;
+  const int z = (int)k + 1;
+  float tvol = 0.f;
+  V<KV> tx = splat<KV>(0.f), ty = splat<KV>(0.f);
+  for (int j = m.nie_ptr[n]; j < m.nie_ptr[n + 1]; ++j) {
+    const int el = m.nie_idx[j];
+    if (m.elem_nlev[el] - 1 < z) continue;
+    const int a = m.elem_nodes[3 * el], b = m.elem_nodes[3 * el + 1], c = m.elem_nodes[3 * el + 2];
+    const float* gs = g.grad_sca + 6 * (size_t)el;
+    const V<KV> ta = ld<KV>(TA, a * LZ + k), tb = ld<KV>(TA, b * LZ + k), tc = ld<KV>(TA, c * LZ + k);
+    const V<KV> ex = fmas(tc, gs[2], fmas(tb, gs[1], muls(ta, gs[0])));
+    const V<KV> ey = fmas(tc, gs[5], fmas(tb, gs[4], muls(ta, gs[3])));
+    const float ar = g.elem_area[el];
+    tvol += ar;
+    tx = fmas(ex, ar, tx);
+    ty = fmas(ey, ar, ty);
+  }
+  const float inv = 1.f / tvol;
+  gx = muls(tx, inv);
+  gy = muls(ty, inv);
+}
+
+template <int HOR, bool FCT, int KV>
+__global__ void __launch_bounds__(256, 2) kf_hflux(DMesh m, FastPtrs a) {
+  const int lane = threadIdx.x & (kW - 1);
+  const int w = blockIdx.x * (blockDim.x / kW) + (threadIdx.x / kW);
+  if (w >= m.E) return;
+  const int e = m.edge_order ? m.edge_order[w] : w;
+  const unsigned LZ = m.LZ;
+  const int nz = m.nz;
+  const int n1 = m.edge_nodes[2 * e], n2 = m.edge_nodes[2 * e + 1];
+  const int hi = max(m.edge_lev[4 * e + 1], m.edge_lev[4 * e + 3]);
+  int4 tri = make_int4(0, 0, 0, 0);
+  float4 wu = make_float4(0.f, 0.f, 0.f, 0.f), wd = wu;
+  int gm0 = -1, gm1 = -1, nb1 = 0, nb2 = 0;
+  float ex = 0.f, ey = 0.f;
+  if (HOR != 0) {
+    gm0 = m.edge_gm[2 * e];
+    gm1 = m.edge_gm[2 * e + 1];
+    nb1 = m.nbl[n1];
+    nb2 = m.nbl[n2];
+    ex = m.g32.edge_dxa[2 * e];
+    ey = m.g32.edge_dxa[2 * e + 1];
+    if (gm0 >= 0) {
+      tri = reinterpret_cast<const int4*>(m.f_tri)[e];
+      wu = reinterpret_cast<const float4*>(m.f_wu)[e];
+      wd = reinterpret_cast<const float4*>(m.f_wd)[e];
+    }
+  }
+  const float A = 0.5f * (1.f - a.ph);
+  const bool ta_sep = a.TA != a.T;
+  for (unsigned base = 0; base < LZ; base += kPass) {
+    unsigned kk[kSlices];
+    bool in[kSlices], act[kSlices], tri_ok[kSlices];
+    float vp[kSlices], vm[kSlices], B[kSlices], c1[kSlices], c2[kSlices];
+    bool all_tri = true;
+#pragma unroll
+    for (int i = 0; i < kSlices; ++i) {
+      const unsigned k = base + lane + kW * i;
+      in[i] = k < LZ;
+      kk[i] = in[i] ? k : LZ - 1;
+      const int z = (int)k + 1;
+      act[i] = in[i] && (int)k < nz && z <= hi;
+      const float v = a.vf[e * LZ + kk[i]];
+      vp[i] = v + fabsf(v);
+      vm[i] = v - fabsf(v);
+      B[i] = (v * a.ph) * 0.5f;
+      tri_ok[i] = gm0 >= 0 && z >= gm0 && z <= gm1 - 1;
+      c1[i] = (HOR == 2 || nb1 - z >= 0) ? 1.f : 0.f;
+      c2[i] = (HOR == 2 || nb2 - z >= 0) ? 1.f : 0.f;
+      if (HOR != 0 && act[i] && !tri_ok[i]) all_tri = false;
+    }
+    const bool fast_tri = __all_sync(0xffffffffu, all_tri);
+    for (int gi = 0; gi < a.G; ++gi) {
+      const float* __restrict__ Tg = a.T + gi * a.gT;
+      const float* __restrict__ TAg = ta_sep ? a.TA + gi * a.gTA : Tg;
+      float* __restrict__ out = a.adfh + gi * a.gE;
+      V<KV> s1[kSlices], s2[kSlices], r1[kSlices], r2[kSlices];
+#pragma unroll
+      for (int i = 0; i < kSlices; ++i) {
+        s1[i] = ld<KV>(TAg, n1 * LZ + kk[i]);
+        s2[i] = ld<KV>(TAg, n2 * LZ + kk[i]);
+        if (FCT && ta_sep) {
+          r1[i] = ld<KV>(Tg, n1 * LZ + kk[i]);
+          r2[i] = ld<KV>(Tg, n2 * LZ + kk[i]);
+        } else {
+          r1[i] = s1[i];
+          r2[i] = s2[i];
+        }
+      }
+      V<KV> h[kSlices];
+      if (HOR == 0) {
+#pragma unroll
+        for (int i = 0; i < kSlices; ++i) h[i] = muls(fmas(s2[i], vm[i], muls(s1[i], vp[i])), -0.5f);
+      } else {
+        V<KV> tm1[kSlices], tm2[kSlices];
+        if (fast_tri) {
+          V<KV> u1[kSlices], u2[kSlices], d1[kSlices], d2[kSlices];
+#pragma unroll
+          for (int i = 0; i < kSlices; ++i) {
+            u1[i] = ld<KV>(TAg, tri.x * LZ + kk[i]);
+            u2[i] = ld<KV>(TAg, tri.y * LZ + kk[i]);
+            d1[i] = ld<KV>(TAg, tri.z * LZ + kk[i]);
+            d2[i] = ld<KV>(TAg, tri.w * LZ + kk[i]);
+          }
+#pragma unroll
+          for (int i = 0; i < kSlices; ++i) {
+            const V<KV> dT3 = muls(sub(s2[i], s1[i]), 1.f / 3.f);
+            const V<KV> p1 = fmas(u2[i], wu.z, fmas(u1[i], wu.y, fmas(s1[i], wu.x, dT3)));
+            const V<KV> p2 = fmas(d2[i], wd.z, fmas(d1[i], wd.y, fmas(s2[i], wd.x, dT3)));
+            tm1[i] = fmas(p1, c1[i], s1[i]);
+            tm2[i] = fmas(p2, -c2[i], s2[i]);
+          }
+        } else {
+#pragma unroll
+          for (int i = 0; i < kSlices; ++i) {
+            const V<KV> dT3 = muls(sub(s2[i], s1[i]), 1.f / 3.f);
+            V<KV> p1, p2;
+            if (tri_ok[i]) {
+              const V<KV> u1 = ld<KV>(TAg, tri.x * LZ + kk[i]), u2 = ld<KV>(TAg, tri.y * LZ + kk[i]);
+              const V<KV> d1 = ld<KV>(TAg, tri.z * LZ + kk[i]), d2 = ld<KV>(TAg, tri.w * LZ + kk[i]);
+              p1 = fmas(u2, wu.z, fmas(u1, wu.y, fmas(s1[i], wu.x, dT3)));
+              p2 = fmas(d2, wd.z, fmas(d1, wd.y, fmas(s2[i], wd.x, dT3)));
+            } else if (act[i]) {
+              V<KV> gx, gy;
+              node_grad<KV>(m, TAg, n1, kk[i], gx, gy);
+              p1 = fmas(fmas(gy, ey, muls(gx, ex)), 1.f / 6.f, dT3);
+              node_grad<KV>(m, TAg, n2, kk[i], gx, gy);
+              p2 = fmas(fmas(gy, ey, muls(gx, ex)), 1.f / 6.f, dT3);
+            } else {
+              p1 = splat<KV>(0.f);
+              p2 = p1;
+            }
+            tm1[i] = fmas(p1, c1[i], s1[i]);
+            tm2[i] = fmas(p2, -c2[i], s2[i]);
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < kSlices; ++i) {
+          const V<KV> cho = fmas(tm2[i], vm[i], muls(tm1[i], vp[i]));
+          h[i] = fmas(add(tm1[i], tm2[i]), -B[i], muls(cho, -A));
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < kSlices; ++i) {
+        V<KV> r = h[i];
+        if (FCT) r = fmas(fmas(r2[i], vm[i], muls(r1[i], vp[i])), 0.5f, r);
+        if (!act[i]) r = splat<KV>(0.f);
+        if (in[i]) st<KV>(out, e * LZ + kk[i], r);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Column staging and vertical fluxes (lib/oce_adv_tra_ver.F90:248-712).
+// ---------------------------------------------------------------------------
+struct ColF {
+  const float* W;
+  const float* area;
+  const float* hn;   // PPM
+  const float* hnn;  // PPM
+  const float* Z;    // QR4C
+  const float* zb;   // QR4C
+};
+
+__device__ __forceinline__ void stage_f(float* dst, const float* __restrict__ src, int n, int lane) {
+  for (int k = lane; k < n; k += kW) dst[k] = src[k];
+}
+template <int KV>
+__device__ __forceinline__ void stage_v(V<KV>* dst, const float* __restrict__ src, unsigned first, int n, int lane) {
+  for (int k = lane; k < n; k += kW) dst[k] = ld<KV>(src, first + k);
+}
+
+// PPM slope of layer j (0-based) from layers j-1, j, j+1, limited (the
+// deltaj / deltaj+1 of lib/oce_adv_tra_ver.F90:525-545).
+template <int KV>
+__device__ __forceinline__ V<KV> ppm_slope(const V<KV>* T, const float* hnn, int j) {
+  const float dzm = hnn[j - 1], dz = hnn[j], dzp = hnn[j + 1];
+  const float f = dz / (dzm + dz + dzp);
+  const float s1 = f * ((2.f * dzm + dz) / (dzp + dz));
+  const float s0 = f * ((dz + 2.f * dzp) / (dzm + dz));
+  V<KV> r;
+#pragma unroll
+  for (int t = 0; t < KV; ++t) {
+    const float d1 = T[j + 1].v[t] - T[j].v[t], d0 = T[j].v[t] - T[j - 1].v[t];
+    const float s = s1 * d1 + s0 * d0;
+    r.v[t] = (d1 * d0 > 0.f) ? copysignf(min3f(fabsf(s), 2.f * fabsf(d1), 2.f * fabsf(d0)), s) : 0.f;
+  }
+  return r;
+}
+
+// PPM edge value at interface z (1-based), lib/oce_adv_tra_ver.F90:510-594;
+// the later assignment wins where the special cases coincide.
+template <int KV>
+__device__ __forceinline__ V<KV> ppm_edge(const V<KV>* T, const V<KV>* D, const ColF& c, int z, int nzmin,
+                                          int nzmax) {
+  if (z >= nzmin + 2 && z <= nzmax - 2) {
+    const int j0 = z - 2;  // layer above the interface
+    const float dzm = c.hnn[j0 - 1], dz = c.hnn[j0], dzp = c.hnn[j0 + 1], dzpp = c.hnn[j0 + 2];
+    const float c0 = dz / (dz + dzp);
+    const float c1 = ((2.f * dzp) * dz / (dz + dzp)) * ((dzm + dz) / (2.f * dz + dzp) - (dzpp + dzp) / (2.f * dzp + dz));
+    const float ci = 1.f / (dzm + dz + dzp + dzpp);
+    const float P = c0 + ci * c1;
+    const float Q2 = ci * (dz * (dzm + dz) / (2.f * dz + dzp));
+    const float Q3 = ci * (dzp * (dzp + dzpp) / (dz + 2.f * dzp));
+    const V<KV> d = sub(T[j0 + 1], T[j0]);
+    return fmas(D[j0], Q3, fmas(D[j0 + 1], -Q2, fmas(d, P, T[j0])));
+  }
+  if (z == nzmax) return T[nzmax - 2];
+  if (z == nzmax - 1) {
+    const float s = copysignf(1.f, c.W[nzmax - 2]);
+    return fmas(T[nzmax - 2], fmaxf(s, 0.f), muls(T[nzmax - 3], -fminf(s, 0.f)));
+  }
+  if (z == nzmin + 1) return muls(add(T[nzmin - 1], T[nzmin]), 0.5f);
+  return T[nzmin - 1];
+}
+
+// PPM flux of layer L (1-based) through its upper (W > 0) or lower (W < 0)
+// interface, lib/oce_adv_tra_ver.F90:598-632; x = min(|W| dt / h, 1).
+template <int KV>
+__device__ __forceinline__ V<KV> ppm_flux(const V<KV>& aL0, const V<KV>& aR0, const V<KV>& T0, float x, bool upper,
+                                          float aw) {
+  const float hx = 0.5f * x, cx = 1.f - (2.f / 3.f) * x;
+  V<KV> r;
+#pragma unroll
+  for (int t = 0; t < KV; ++t) {
+    float aL = aL0.v[t], aR = aR0.v[t];
+    const float t0 = T0.v[t];
+    if ((aR - t0) * (t0 - aL) <= 0.f) {
+      aL = t0;
+      aR = t0;
+    }
+    const float dd = (aR - aL) * (aR - aL) * (1.f / 6.f);
+    if ((aR - aL) * (t0 - 0.5f * (aL + aR)) > dd) aL = 3.f * t0 - 2.f * aR;
+    if ((aR - aL) * (t0 - 0.5f * (aR + aL)) < -((aR - aL) * (aR - aL) * (1.f / 6.f))) aR = 3.f * t0 - 2.f * aL;
+    const float aj = 6.f * (t0 - 0.5f * (aL + aR));
+    const float tv = upper ? -aL - hx * ((aR - aL) + cx * aj) : -aR + hx * ((aR - aL) - cx * aj);
+    r.v[t] = tv * aw;
+  }
+  return r;
+}
+
+// Vertical flux of the column at every interface into out[iz], minus fold[iz]
+// (fold = nullptr: zero). VER: 0 UPW1, 1 QR4C, 2 CDIFF, 3 PPM. T holds the
+// column's layers; D and TV are scratch columns for PPM.
+template <int VER, int KV>
+__device__ void vert_flux(const ColF& c, const V<KV>* T, V<KV>* D, V<KV>* TV, const V<KV>* fold, V<KV>* out, int nl,
+                          int nzmin, int nzmax, float num_ord, float dt, int lane) {
+  if (VER == 3) {
+    for (int j = lane; j < nl; j += kW)
+      if (j >= nzmin && j <= nzmax - 3) D[j] = ppm_slope<KV>(T, c.hnn, j);
+    __syncwarp();
+    for (int iz = lane; iz < nl; iz += kW) {
+      const int z = iz + 1;
+      if (z >= nzmin && z <= nzmax) TV[iz] = ppm_edge<KV>(T, D, c, z, nzmin, nzmax);
+    }
+    __syncwarp();
+  }
+  for (int iz = lane; iz < nl; iz += kW) {
+    const int z = iz + 1;
+    const V<KV> f0 = fold ? fold[iz] : splat<KV>(0.f);
+    V<KV> r = f0;
+    if (z >= nzmin && z <= nzmax) {
+      const float W = c.W[iz], ar = c.area[iz];
+      if (VER == 0) {
+        if (z == nzmin) r = sub(muls(T[z - 1], -(W * ar)), f0);
+        else if (z == nzmax) r = sub(splat<KV>(0.f), f0);
+        else
+          r = sub(fmas(T[z - 2], -0.5f * (W - fabsf(W)) * ar, muls(T[z - 1], -0.5f * (W + fabsf(W)) * ar)), f0);
+      } else if (VER == 1) {
+        if (z == nzmin) {
+          r = sub(muls(T[z - 1], -(W * ar)), f0);
+        } else if (z == nzmax) {
+          r = sub(splat<KV>(0.f), f0);
+        } else if (z == nzmin + 1 || z == nzmax - 1) {
+          const V<KV> x = muls(add(T[z - 2], T[z - 1]), -0.5f * W * ar);
+          r = sub(x, f0);
+          if (nzmin + 1 == nzmax - 1) r = sub(x, r);  // written twice (lib/oce_adv_tra_ver.F90:405-411)
+        } else {
+          const float Z0 = c.Z[z - 1], Zm1 = c.Z[z - 2], Zm2 = c.Z[z - 3], Zp1 = c.Z[z];
+          const float ic = 1.f / (Zm1 - Z0), iu = 1.f / (Z0 - Zp1), idn = 1.f / (Zm2 - Zm1);
+          const float zb = c.zb[z - 1];
+          const float a1 = (zb - Z0) * (1.f / 3.f), a2 = (zb - Zm1) * (1.f / 3.f);
+          const float wp = W + fabsf(W), wm = W - fabsf(W);
+          const float cA = -(0.5f * (1.f - num_ord)) * ar, cB = -(num_ord * 0.5f) * W * ar;
+          const V<KV> T0 = T[z - 1], Tm1 = T[z - 2], Tm2 = T[z - 3], Tp1 = T[z];
+          const V<KV> qc = muls(sub(Tm1, T0), ic), qu = muls(sub(T0, Tp1), iu), qd = muls(sub(Tm2, Tm1), idn);
+          const V<KV> tm1 = fmas(fmas(qc, 2.f, qu), a1, T0);
+          const V<KV> tm2 = fmas(fmas(qc, 2.f, qd), a2, Tm1);
+          const V<KV> tm = fmas(tm2, wm, muls(tm1, wp));
+          r = sub(fmas(add(tm1, tm2), cB, muls(tm, cA)), f0);
+        }
+      } else if (VER == 2) {
+        const int nzc = nzmax - 1;  // lib/oce_adv_tra_ver.F90:689
+        if (z == nzmin) r = sub(muls(T[z - 1], -(W * ar)), f0);
+        else if (z <= nzc) r = sub(muls(add(T[z - 2], T[z - 1]), -0.5f * W * ar), f0);
+      } else {
+        V<KV> tvert = splat<KV>(0.f);
+        if (z == nzmin) {
+          tvert = muls(TV[nzmin - 1], -(W * ar));
+        } else if (z < nzmax) {
+          if (W > 0.f) {
+            const float x = fminf(W * dt / c.hn[z - 1], 1.f);
+            tvert = ppm_flux<KV>(TV[z - 1], TV[z], T[z - 1], x, true, ar * W);
+          } else if (W < 0.f) {
+            const float x = fminf(-(W * dt / c.hn[z - 2]), 1.f);
+            tvert = ppm_flux<KV>(TV[z - 2], TV[z - 1], T[z - 2], x, false, ar * W);
+          }
+        }
+        r = sub(tvert, f0);
+      }
+    }
+    out[iz] = r;
+  }
+  __syncwarp();
+}
+
+// ---------------------------------------------------------------------------
+// Node kernels: incident edges staged as (edge code, other node).
+// ---------------------------------------------------------------------------
+struct NbrF {
+  const int2* s;
+  int j0, deg;
+  __device__ __forceinline__ int2 get(const DMesh& m, int j) const {
+    return deg <= kMaxDegF ? s[j] : make_int2(m.ne_code[j0 + j], m.ne_other[j0 + j]);
+  }
+};
+__device__ __forceinline__ NbrF stage_nbrs_f(const DMesh& m, int n, int2* s, int lane) {
+  NbrF L{s, m.ne_ptr[n], m.ne_ptr[n + 1] - m.ne_ptr[n]};
+  if (L.deg <= kMaxDegF)
+    for (int j = lane; j < L.deg; j += kW) s[j] = make_int2(m.ne_code[L.j0 + j], m.ne_other[L.j0 + j]);
+  return L;
+}
+
+// Shared memory of one warp: floats of the scalar columns, vectors, the edge
+// list and the cluster list, each 16-byte aligned.
+__host__ __device__ constexpr int al4(int v) { return (v + 3) / 4 * 4; }
+template <int KV>
+__host__ __device__ constexpr size_t warp_bytes(int scalar_cols, int vec_cols, int LW) {
+  return (size_t)scalar_cols * al4(LW) * 4 + (size_t)vec_cols * LW * KV * 4 + kMaxDegF * sizeof(int2) +
+         kMaxClF * sizeof(int2);
+}
+// Shared columns per warp (scalars, vectors) of each kernel, from the flags
+// that decide which of them a launch needs.
+struct LoCols {
+  int scal, vec;
+};
+__host__ __device__ constexpr LoCols lo_cols(int ver, bool we_sep, bool ta_sep) {
+  // W, area (+ WE) (+ hn, hnn for PPM) (+ Z, zbar for QR4C);
+  // T, Flo, Fho/D, TV (+ TA)
+  return LoCols{2 + (we_sep ? 1 : 0) + (ver == 3 ? 2 : 0) + (ver == 1 ? 2 : 0), 4 + (ta_sep ? 1 : 0)};
+}
+__host__ __device__ constexpr LoCols nofct_cols(int ver) {
+  // W, area (+ hn, hnn) (+ Z, zbar); TA, F/D, TV
+  return LoCols{2 + (ver == 3 ? 2 : 0) + (ver == 1 ? 2 : 0), 3};
+}
+constexpr int kRatioVec = 3, kUpdVec = 3;
+
+struct WarpMem {
+  unsigned char* p;
+  __device__ float* f(int n) {
+    float* r = reinterpret_cast<float*>(p);
+    p += (size_t)al4(n) * 4;
+    return r;
+  }
+  template <int KV>
+  __device__ V<KV>* v(int n) {
+    V<KV>* r = reinterpret_cast<V<KV>*>(p);
+    p += (size_t)n * KV * 4;
+    return r;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// FCT stage 1: low-order solution and vertical antidiffusive flux
+// (lib/oce_adv_tra_driver.F90:91-235). Low-order edge flux of edge j at this
+// node: role 0 -(vp T_n + vm T_o)/2, role 1 +(vp T_o + vm T_n)/2, with
+// vp = v + |v|, vm = v - |v|; the T_n coefficients are summed first.
+// ---------------------------------------------------------------------------
+template <int VER, int KV>
+__global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
+  const int n = blockIdx.x * (blockDim.x / kW) + wib;
+  if (n >= m.N) return;
+  const GeoPtrs<float>& g = m.g32;
+  const unsigned LZ = m.LZ, LW = m.LW;
+  const int nl = m.nl, nz = m.nz;
+  const bool ta_sep = a.TA != a.T, we_sep = a.we != a.w;
+  const LoCols cols = lo_cols(VER, we_sep, ta_sep);
+  WarpMem wm{smem_raw + (size_t)wib * warp_bytes<KV>(cols.scal, cols.vec, LW)};
+  float* sW = wm.f(LW);
+  float* sA = wm.f(LW);
+  float* sWE = we_sep ? wm.f(LW) : sW;
+  float* sHn = VER == 3 ? wm.f(LW) : nullptr;
+  float* sHnn = VER == 3 ? wm.f(LW) : nullptr;
+  float* sZ = VER == 1 ? wm.f(LW) : nullptr;
+  float* sZb = VER == 1 ? wm.f(LW) : nullptr;
+  V<KV>* sT = wm.v<KV>(LW);
+  V<KV>* sFlo = wm.v<KV>(LW);
+  V<KV>* sD = wm.v<KV>(LW);  // PPM slopes, then the HO - LO fluxes
+  V<KV>* sTV = wm.v<KV>(LW);
+  V<KV>* sTA = ta_sep ? wm.v<KV>(LW) : sT;
+  V<KV>* sFho = sD;
+  const NbrF nb = stage_nbrs_f(m, n, reinterpret_cast<int2*>(wm.p), lane);
+  stage_f(sW, a.w + n * LW, nl, lane);
+  if (we_sep) stage_f(sWE, a.we + n * LW, nl, lane);
+  stage_f(sA, g.area + n * LW, nl, lane);
+  if (VER == 3) {
+    stage_f(sHn, g.hnode + n * LZ, nz, lane);
+    stage_f(sHnn, g.hnode_new + n * LZ, nz, lane);
+  }
+  if (VER == 1) {
+    stage_f(sZ, g.Z3 + n * LZ, nz, lane);
+    stage_f(sZb, g.zbar3 + n * LW, nl, lane);
+  }
+  const int nzmin = m.ulev[n], nzmax = m.nlev[n];
+  const float dt = a.dt;
+  const ColF clo{sWE, sA, sHn, sHnn, sZ, sZb};
+  const ColF cho{sW, sA, sHn, sHnn, sZ, sZb};
+  for (int gi = 0; gi < a.G; ++gi) {
+    const float* __restrict__ Tg = a.T + gi * a.gT;
+    stage_v<KV>(sT, Tg, n * LZ, LZ, lane);
+    if (ta_sep) stage_v<KV>(sTA, a.TA + gi * a.gTA, n * LZ, nz, lane);
+    __syncwarp();
+    // LO vertical flux: upwind with w_e on T.
+    vert_flux<0, KV>(clo, sT, nullptr, nullptr, nullptr, sFlo, nl, nzmin, nzmax, 1.f, dt, lane);
+    // HO vertical flux on T_AB with w; adf_v = HO - LO.
+    vert_flux<VER, KV>(cho, sTA, sD, sTV, sFlo, sFho, nl, nzmin, nzmax, a.pv, dt, lane);
+    float* __restrict__ adfv = a.adfv + gi * a.gW;
+    for (unsigned iz = lane; iz < LW; iz += kW) st<KV>(adfv, n * LW + iz, (int)iz < nl ? sFho[iz] : splat<KV>(0.f));
+    float* __restrict__ lo = a.lo + gi * a.gN;
+    for (unsigned base = 0; base < LZ; base += kPass) {
+      unsigned kk[kSlices];
+      bool in[kSlices];
+      float cn[kSlices];
+      V<KV> acc[kSlices];
+#pragma unroll
+      for (int i = 0; i < kSlices; ++i) {
+        const unsigned k = base + lane + kW * i;
+        in[i] = k < LZ;
+        kk[i] = in[i] ? k : LZ - 1;
+        cn[i] = 0.f;
+        acc[i] = splat<KV>(0.f);
+      }
+#pragma unroll 2
+      for (int j = 0; j < nb.deg; ++j) {
+        const int2 q = nb.get(m, j);
+        const unsigned ed = (unsigned)(q.x >> 1);
+        const bool role = q.x & 1;
+        float v[kSlices];
+        V<KV> to[kSlices];
+#pragma unroll
+        for (int i = 0; i < kSlices; ++i) {
+          v[i] = a.vf[ed * LZ + kk[i]];
+          to[i] = ld<KV>(Tg, q.y * LZ + kk[i]);
+        }
+#pragma unroll
+        for (int i = 0; i < kSlices; ++i) {
+          const float vp = v[i] + fabsf(v[i]), vmn = v[i] - fabsf(v[i]);
+          const float cnj = role ? 0.5f * vmn : -0.5f * vp;
+          const float coj = role ? 0.5f * vp : -0.5f * vmn;
+          cn[i] += cnj;
+          acc[i] = fmas(to[i], coj, acc[i]);
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < kSlices; ++i) {
+        if (!in[i]) continue;
+        const unsigned k = kk[i];
+        const int z = (int)k + 1;
+        const V<KV> tn = sT[k];
+        V<KV> l = fmas(tn, cn[i], acc[i]);
+        if (z >= nzmin && z <= nzmax - 1) {
+          const float hn = g.hnode[n * LZ + k], hnn = g.hnode_new[n * LZ + k], av = g.areasvol[n * LZ + k];
+          const float ra = hn / hnn, rb = dt / (av * hnn);
+          l = fmas(add(l, sub(sFlo[k], sFlo[k + 1])), rb, muls(tn, ra));
+        }
+        st<KV>(lo, n * LZ + k, l);
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FCT stage 2: bounds a1-a3, antidiffusive sums b1 and limiting factors b2
+// (lib/oce_adv_tra_fct.F90:98-374).
+// ---------------------------------------------------------------------------
+template <int KV>
+__global__ void __launch_bounds__(128, 8) kf_ratio(DMesh m, FastPtrs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
+  const int n = blockIdx.x * (blockDim.x / kW) + wib;
+  if (n >= m.N) return;
+  const GeoPtrs<float>& g = m.g32;
+  const unsigned LZ = m.LZ, LW = m.LW;
+  const int nl = m.nl;
+  WarpMem wm{smem_raw + (size_t)wib * warp_bytes<KV>(0, kRatioVec, LW)};
+  V<KV>*sAdv = wm.v<KV>(LW), *sMx = wm.v<KV>(LW), *sMn = wm.v<KV>(LW);
+  int2* snb = reinterpret_cast<int2*>(wm.p);
+  int2* scl = snb + kMaxDegF;
+  const NbrF nb = stage_nbrs_f(m, n, snb, lane);
+  const int c0 = m.cl_ptr[n], ncl = m.cl_ptr[n + 1] - c0, minlev = m.cl_minlev[n];
+  const bool cl_staged = ncl <= kMaxClF;
+  if (cl_staged)
+    for (int j = lane; j < ncl; j += kW) scl[j] = make_int2(m.cl_node[c0 + j], m.cl_lev[c0 + j]);
+  const int nzmin = m.ulev[n], nzmax = m.nlev[n];
+  const float dt = a.dt;
+  for (int gi = 0; gi < a.G; ++gi) {
+    const float* __restrict__ Tg = a.T + gi * a.gT;
+    const float* __restrict__ Lg = a.lo + gi * a.gN;
+    const float* __restrict__ Fg = a.adfh + gi * a.gE;
+    stage_v<KV>(sAdv, a.adfv + gi * a.gW, n * LW, nl, lane);
+    __syncwarp();
+    // cluster bounds per layer
+    for (unsigned base = 0; base < LZ; base += kPass) {
+      unsigned kk[kSlices];
+      V<KV> mx[kSlices], mn[kSlices];
+#pragma unroll
+      for (int i = 0; i < kSlices; ++i) {
+        const unsigned k = base + lane + kW * i;
+        kk[i] = k < LZ ? k : LZ - 1;
+        // AUX = -/+1e3 of elements without the layer (lib/oce_adv_tra_fct.F90:139-145)
+        const float m0 = (int)k + 1 > minlev ? -1e3f : -INFINITY;
+        mx[i] = splat<KV>(m0);
+        mn[i] = splat<KV>(-m0);
+      }
+#pragma unroll 2
+      for (int j = 0; j < ncl; ++j) {
+        const int2 c = cl_staged ? scl[j] : make_int2(m.cl_node[c0 + j], m.cl_lev[c0 + j]);
+        V<KV> lv[kSlices], tv[kSlices];
+#pragma unroll
+        for (int i = 0; i < kSlices; ++i) {
+          lv[i] = ld<KV>(Lg, c.x * LZ + kk[i]);
+          tv[i] = ld<KV>(Tg, c.x * LZ + kk[i]);
+        }
+#pragma unroll
+        for (int i = 0; i < kSlices; ++i) {
+          if ((int)(base + lane + kW * i) + 1 <= c.y) {
+#pragma unroll
+            for (int t = 0; t < KV; ++t) {
+              mx[i].v[t] = max3f(mx[i].v[t], lv[i].v[t], tv[i].v[t]);
+              mn[i].v[t] = min3f(mn[i].v[t], lv[i].v[t], tv[i].v[t]);
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < kSlices; ++i) {
+        const unsigned k = base + lane + kW * i;
+        if (k < LZ) {
+          sMx[k] = mx[i];
+          sMn[k] = mn[i];
+        }
+      }
+    }
+    __syncwarp();
+    float* __restrict__ Rg = a.rpm + 2 * gi * a.gN;
+    for (unsigned base = 0; base < LZ; base += kPass) {
+      unsigned kk[kSlices];
+      V<KV> pl[kSlices], mi[kSlices];
+#pragma unroll
+      for (int i = 0; i < kSlices; ++i) {
+        const unsigned k = base + lane + kW * i;
+        kk[i] = k < LZ ? k : LZ - 1;
+        const V<KV> ad0 = sAdv[kk[i]], ad1 = sAdv[kk[i] + 1];
+#pragma unroll
+        for (int t = 0; t < KV; ++t) {
+          pl[i].v[t] = fmaxf(0.f, ad0.v[t]) + fmaxf(0.f, -ad1.v[t]);
+          mi[i].v[t] = fminf(0.f, ad0.v[t]) + fminf(0.f, -ad1.v[t]);
+        }
+      }
+#pragma unroll 2
+      for (int j = 0; j < nb.deg; ++j) {
+        const int2 q = nb.get(m, j);
+        const unsigned ed = (unsigned)(q.x >> 1);
+        const float sg = (q.x & 1) ? -1.f : 1.f;
+        V<KV> f[kSlices];
+#pragma unroll
+        for (int i = 0; i < kSlices; ++i) f[i] = ld<KV>(Fg, ed * LZ + kk[i]);
+#pragma unroll
+        for (int i = 0; i < kSlices; ++i)
+#pragma unroll
+          for (int t = 0; t < KV; ++t) {
+            const float x = sg * f[i].v[t];
+            pl[i].v[t] += fmaxf(0.f, x);
+            mi[i].v[t] += fminf(0.f, x);
+          }
+      }
+#pragma unroll
+      for (int i = 0; i < kSlices; ++i) {
+        const unsigned k = base + lane + kW * i;
+        if (k >= LZ) continue;
+        const int z = (int)k + 1;
+        V<KV> rp = splat<KV>(0.f), rm = rp;
+        if (z >= nzmin && z <= nzmax - 1) {
+          const float r = dt / g.areasvol[n * LZ + k];
+          const V<KV> lv = ld<KV>(Lg, n * LZ + k);
+          const bool edge = z == nzmax - 1 || z == nzmin;
+#pragma unroll
+          for (int t = 0; t < KV; ++t) {
+            const float bmax = (edge ? sMx[k].v[t] : max3f(sMx[k - 1].v[t], sMx[k].v[t], sMx[k + 1].v[t])) - lv.v[t];
+            const float bmin = (edge ? sMn[k].v[t] : min3f(sMn[k - 1].v[t], sMn[k].v[t], sMn[k + 1].v[t])) - lv.v[t];
+            rp.v[t] = fminf(1.f, __fdividef(bmax, pl[i].v[t] * r + 1e-16f));
+            rm.v[t] = fminf(1.f, __fdividef(bmin, mi[i].v[t] * r - 1e-16f));
+          }
+        }
+        st<KV>(Rg, 2 * (n * LZ + k), rp);
+        st<KV>(Rg, 2 * (n * LZ + k) + 1, rm);
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FCT stage 3: limiting b3 (lib/oce_adv_tra_fct.F90:396-471), flux divergence
+// (lib/oce_adv_tra_driver.F90:298-450) and the tendency update
+// (src/fesom_analytic.F90:419-437; lib/tracer_c_interface.F90:194-214 with a
+// persistent del_ttf). The limiting factors are at most 1, so min(1, a, b)
+// is min(a, b).
+// ---------------------------------------------------------------------------
+template <int KV>
+__device__ __forceinline__ V<KV> vsel_min(const V<KV>& f, const V<KV>& a_pos, const V<KV>& b_pos, const V<KV>& a_neg,
+                                          const V<KV>& b_neg) {
+  V<KV> r;
+#pragma unroll
+  for (int t = 0; t < KV; ++t)
+    r.v[t] = f.v[t] >= 0.f ? fminf(a_pos.v[t], b_pos.v[t]) : fminf(a_neg.v[t], b_neg.v[t]);
+  return r;
+}
+
+template <int KV>
+__device__ __forceinline__ void finish_node(const DMesh& m, const FastPtrs& a, int gi, int n, unsigned k, int nzmin,
+                                            int nzmax, const V<KV>& dh, const V<KV>& dvflux, const V<KV>* lo_or_null,
+                                            bool fct) {
+  const GeoPtrs<float>& g = m.g32;
+  const unsigned LZ = m.LZ;
+  float* __restrict__ T = a.T + gi * a.gT;
+  const V<KV> Tn = ld<KV>(T, n * LZ + k);
+  float* del = a.del ? a.del + gi * a.gN : nullptr;
+  const V<KV> d0 = del ? ld<KV>(del, n * LZ + k) : splat<KV>(0.f);
+  const int z = (int)k + 1;
+  const bool act = z >= nzmin && z <= nzmax - 1;
+  V<KV> tnew = Tn, enew = d0;
+  if (act) {
+    const float av = g.areasvol[n * LZ + k], hnn = g.hnode_new[n * LZ + k];
+    const float r = a.dt / av;
+    V<KV> dv;
+    if (fct) {
+      const float hn = g.hnode[n * LZ + k];
+      dv = fmas(*lo_or_null, hnn, muls(Tn, -hn));
+      dv = fmas(dvflux, r, dv);
+    } else {
+      dv = muls(dvflux, r);
+    }
+    enew = add(add(d0, muls(dh, r)), dv);
+    tnew = fmas(enew, 1.f / hnn, Tn);
+  }
+  st<KV>(T, n * LZ + k, tnew);
+  if (del) st<KV>(del, n * LZ + k, enew);
+  if (a.TAout) st<KV>(a.TAout + gi * a.gTA, n * LZ + k, tnew);
+}
+
+template <int KV>
+__global__ void __launch_bounds__(128, 6) kf_update(DMesh m, FastPtrs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
+  const int n = blockIdx.x * (blockDim.x / kW) + wib;
+  if (n >= m.N) return;
+  const unsigned LZ = m.LZ, LW = m.LW;
+  const int nl = m.nl, nz = m.nz;
+  WarpMem wm{smem_raw + (size_t)wib * warp_bytes<KV>(0, kUpdVec, LW)};
+  V<KV>*sLv = wm.v<KV>(LW), *sRp = wm.v<KV>(LW), *sRm = wm.v<KV>(LW);
+  const NbrF nb = stage_nbrs_f(m, n, reinterpret_cast<int2*>(wm.p), lane);
+  const int nzmin = m.ulev[n], nzmax = m.nlev[n];
+  for (int gi = 0; gi < a.G; ++gi) {
+    const float* __restrict__ Rg = a.rpm + 2 * gi * a.gN;
+    const float* __restrict__ Fg = a.adfh + gi * a.gE;
+    for (int k = lane; k < nz; k += kW) {
+      sRp[k] = ld<KV>(Rg, 2 * (n * LZ + k));
+      sRm[k] = ld<KV>(Rg, 2 * (n * LZ + k) + 1);
+    }
+    __syncwarp();
+    const float* __restrict__ adfv = a.adfv + gi * a.gW;
+    for (int iz = lane; iz < nl; iz += kW) {
+      const int z = iz + 1;
+      V<KV> f = ld<KV>(adfv, n * LW + iz);
+      if (z == nzmin) {
+        f = mul(f, vsel_min(f, splat<KV>(1.f), sRp[iz], splat<KV>(1.f), sRm[iz]));
+      } else if (z > nzmin && z <= nzmax - 1) {
+        f = mul(f, vsel_min(f, sRm[iz - 1], sRp[iz], sRp[iz - 1], sRm[iz]));
+      }
+      sLv[iz] = f;
+    }
+    __syncwarp();
+    const float* __restrict__ Lg = a.lo + gi * a.gN;
+    for (unsigned base = 0; base < LZ; base += kPass) {
+      unsigned kk[kSlices];
+      V<KV> dh[kSlices], rpn[kSlices], rmn[kSlices];
+#pragma unroll
+      for (int i = 0; i < kSlices; ++i) {
+        const unsigned k = base + lane + kW * i;
+        kk[i] = k < LZ ? k : LZ - 1;
+        dh[i] = splat<KV>(0.f);
+        rpn[i] = ld<KV>(Rg, 2 * (n * LZ + kk[i]));
+        rmn[i] = ld<KV>(Rg, 2 * (n * LZ + kk[i]) + 1);
+      }
+#pragma unroll 2
+      for (int j = 0; j < nb.deg; ++j) {
+        const int2 q = nb.get(m, j);
+        const unsigned ed = (unsigned)(q.x >> 1);
+        const bool role = q.x & 1;
+        V<KV> f[kSlices], rpo[kSlices], rmo[kSlices];
+#pragma unroll
+        for (int i = 0; i < kSlices; ++i) {
+          f[i] = ld<KV>(Fg, ed * LZ + kk[i]);
+          rpo[i] = ld<KV>(Rg, 2 * (q.y * LZ + kk[i]));
+          rmo[i] = ld<KV>(Rg, 2 * (q.y * LZ + kk[i]) + 1);
+        }
+#pragma unroll
+        for (int i = 0; i < kSlices; ++i) {
+          if (role) {  // this node is the edge's second node
+            const V<KV> ae = vsel_min(f[i], rpo[i], rmn[i], rmo[i], rpn[i]);
+            dh[i] = sub(dh[i], mul(ae, f[i]));
+          } else {
+            const V<KV> ae = vsel_min(f[i], rpn[i], rmo[i], rmn[i], rpo[i]);
+            dh[i] = fma(ae, f[i], dh[i]);
+          }
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < kSlices; ++i) {
+        const unsigned k = base + lane + kW * i;
+        if (k >= LZ) continue;
+        const V<KV> lo = ld<KV>(Lg, n * LZ + k);
+        finish_node<KV>(m, a, gi, n, k, nzmin, nzmax, dh[i], sub(sLv[k], sLv[k + 1]), &lo, true);
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Without a limiter: vertical HO flux on T_AB with w_e, flux divergence and
+// the tendency update in one pass.
+// ---------------------------------------------------------------------------
+template <int VER, int KV>
+__global__ void __launch_bounds__(128, 8) kf_nofct(DMesh m, FastPtrs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
+  const int n = blockIdx.x * (blockDim.x / kW) + wib;
+  if (n >= m.N) return;
+  const GeoPtrs<float>& g = m.g32;
+  const unsigned LZ = m.LZ, LW = m.LW;
+  const int nl = m.nl, nz = m.nz;
+  const LoCols cols = nofct_cols(VER);
+  WarpMem wm{smem_raw + (size_t)wib * warp_bytes<KV>(cols.scal, cols.vec, LW)};
+  float* sW = wm.f(LW);
+  float* sA = wm.f(LW);
+  float* sHn = VER == 3 ? wm.f(LW) : nullptr;
+  float* sHnn = VER == 3 ? wm.f(LW) : nullptr;
+  float* sZ = VER == 1 ? wm.f(LW) : nullptr;
+  float* sZb = VER == 1 ? wm.f(LW) : nullptr;
+  V<KV>* sTA = wm.v<KV>(LW);
+  V<KV>* sD = wm.v<KV>(LW);  // PPM slopes, then the fluxes
+  V<KV>* sTV = wm.v<KV>(LW);
+  V<KV>* sF = sD;
+  const NbrF nb = stage_nbrs_f(m, n, reinterpret_cast<int2*>(wm.p), lane);
+  stage_f(sW, a.we + n * LW, nl, lane);
+  stage_f(sA, g.area + n * LW, nl, lane);
+  if (VER == 3) {
+    stage_f(sHn, g.hnode + n * LZ, nz, lane);
+    stage_f(sHnn, g.hnode_new + n * LZ, nz, lane);
+  }
+  if (VER == 1) {
+    stage_f(sZ, g.Z3 + n * LZ, nz, lane);
+    stage_f(sZb, g.zbar3 + n * LW, nl, lane);
+  }
+  const int nzmin = m.ulev[n], nzmax = m.nlev[n];
+  const ColF c{sW, sA, sHn, sHnn, sZ, sZb};
+  for (int gi = 0; gi < a.G; ++gi) {
+    const float* __restrict__ TAg = a.TA + gi * a.gTA;
+    const float* __restrict__ Fg = a.adfh + gi * a.gE;
+    stage_v<KV>(sTA, TAg, n * LZ, nz, lane);
+    __syncwarp();
+    vert_flux<VER, KV>(c, sTA, sD, sTV, nullptr, sF, nl, nzmin, nzmax, a.pv, a.dt, lane);
+    for (unsigned base = 0; base < LZ; base += kPass) {
+      unsigned kk[kSlices];
+      V<KV> dh[kSlices];
+#pragma unroll
+      for (int i = 0; i < kSlices; ++i) {
+        const unsigned k = base + lane + kW * i;
+        kk[i] = k < LZ ? k : LZ - 1;
+        dh[i] = splat<KV>(0.f);
+      }
+#pragma unroll 2
+      for (int j = 0; j < nb.deg; ++j) {
+        const int2 q = nb.get(m, j);
+        const unsigned ed = (unsigned)(q.x >> 1);
+        const bool role = q.x & 1;
+#pragma unroll
+        for (int i = 0; i < kSlices; ++i) {
+          const V<KV> f = ld<KV>(Fg, ed * LZ + kk[i]);
+          dh[i] = role ? sub(dh[i], f) : add(dh[i], f);
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < kSlices; ++i) {
+        const unsigned k = base + lane + kW * i;
+        if (k >= LZ) continue;
+        finish_node<KV>(m, a, gi, n, k, nzmin, nzmax, dh[i], sub(sF[k], sF[k + 1]), nullptr, false);
+      }
+    }
+    __syncwarp();
+  }
+}
+
+}  // namespace fast
+}  // namespace fgb

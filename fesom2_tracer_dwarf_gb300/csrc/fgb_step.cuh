@@ -16,23 +16,6 @@ constexpr int kEdgeWarps = 8;  // default edges per block
 constexpr int kNodeWarps = 4;  // default node columns per block (the kernels' launch bound)
 
 
-template <typename R>
-WorkspaceLayout workspace_layout(const DMesh& m, int K) {
-  WorkspaceLayout w;
-  const long long E = m.E, N = m.N, LZ = m.LZ, LW = m.LW, s = sizeof(R);
-  auto al = [](long long b) { return (b + 255) / 256 * 256; };
-  long long off = 0;
-  w.off[0] = off; off += al(E * LZ * s);          // vf
-  w.off[1] = off;                                         // (unused slot)
-  w.off[2] = off; off += al((long long)K * E * LZ * s);  // adfh
-  w.off[3] = off; off += al((long long)K * N * LZ * s);  // lo
-  w.off[4] = off; off += al((long long)K * N * LW * s);  // adfv
-  w.off[5] = off; off += al(2LL * K * N * LZ * s);       // R+, R- interleaved
-  w.off[6] = w.off[5];                                    // (same array)
-  w.total = off;
-  return w;
-}
-
 template <typename R, int HOR>
 void launch_hflux(const DMesh& m, const StepPtrs<R>& a, bool fct, int ew, cudaStream_t s) {
   dim3 grid((m.E + ew - 1) / ew), block(ew * kWarp);
@@ -110,6 +93,7 @@ int launch_stages(const DMesh& m, const fgb_step_desc& d, int mask, cudaStream_t
                   std::string* err) {
   const int K = d.ntracers;
   if (K < 1 || K > 65535) { *err = "ntracers must be in 1..65535"; return -1; }
+  if (d.tracer_vec > 1) { *err = "tracer groups (tracer_vec > 1) are a layout of the FP32 form"; return -1; }
   if (d.hor < 0 || d.hor > 2 || d.ver < 0 || d.ver > 3 || d.lim < 0 || d.lim > 1) {
     *err = "unknown advection scheme";
     return -1;

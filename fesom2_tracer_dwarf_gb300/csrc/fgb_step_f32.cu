@@ -1,10 +1,99 @@
-// FP32 form of the step (storage and arithmetic in single precision).
-#include "fgb_step.cuh"
+// FP32 form of the step: argument checks and dispatch to the kernels of the
+// tracer-group width (fgb_fast.cuh).
+#include <cstdint>
+
+#include "fgb_internal.hpp"
 
 namespace fgb {
+namespace fast {
+int launch_fast_kv1(const DMesh& m, const FastPtrs& a, const LaunchArgs& L, cudaStream_t s);
+int launch_fast_kv2(const DMesh& m, const FastPtrs& a, const LaunchArgs& L, cudaStream_t s);
+int launch_fast_kv4(const DMesh& m, const FastPtrs& a, const LaunchArgs& L, cudaStream_t s);
+}  // namespace fast
+
 WorkspaceLayout workspace_layout_f32(const DMesh& m, int K) { return workspace_layout<float>(m, K); }
+
 int launch_stages_f32(const DMesh& m, const fgb_step_desc& d, int mask, cudaStream_t s, int* nlaunch,
                       std::string* err) {
-  return launch_stages<float>(m, d, mask, s, nlaunch, err);
+  using namespace fast;
+  *nlaunch = 0;
+  const int K = d.ntracers;
+  const int KV = d.tracer_vec <= 1 ? 1 : d.tracer_vec;
+  if (K < 1 || K > 65535) { *err = "ntracers must be in 1..65535"; return -1; }
+  if (KV != 1 && KV != 2 && KV != 4) { *err = "tracer_vec must be 0, 1, 2 or 4"; return -1; }
+  if (K % KV) { *err = "tracer_vec must divide ntracers"; return -1; }
+  if (d.hor < 0 || d.hor > 2 || d.ver < 0 || d.ver > 3 || d.lim < 0 || d.lim > 1) {
+    *err = "unknown advection scheme";
+    return -1;
+  }
+  if (!d.T || !d.vel || !d.w || !d.we || !d.workspace) { *err = "null device pointer"; return -1; }
+  const WorkspaceLayout wl = workspace_layout<float>(m, K);
+  if (d.workspace_bytes < wl.total) { *err = "workspace too small"; return -1; }
+  if ((d.ver == FGB_VER_QR4C || d.ver == FGB_VER_PPM) && m.min_layers < 2) {
+    *err = "QR4C/PPM need at least two layers in every column";
+    return -1;
+  }
+  if (d.hor != FGB_HOR_UPW1 && !m.fast_tri_ok) {
+    *err = "FP32 MUSCL/MFCT: an upwind triangle does not hold its edge node";
+    return -1;
+  }
+  // Offsets inside a group are 32-bit (units of KV floats).
+  const long long lim = 1LL << 32;
+  if ((long long)m.E * m.LZ >= lim || 2LL * m.N * m.LZ >= lim || (long long)m.N * m.LW >= lim ||
+      (long long)m.M * m.LZ >= lim) {
+    *err = "mesh too large for the FP32 form (edges x padded layers must stay below 2^32)";
+    return -1;
+  }
+  const uintptr_t al = 4u * KV;
+  auto misaligned = [&](const void* p) { return p && (reinterpret_cast<uintptr_t>(p) % al) != 0; };
+  if (misaligned(d.T) || misaligned(d.TA) || misaligned(d.TAout) || misaligned(d.del) ||
+      reinterpret_cast<uintptr_t>(d.vel) % 8 != 0 || d.strideT % KV != 0 || (d.TA && d.strideTA % KV != 0)) {
+    *err = "FP32 tracer arrays must be aligned to their group (4 * tracer_vec bytes, strides multiples of tracer_vec)";
+    return -1;
+  }
+  char* ws = static_cast<char*>(d.workspace);
+  FastPtrs a;
+  a.T = static_cast<float*>(d.T);
+  a.TA = d.TA ? static_cast<const float*>(d.TA) : a.T;
+  a.TAout = static_cast<float*>(d.TAout);
+  a.vel = static_cast<const float*>(d.vel);
+  a.w = static_cast<const float*>(d.w);
+  a.we = static_cast<const float*>(d.we);
+  a.vf = reinterpret_cast<float*>(ws + wl.off[0]);
+  a.adfh = reinterpret_cast<float*>(ws + wl.off[2]);
+  a.lo = reinterpret_cast<float*>(ws + wl.off[3]);
+  a.adfv = reinterpret_cast<float*>(ws + wl.off[4]);
+  a.rpm = reinterpret_cast<float*>(ws + wl.off[5]);
+  a.del = static_cast<float*>(d.del);
+  a.gT = d.strideT;
+  a.gTA = d.TA ? d.strideTA : d.strideT;
+  a.gE = (long long)m.E * m.LZ * KV;
+  a.gN = (long long)m.N * m.LZ * KV;
+  a.gW = (long long)m.N * m.LW * KV;
+  a.G = K / KV;
+  a.dt = (float)d.dt;
+  a.ph = (float)d.ph;
+  a.pv = (float)d.pv;
+  auto pick = [](int want, int x, int y, int z, int def) { return (want == x || want == y || want == z) ? want : def; };
+  LaunchArgs L;
+  L.mask = mask;
+  L.edge_warps = pick(d.cfg[0], 2, 4, 8, 8);
+  L.nw_lo = pick(d.cfg[1], 1, 2, 4, 4);
+  L.nw_ratio = pick(d.cfg[2], 1, 2, 4, 4);
+  L.nw_upd = pick(d.cfg[3], 1, 2, 4, 4);
+  L.hor = d.hor;
+  L.ver = d.ver;
+  L.fct = d.lim == FGB_LIM_FCT;
+  int n = 0;
+  if (KV == 4) n = launch_fast_kv4(m, a, L, s);
+  else if (KV == 2) n = launch_fast_kv2(m, a, L, s);
+  else n = launch_fast_kv1(m, a, L, s);
+  *nlaunch = n;
+  cudaError_t ce = cudaGetLastError();
+  if (ce != cudaSuccess) {
+    *err = std::string("kernel launch failed: ") + cudaGetErrorString(ce);
+    return -1;
+  }
+  return 0;
 }
 }  // namespace fgb

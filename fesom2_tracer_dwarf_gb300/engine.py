@@ -4,7 +4,10 @@ kernels launched through the C-ABI on torch's current CUDA stream.
 ``TracerAdvection`` advances K tracers of one mesh with do_oce_adv_tra
 (lib/oce_adv_tra_driver.F90:23-294) followed by the analytic driver's
 tendency update (src/fesom_analytic.F90:404-437). Tracer values live in a
-(K, N, LZ) tensor (level index fastest, padded to LZ layers).
+(K, N, LZ) tensor (level index fastest, padded to LZ layers) in the FP64
+form; the FP32 form groups V = 4 (or 2) tracers per node-layer, a
+(K/V, N, LZ, V) tensor, so one vector load brings a group. ``to_layout`` and
+``from_layout`` convert between (K, N, LZ) and the engine's layout.
 
 valuesAB (the field the high-order fluxes read) is either frozen at the
 values given to ``set_tracers`` -- the analytic dwarf, src/fesom_analytic.F90:335
@@ -32,20 +35,26 @@ def _require_cuda():
 class TracerAdvection:
     def __init__(self, mesh: Mesh, ntracers: int, precision: str = "fp64", hor: str = "UPW1",
                  ver: str = "UPW1", lim: str = "NONE", ph: float = 1.0, pv: float = 1.0,
-                 copy_ab: bool = False, device: str = "cuda"):
+                 copy_ab: bool = False, device: str = "cuda", tracer_vec: int | None = None):
         _require_cuda()
         if precision not in _DT:
             raise ValueError(f"precision must be one of {list(_DT)}")
         self.mesh, self.K, self.precision = mesh, int(ntracers), precision
         self.dtype = _DT[precision]
+        if tracer_vec is None:
+            tracer_vec = 1 if precision == "fp64" else next(v for v in (4, 2, 1) if self.K % v == 0)
+        if tracer_vec not in (1, 2, 4) or self.K % tracer_vec or (precision == "fp64" and tracer_vec != 1):
+            raise ValueError("tracer_vec must be 1 (FP64) or 1, 2, 4 dividing ntracers (FP32)")
+        self.V = int(tracer_vec)
+        self.G = self.K // self.V
         self.device = torch.device(device)
         self.set_schemes(hor, ver, lim, ph, pv)
         self.copy_ab = copy_ab
         m = mesh
         m.upload()
         z = lambda *s: torch.zeros(*s, dtype=self.dtype, device=self.device)
-        self.T = z(self.K, m.N, m.LZ)
-        self.TA = None if copy_ab else z(self.K, m.N, m.LZ)
+        self.T = z(*self.layout_shape)
+        self.TA = None if copy_ab else z(*self.layout_shape)
         self.vel = z(m.M, m.LZ, 2)
         self.w = z(m.N, m.LW)
         self.we = self.w
@@ -73,6 +82,26 @@ class TracerAdvection:
             raise ValueError("a launch configuration has 8 entries")
         self.cfg = cfg
 
+    # ---- layout ------------------------------------------------------------
+    @property
+    def layout_shape(self):
+        m = self.mesh
+        return (self.K, m.N, m.LZ) if self.V == 1 else (self.G, m.N, m.LZ, self.V)
+
+    def to_layout(self, x):
+        """(K, N, LZ) tensor -> the engine's tracer layout (a view when V = 1)."""
+        if self.V == 1:
+            return x
+        m = self.mesh
+        return x.reshape(self.G, self.V, m.N, m.LZ).permute(0, 2, 3, 1).contiguous()
+
+    def from_layout(self, x):
+        """The engine's tracer layout -> (K, N, LZ)."""
+        if self.V == 1:
+            return x
+        m = self.mesh
+        return x.permute(0, 3, 1, 2).reshape(self.K, m.N, m.LZ)
+
     # ---- configuration -----------------------------------------------------
     def set_schemes(self, hor="UPW1", ver="UPW1", lim="NONE", ph=1.0, pv=1.0):
         for name, table, v in (("hor", _lib.HOR, hor), ("ver", _lib.VER, ver), ("lim", _lib.LIM, lim)):
@@ -89,10 +118,11 @@ class TracerAdvection:
     def set_tracers(self, values, values_ab=None):
         """values: (K, N, nz) array. values_ab defaults to values."""
         m = self.mesh
-        v = self._pad_nodes(values, m.nz, m.LZ).reshape(self.K, m.N, m.LZ)
+        v = self.to_layout(self._pad_nodes(values, m.nz, m.LZ).reshape(self.K, m.N, m.LZ))
         self.T.copy_(v)
         if self.TA is not None:
-            self.TA.copy_(v if values_ab is None else self._pad_nodes(values_ab, m.nz, m.LZ).reshape(self.K, m.N, m.LZ))
+            vab = v if values_ab is None else self._pad_nodes(values_ab, m.nz, m.LZ).reshape(self.K, m.N, m.LZ)
+            self.TA.copy_(self.to_layout(vab) if values_ab is not None else v)
 
     def set_velocity(self, vel, w, we=None):
         """vel: (M, nz, 2) on elements; w, we: (N, nl) at node interfaces."""
@@ -110,9 +140,9 @@ class TracerAdvection:
         """Copy device tensors that already have the padded layouts
         (K,N,LZ), (M,LZ,2), (N,LW)."""
         if T is not None:
-            self.T.copy_(T)
+            self.T.copy_(self.to_layout(T))
         if TA is not None and self.TA is not None:
-            self.TA.copy_(TA)
+            self.TA.copy_(self.to_layout(TA))
         if vel is not None:
             self.vel.copy_(vel)
         if w is not None:
@@ -130,9 +160,10 @@ class TracerAdvection:
         d.ph, d.pv, d.dt = self.ph, self.pv, float(dt)
         m = self.mesh
         d.T = self.T.data_ptr()
-        d.strideT = m.N * m.LZ
+        d.strideT = m.N * m.LZ * self.V
         d.TA = None if self.TA is None else self.TA.data_ptr()
-        d.strideTA = m.N * m.LZ
+        d.strideTA = m.N * m.LZ * self.V
+        d.tracer_vec = self.V
         d.TAout = None
         d.vel, d.w, d.we = self.vel.data_ptr(), self.w.data_ptr(), self.we.data_ptr()
         d.del_ = None
@@ -152,22 +183,30 @@ class TracerAdvection:
 
     # ---- outputs -----------------------------------------------------------
     def values(self) -> np.ndarray:
+        """(K, N, nz) tracer values as float64."""
         m = self.mesh
-        return self.T[:, :, : m.nz].double().cpu().numpy()
+        return self.from_layout(self.T)[:, :, : m.nz].double().cpu().numpy()
 
     def workspace_view(self, name: str):
-        """A view of one workspace array: vf (E,LZ), adfh (K,E,LZ), lo (K,N,LZ),
-        adfv (K,N,LW), rp / rm (K,N,LZ; stored interleaved)."""
+        """One workspace array per tracer: vf (E,LZ), adfh (K,E,LZ), lo (K,N,LZ),
+        adfv (K,N,LW), rp / rm (K,N,LZ). Views of the workspace in the FP64
+        form; copies when the FP32 form groups tracers."""
         m = self.mesh
         L = _lib.load()
         offs = (ctypes.c_longlong * 7)()
         _lib.check(L.fgb_workspace_offsets(m.handle, _PREC[self.precision], self.K, offs), "offsets")
         slot = {"vf": 0, "adfh": 2, "lo": 3, "adfv": 4, "rp": 5, "rm": 5}[name]
-        shape = {"vf": (m.E, m.LZ), "adfh": (self.K, m.E, m.LZ), "lo": (self.K, m.N, m.LZ),
-                 "adfv": (self.K, m.N, m.LW), "rp": (self.K, m.N, m.LZ, 2), "rm": (self.K, m.N, m.LZ, 2)}[name]
+        G, V = self.G, self.V
+        rows = {"vf": None, "adfh": (m.E, m.LZ), "lo": (m.N, m.LZ), "adfv": (m.N, m.LW), "rp": (m.N, m.LZ, 2),
+                "rm": (m.N, m.LZ, 2)}[name]
+        shape = (m.E, m.LZ) if rows is None else (G, *rows, V)
         n = int(np.prod(shape))
         es = self.T.element_size()
         v = self.workspace[offs[slot]: offs[slot] + n * es].view(self.dtype).view(shape)
+        if rows is None:
+            return v
+        # (G, rows..., V) -> (K, rows...)
+        v = v.movedim(-1, 1).reshape(self.K, *rows)
         if name == "rp":
             return v[..., 0]
         if name == "rm":
@@ -179,7 +218,13 @@ class TracerAdvection:
         L = _lib.load()
         m = self.mesh
         stream = ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
-        _lib.check(L.fgb_tracer_stats(m.handle, _PREC[self.precision], ctypes.c_void_p(self.T.data_ptr()),
-                                      m.N * m.LZ, self.K, ctypes.c_void_p(self._stats_scratch.data_ptr()),
-                                      ctypes.c_void_p(self._stats_out.data_ptr()), stream), "fgb_tracer_stats")
+        if self.V == 1:
+            _lib.check(L.fgb_tracer_stats(m.handle, _PREC[self.precision], ctypes.c_void_p(self.T.data_ptr()),
+                                          m.N * m.LZ, self.K, ctypes.c_void_p(self._stats_scratch.data_ptr()),
+                                          ctypes.c_void_p(self._stats_out.data_ptr()), stream), "fgb_tracer_stats")
+        else:
+            _lib.check(L.fgb_tracer_stats_grouped(m.handle, ctypes.c_void_p(self.T.data_ptr()), m.N * m.LZ * self.V,
+                                                  self.K, self.V, ctypes.c_void_p(self._stats_scratch.data_ptr()),
+                                                  ctypes.c_void_p(self._stats_out.data_ptr()), stream),
+                       "fgb_tracer_stats_grouped")
         return self._stats_out.cpu().numpy()

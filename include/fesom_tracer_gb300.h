@@ -164,7 +164,13 @@ int fgb_workspace_offsets(const fgb_mesh* m, int precision, int ntracers, long l
  *   TAout  optional, receives the new values (copy-AB time level)
  *   vel    (M,LZ,2) velocity on elements; w, we (N,LW) vertical velocities
  *   del    optional (K,N,LZ) persistent tendency (reference C-ABI semantics)
- *   workspace of fgb_workspace_bytes. */
+ *   workspace of fgb_workspace_bytes.
+ * Tracer grouping (FP32 form only): with tracer_vec = V in {2, 4} (V divides
+ * ntracers) the per-tracer arrays T, TA, TAout and del hold groups of V
+ * tracers interleaved per node-layer: tracer t, node n, layer k is element
+ * (t / V) * stride + (n * LZ + k) * V + t % V, each group 16-byte aligned;
+ * strideT / strideTA then count the elements between groups. tracer_vec 0
+ * or 1 is the (K,N,LZ) layout above, the only one of the FP64 form. */
 typedef struct {
   int precision;
   int ntracers;
@@ -181,12 +187,14 @@ typedef struct {
   void* del;
   void* workspace;
   long long workspace_bytes;
+  int tracer_vec; /* tracers per group of the FP32 layout: 0 or 1, 2, 4 */
   /* Launch configuration; 0 picks the default. Results do not depend on it.
    * cfg[0]     warps (edges) per block of the edge-flux kernel: 2, 4, 8 (default 8)
    * cfg[1..3]  warps (node columns) per block of the LO, ratio and update
    *            kernels: 1, 2, 4 (default 4)
-   * cfg[4..6]  tracers per chunk of the same three kernels: 1, 2, 4, used when
-   *            it divides ntracers (default: the largest of 4, 2, 1 that does)
+   * cfg[4..6]  FP64 form: tracers per chunk of the same three kernels: 1, 2,
+   *            4, used when it divides ntracers (default: the largest of 4, 2,
+   *            1 that does). The FP32 form works one tracer group at a time.
    * cfg[7]     reserved, 0 */
   int cfg[8];
 } fgb_step_desc;
@@ -202,6 +210,10 @@ int fgb_adv_stages(const fgb_mesh* m, const fgb_step_desc* d, int stage_mask, vo
 long long fgb_stats_scratch_bytes(const fgb_mesh* m, int ntracers);
 int fgb_tracer_stats(const fgb_mesh* m, int precision, const void* T, long long strideT, int ntracers,
                      void* scratch, double* out_dev, void* stream);
+/* The same for FP32 values in the grouped layout of fgb_step_desc.tracer_vec
+ * (strideT: elements between groups). */
+int fgb_tracer_stats_grouped(const fgb_mesh* m, const float* T, long long strideT, int ntracers, int tracer_vec,
+                             void* scratch, double* out_dev, void* stream);
 
 /* Number of kernels the last fgb_adv_step / fgb_adv_stages call launched. */
 int fgb_last_launch_count(void);

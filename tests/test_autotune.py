@@ -18,6 +18,7 @@ def test_candidates_cover_allowed_values():
     assert autotune.chunk_candidates(5) == [1]
     up = autotune.stage_candidates("update", 2)
     assert all(set(c) == {3, 6} for c in up)
+    assert autotune.stage_candidates("ratio", 4, "fp32") == [{2: 1}, {2: 2}, {2: 4}]
 
 
 def test_cache_file_round_trip(tmp_path):
@@ -83,7 +84,7 @@ def test_autotune_returns_valid_config_and_restores_fields(tmp_path):
     cfg = res["cfg"]
     assert cfg[0] in autotune.EDGE_WARPS
     assert all(c in autotune.NODE_WARPS for c in cfg[1:4])
-    assert all(c in autotune.CHUNKS for c in cfg[4:7])
+    assert cfg[4:7] == [0, 0, 0]  # the FP32 form has no chunk knobs
     assert set(res["ms"]) == {"hflux", "lo", "ratio", "update"}
     assert np.array_equal(e.values(), before)
     again = autotune.tune(e, dt=200.0, cache_path=str(tmp_path / "t.json"))

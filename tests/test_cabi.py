@@ -104,3 +104,38 @@ def test_cabi_steps_match_oracle(tracer, oracle_mod, schemes):
         st = tracer.get_statistics()
         assert st["min"] == vals.min() and st["max"] == vals.max()
         assert abs(st["sum"] - vals.sum()) <= 1e-12 * abs(vals.sum())
+
+
+@pytest.mark.gpu
+def test_cabi_fp32_form_close(tracer, oracle_mod):
+    """tracer_set_precision(1): the FP32 form through the reference interface,
+    del_ttf kept in single precision, within 1e-5 of the FP64 oracle."""
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA GPU")
+    from fesom2_tracer_dwarf_gb300 import synthetic
+    from fesom2_tracer_dwarf_gb300.mesh import Mesh
+
+    O = oracle_mod
+    nx, ny, nl = 14, 12, 9
+    assert tracer.generate_analytic_mesh(nx, ny, nl, periodic=True) == 0
+    om = O.Mesh(nx, ny, nl, periodic=True)
+    hm = Mesh(nx, ny, nl, periodic=True, upload=False)
+    rng = np.random.default_rng(22)
+    vel, w = synthetic.random_flow(hm, rng)
+    T = synthetic.random_field(hm, rng, 1)[0]
+    nz, N, E = nl - 1, hm.N, hm.E
+    assert tracer.allocate_tracers(1, nl, N) == 0
+    assert tracer.set_values(1, np.asfortranarray(T.T)) == 0
+    assert tracer.set_velocity(_reference_layout_uv(vel, nz, E), np.asfortranarray(w.T)) == 0
+    assert tracer.set_schemes(1, "MUSCL", "PPM", "FCT") == 0
+    assert tracer.set_precision("fp32") == 0
+    assert tracer.init_ale_arrays() == 0 and tracer.init_for_advection() == 0 and tracer.init_complete() == 0
+    vals = np.ascontiguousarray(T.copy())
+    vab = vals.copy()
+    del_ttf = np.zeros_like(vals)
+    W = O.Work(om)
+    for _ in range(3):
+        assert tracer.advect_step(600.0) == 0
+        O.cabi_step(om, W, 600.0, vel, w, vals, vab, del_ttf, "MUSCL", "PPM", "FCT")
+    got = tracer.get_tracer_values()
+    assert float(np.abs(got.T - vals).max()) <= 1e-5 * float(np.abs(vals).max())
