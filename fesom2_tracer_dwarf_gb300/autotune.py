@@ -3,7 +3,8 @@
 The step is five kernels (vertical fluxes, edge fluxes, FCT low-order
 solution, FCT ratios, update); four of them have launch knobs that do not
 change results (fgb_step_desc.cfg): edges per block of the edge-flux kernel,
-node columns per block and tracers per chunk of the three node kernels. The
+node columns per block of the three node kernels, and tracers per chunk
+(FP64) or layers per lane per pass (FP32). The
 best choice depends on the mesh size, the number of layers, the tracer count
 and the precision, so this module times the candidates of each kernel on the
 caller's own engine (its mesh, fields and schemes) and keeps the fastest.
@@ -28,6 +29,7 @@ from . import _lib
 EDGE_WARPS = (2, 4, 8)
 NODE_WARPS = (1, 2, 4)
 CHUNKS = (1, 2, 4)
+SLICES = (1, 2)
 
 _MEMO: dict = {}
 
@@ -39,12 +41,15 @@ def chunk_candidates(K: int):
 
 def stage_candidates(stage: str, K: int, precision: str = "fp64"):
     """Candidate knob values per tuned stage: a list of dicts of cfg index -> value.
-    The FP32 form works one tracer group at a time, so only its block sizes vary."""
+    FP64: block size and tracers per chunk. FP32 (one tracer group at a time):
+    block size and layers per lane per pass."""
     if stage == "hflux":
+        if precision == "fp32":
+            return [{0: w, 7: ns} for w, ns in product(EDGE_WARPS, SLICES)]
         return [{0: w} for w in EDGE_WARPS]
     slot = {"lo": 0, "ratio": 1, "update": 2}[stage]
     if precision == "fp32":
-        return [{1 + slot: w} for w in NODE_WARPS]
+        return [{1 + slot: w, 4 + slot: ns} for w, ns in product(NODE_WARPS, SLICES)]
     return [{1 + slot: w, 4 + slot: c} for w, c in product(NODE_WARPS, chunk_candidates(K))]
 
 
@@ -53,7 +58,7 @@ def cache_key(engine) -> str:
 
     m = engine.mesh
     dev = torch.cuda.get_device_name(engine.device)
-    return "|".join(str(x) for x in (dev, engine.precision, engine.K, engine.hor, engine.ver, engine.lim,
+    return "|".join(str(x) for x in (dev, engine.precision, engine.K, engine.V, engine.hor, engine.ver, engine.lim,
                                      m.N, m.E, m.nz))
 
 

@@ -102,6 +102,7 @@ struct FastPtrs {
 // Launch shape of one FP32 call.
 struct LaunchArgs {
   int mask, edge_warps, nw_lo, nw_ratio, nw_upd, hor, ver, fct;
+  int ns_h, ns_lo, ns_ratio, ns_upd;  // layers per lane per pass (1 or 2)
 };
 }  // namespace fast
 

@@ -34,8 +34,8 @@ namespace fgb {
 namespace fast {
 
 constexpr int kW = 32;
-constexpr int kSlices = 2;              // layers per lane per pass
-constexpr int kPass = kW * kSlices;     // layers per pass
+// Each kernel handles NS (1 or 2) layers per lane per pass: a warp covers
+// 32 * NS layers of a column or edge per pass.
 constexpr int kMaxDegF = 16;            // incident edges staged per node
 constexpr int kMaxClF = 24;             // cluster nodes staged per node
 
@@ -153,28 +153,46 @@ __device__ __forceinline__ float min3f(float a, float b, float c) {
 // 215-216). With ulevels = 1 the segments reduce to: element 1 contributes at
 // layers 1..nl1, element 2 at layers 1..nl2.
 // ---------------------------------------------------------------------------
+//
+// Each warp handles 32 consecutive edges of the visit order: lane j loads the
+// tables of edge j once, then the warp sweeps the edges' layers.
 static __global__ void __launch_bounds__(256) kf_vflux(DMesh m, const float* __restrict__ vel, float* __restrict__ vf) {
   const int lane = threadIdx.x & (kW - 1);
-  const int e = blockIdx.x * (blockDim.x / kW) + (threadIdx.x / kW);
-  if (e >= m.E) return;
+  const int w0 = (blockIdx.x * (blockDim.x / kW) + (threadIdx.x / kW)) * kW;
+  if (w0 >= m.E) return;
+  const int cnt = min(kW, m.E - w0);
   const GeoPtrs<float>& g = m.g32;
-  const int nl1 = m.edge_lev[4 * e + 1], nl2 = m.edge_lev[4 * e + 3];
-  const int el1 = m.edge_tri[2 * e], el2 = m.edge_tri[2 * e + 1];
-  const float4 cr = reinterpret_cast<const float4*>(g.edge_cross)[e];
+  int e = 0, el1 = 0, el2 = 0, nl1 = 0, nl2 = 0;
+  float4 cr = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (lane < cnt) {
+    e = m.edge_order ? m.edge_order[w0 + lane] : w0 + lane;  // the edges of a node together: element reuse in L2
+    el1 = m.edge_tri[2 * e];
+    el2 = m.edge_tri[2 * e + 1];
+    nl1 = m.edge_lev[4 * e + 1];
+    nl2 = m.edge_lev[4 * e + 3];
+    cr = reinterpret_cast<const float4*>(g.edge_cross)[e];
+  }
   const unsigned LZ = m.LZ;
   const float2* __restrict__ uv = reinterpret_cast<const float2*>(vel);
-  for (unsigned k = lane; k < LZ; k += kW) {
-    const int z = (int)k + 1;
-    float v = 0.f;
-    if (z <= nl1) {
-      const float2 u = uv[el1 * LZ + k];
-      v = (-(u.y * cr.x) + u.x * cr.y) * g.helem[el1 * LZ + k];
+  for (int i = 0; i < cnt; ++i) {
+    const int ei = __shfl_sync(0xffffffffu, e, i);
+    const int e1 = __shfl_sync(0xffffffffu, el1, i), e2 = __shfl_sync(0xffffffffu, el2, i);
+    const int l1 = __shfl_sync(0xffffffffu, nl1, i), l2 = __shfl_sync(0xffffffffu, nl2, i);
+    const float dX1 = __shfl_sync(0xffffffffu, cr.x, i), dY1 = __shfl_sync(0xffffffffu, cr.y, i);
+    const float dX2 = __shfl_sync(0xffffffffu, cr.z, i), dY2 = __shfl_sync(0xffffffffu, cr.w, i);
+    for (unsigned k = lane; k < LZ; k += kW) {
+      const int z = (int)k + 1;
+      float v = 0.f;
+      if (z <= l1) {
+        const float2 u = uv[e1 * LZ + k];
+        v = (-(u.y * dX1) + u.x * dY1) * g.helem[e1 * LZ + k];
+      }
+      if (z <= l2) {
+        const float2 u = uv[e2 * LZ + k];
+        v = v + (u.y * dX2 - u.x * dY2) * g.helem[e2 * LZ + k];
+      }
+      vf[ei * LZ + k] = v;
     }
-    if (z <= nl2) {
-      const float2 u = uv[el2 * LZ + k];
-      v = v + (u.y * cr.z - u.x * cr.w) * g.helem[el2 * LZ + k];
-    }
-    vf[e * LZ + k] = v;
   }
 }
 
@@ -217,42 +235,73 @@ __device__ __forceinline__ void node_grad(const DMesh& m, const float* __restric
   gy = muls(ty, inv);
 }
 
-template <int HOR, bool FCT, int KV>
-__global__ void __launch_bounds__(256, 2) kf_hflux(DMesh m, FastPtrs a) {
-  const int lane = threadIdx.x & (kW - 1);
-  const int w = blockIdx.x * (blockDim.x / kW) + (threadIdx.x / kW);
-  if (w >= m.E) return;
+// Tables of one edge, filled by one lane and read by the whole warp.
+struct alignas(16) EdgeRec {
+  int e, n1, n2, hi;
+  int gm0, gm1, nb1, nb2;
+  float ex, ey, pad0, pad1;
+  int4 tri;
+  float4 wu, wd;
+};
+
+template <int HOR>
+__device__ __forceinline__ void fill_edge(const DMesh& m, int w, EdgeRec& r) {
   const int e = m.edge_order ? m.edge_order[w] : w;
-  const unsigned LZ = m.LZ;
-  const int nz = m.nz;
-  const int n1 = m.edge_nodes[2 * e], n2 = m.edge_nodes[2 * e + 1];
-  const int hi = max(m.edge_lev[4 * e + 1], m.edge_lev[4 * e + 3]);
-  int4 tri = make_int4(0, 0, 0, 0);
-  float4 wu = make_float4(0.f, 0.f, 0.f, 0.f), wd = wu;
-  int gm0 = -1, gm1 = -1, nb1 = 0, nb2 = 0;
-  float ex = 0.f, ey = 0.f;
+  r.e = e;
+  r.n1 = m.edge_nodes[2 * e];
+  r.n2 = m.edge_nodes[2 * e + 1];
+  r.hi = max(m.edge_lev[4 * e + 1], m.edge_lev[4 * e + 3]);
+  r.gm0 = -1;
+  r.gm1 = -1;
+  r.nb1 = r.nb2 = 0;
+  r.ex = r.ey = r.pad0 = r.pad1 = 0.f;
+  r.tri = make_int4(0, 0, 0, 0);
+  r.wu = r.wd = make_float4(0.f, 0.f, 0.f, 0.f);
   if (HOR != 0) {
-    gm0 = m.edge_gm[2 * e];
-    gm1 = m.edge_gm[2 * e + 1];
-    nb1 = m.nbl[n1];
-    nb2 = m.nbl[n2];
-    ex = m.g32.edge_dxa[2 * e];
-    ey = m.g32.edge_dxa[2 * e + 1];
-    if (gm0 >= 0) {
-      tri = reinterpret_cast<const int4*>(m.f_tri)[e];
-      wu = reinterpret_cast<const float4*>(m.f_wu)[e];
-      wd = reinterpret_cast<const float4*>(m.f_wd)[e];
+    r.gm0 = m.edge_gm[2 * e];
+    r.gm1 = m.edge_gm[2 * e + 1];
+    r.nb1 = m.nbl[r.n1];
+    r.nb2 = m.nbl[r.n2];
+    r.ex = m.g32.edge_dxa[2 * e];
+    r.ey = m.g32.edge_dxa[2 * e + 1];
+    if (r.gm0 >= 0) {
+      r.tri = reinterpret_cast<const int4*>(m.f_tri)[e];
+      r.wu = reinterpret_cast<const float4*>(m.f_wu)[e];
+      r.wd = reinterpret_cast<const float4*>(m.f_wd)[e];
     }
   }
+}
+
+// Each warp handles 32 consecutive edges of the visit order: lane j fills the
+// table record of edge j, then the warp computes the edges one after another.
+template <int HOR, bool FCT, int KV, int NS>
+__global__ void __launch_bounds__(256, (NS == 1 ? 3 : 2)) kf_hflux(DMesh m, FastPtrs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  EdgeRec* recs = reinterpret_cast<EdgeRec*>(smem_raw) + (threadIdx.x / kW) * kW;  // this warp's 32 records
+  const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
+  const int w0 = (blockIdx.x * (blockDim.x / kW) + wib) * kW;
+  if (w0 >= m.E) return;
+  const int cnt = min(kW, m.E - w0);
+  if (lane < cnt) fill_edge<HOR>(m, w0 + lane, recs[lane]);
+  __syncwarp();
+  const unsigned LZ = m.LZ;
+  const int nz = m.nz;
+  for (int ie = 0; ie < cnt; ++ie) {
+  const EdgeRec& rec = recs[ie];
+  const int e = rec.e, n1 = rec.n1, n2 = rec.n2, hi = rec.hi;
+  const int gm0 = rec.gm0, gm1 = rec.gm1, nb1 = rec.nb1, nb2 = rec.nb2;
+  const float ex = rec.ex, ey = rec.ey;
+  const int4 tri = rec.tri;
+  const float4 wu = rec.wu, wd = rec.wd;
   const float A = 0.5f * (1.f - a.ph);
   const bool ta_sep = a.TA != a.T;
-  for (unsigned base = 0; base < LZ; base += kPass) {
-    unsigned kk[kSlices];
-    bool in[kSlices], act[kSlices], tri_ok[kSlices];
-    float vp[kSlices], vm[kSlices], B[kSlices], c1[kSlices], c2[kSlices];
+  for (unsigned base = 0; base < LZ; base += kW * NS) {
+    unsigned kk[NS];
+    bool in[NS], act[NS], tri_ok[NS];
+    float vp[NS], vm[NS], B[NS], c1[NS], c2[NS];
     bool all_tri = true;
 #pragma unroll
-    for (int i = 0; i < kSlices; ++i) {
+    for (int i = 0; i < NS; ++i) {
       const unsigned k = base + lane + kW * i;
       in[i] = k < LZ;
       kk[i] = in[i] ? k : LZ - 1;
@@ -272,9 +321,9 @@ __global__ void __launch_bounds__(256, 2) kf_hflux(DMesh m, FastPtrs a) {
       const float* __restrict__ Tg = a.T + gi * a.gT;
       const float* __restrict__ TAg = ta_sep ? a.TA + gi * a.gTA : Tg;
       float* __restrict__ out = a.adfh + gi * a.gE;
-      V<KV> s1[kSlices], s2[kSlices], r1[kSlices], r2[kSlices];
+      V<KV> s1[NS], s2[NS], r1[NS], r2[NS];
 #pragma unroll
-      for (int i = 0; i < kSlices; ++i) {
+      for (int i = 0; i < NS; ++i) {
         s1[i] = ld<KV>(TAg, n1 * LZ + kk[i]);
         s2[i] = ld<KV>(TAg, n2 * LZ + kk[i]);
         if (FCT && ta_sep) {
@@ -285,23 +334,23 @@ __global__ void __launch_bounds__(256, 2) kf_hflux(DMesh m, FastPtrs a) {
           r2[i] = s2[i];
         }
       }
-      V<KV> h[kSlices];
+      V<KV> h[NS];
       if (HOR == 0) {
 #pragma unroll
-        for (int i = 0; i < kSlices; ++i) h[i] = muls(fmas(s2[i], vm[i], muls(s1[i], vp[i])), -0.5f);
+        for (int i = 0; i < NS; ++i) h[i] = muls(fmas(s2[i], vm[i], muls(s1[i], vp[i])), -0.5f);
       } else {
-        V<KV> tm1[kSlices], tm2[kSlices];
+        V<KV> tm1[NS], tm2[NS];
         if (fast_tri) {
-          V<KV> u1[kSlices], u2[kSlices], d1[kSlices], d2[kSlices];
+          V<KV> u1[NS], u2[NS], d1[NS], d2[NS];
 #pragma unroll
-          for (int i = 0; i < kSlices; ++i) {
+          for (int i = 0; i < NS; ++i) {
             u1[i] = ld<KV>(TAg, tri.x * LZ + kk[i]);
             u2[i] = ld<KV>(TAg, tri.y * LZ + kk[i]);
             d1[i] = ld<KV>(TAg, tri.z * LZ + kk[i]);
             d2[i] = ld<KV>(TAg, tri.w * LZ + kk[i]);
           }
 #pragma unroll
-          for (int i = 0; i < kSlices; ++i) {
+          for (int i = 0; i < NS; ++i) {
             const V<KV> dT3 = muls(sub(s2[i], s1[i]), 1.f / 3.f);
             const V<KV> p1 = fmas(u2[i], wu.z, fmas(u1[i], wu.y, fmas(s1[i], wu.x, dT3)));
             const V<KV> p2 = fmas(d2[i], wd.z, fmas(d1[i], wd.y, fmas(s2[i], wd.x, dT3)));
@@ -310,7 +359,7 @@ __global__ void __launch_bounds__(256, 2) kf_hflux(DMesh m, FastPtrs a) {
           }
         } else {
 #pragma unroll
-          for (int i = 0; i < kSlices; ++i) {
+          for (int i = 0; i < NS; ++i) {
             const V<KV> dT3 = muls(sub(s2[i], s1[i]), 1.f / 3.f);
             V<KV> p1, p2;
             if (tri_ok[i]) {
@@ -333,19 +382,20 @@ __global__ void __launch_bounds__(256, 2) kf_hflux(DMesh m, FastPtrs a) {
           }
         }
 #pragma unroll
-        for (int i = 0; i < kSlices; ++i) {
+        for (int i = 0; i < NS; ++i) {
           const V<KV> cho = fmas(tm2[i], vm[i], muls(tm1[i], vp[i]));
           h[i] = fmas(add(tm1[i], tm2[i]), -B[i], muls(cho, -A));
         }
       }
 #pragma unroll
-      for (int i = 0; i < kSlices; ++i) {
+      for (int i = 0; i < NS; ++i) {
         V<KV> r = h[i];
         if (FCT) r = fmas(fmas(r2[i], vm[i], muls(r1[i], vp[i])), 0.5f, r);
         if (!act[i]) r = splat<KV>(0.f);
         if (in[i]) st<KV>(out, e * LZ + kk[i], r);
       }
     }
+  }
   }
 }
 
@@ -441,20 +491,29 @@ __device__ __forceinline__ V<KV> ppm_flux(const V<KV>& aL0, const V<KV>& aR0, co
 // Vertical flux of the column at every interface into out[iz], minus fold[iz]
 // (fold = nullptr: zero). VER: 0 UPW1, 1 QR4C, 2 CDIFF, 3 PPM. T holds the
 // column's layers; D and TV are scratch columns for PPM.
+// The bottom interface z = nl is never inside a column's stencil: its value
+// is set by one lane, so a 64-layer column needs two passes of 32 lanes.
 template <int VER, int KV>
 __device__ void vert_flux(const ColF& c, const V<KV>* T, V<KV>* D, V<KV>* TV, const V<KV>* fold, V<KV>* out, int nl,
                           int nzmin, int nzmax, float num_ord, float dt, int lane) {
+  const int last = nl - 1;
   if (VER == 3) {
-    for (int j = lane; j < nl; j += kW)
+    for (int j = lane; j < nl - 2; j += kW)
       if (j >= nzmin && j <= nzmax - 3) D[j] = ppm_slope<KV>(T, c.hnn, j);
     __syncwarp();
-    for (int iz = lane; iz < nl; iz += kW) {
+    for (int iz = lane; iz < last; iz += kW) {
       const int z = iz + 1;
       if (z >= nzmin && z <= nzmax) TV[iz] = ppm_edge<KV>(T, D, c, z, nzmin, nzmax);
     }
+    if (lane == 0 && nzmax == nl) TV[last] = T[nzmax - 2];
     __syncwarp();
   }
-  for (int iz = lane; iz < nl; iz += kW) {
+  if (lane == 0) {
+    // z = nl: the column's last interface (zero flux, CDIFF leaves it) or below the column
+    const V<KV> f0 = fold ? fold[last] : splat<KV>(0.f);
+    out[last] = (nzmax == nl && VER != 2) ? sub(splat<KV>(0.f), f0) : f0;
+  }
+  for (int iz = lane; iz < last; iz += kW) {
     const int z = iz + 1;
     const V<KV> f0 = fold ? fold[iz] : splat<KV>(0.f);
     V<KV> r = f0;
@@ -575,7 +634,7 @@ struct WarpMem {
 // node: role 0 -(vp T_n + vm T_o)/2, role 1 +(vp T_o + vm T_n)/2, with
 // vp = v + |v|, vm = v - |v|; the T_n coefficients are summed first.
 // ---------------------------------------------------------------------------
-template <int VER, int KV>
+template <int VER, int KV, int NS>
 __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
@@ -626,15 +685,16 @@ __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
     // HO vertical flux on T_AB with w; adf_v = HO - LO.
     vert_flux<VER, KV>(cho, sTA, sD, sTV, sFlo, sFho, nl, nzmin, nzmax, a.pv, dt, lane);
     float* __restrict__ adfv = a.adfv + gi * a.gW;
-    for (unsigned iz = lane; iz < LW; iz += kW) st<KV>(adfv, n * LW + iz, (int)iz < nl ? sFho[iz] : splat<KV>(0.f));
+    for (int iz = lane; iz < nl - 1; iz += kW) st<KV>(adfv, n * LW + iz, sFho[iz]);
+    if (lane == 0) st<KV>(adfv, n * LW + nl - 1, sFho[nl - 1]);
     float* __restrict__ lo = a.lo + gi * a.gN;
-    for (unsigned base = 0; base < LZ; base += kPass) {
-      unsigned kk[kSlices];
-      bool in[kSlices];
-      float cn[kSlices];
-      V<KV> acc[kSlices];
+    for (unsigned base = 0; base < LZ; base += kW * NS) {
+      unsigned kk[NS];
+      bool in[NS];
+      float cn[NS];
+      V<KV> acc[NS];
 #pragma unroll
-      for (int i = 0; i < kSlices; ++i) {
+      for (int i = 0; i < NS; ++i) {
         const unsigned k = base + lane + kW * i;
         in[i] = k < LZ;
         kk[i] = in[i] ? k : LZ - 1;
@@ -646,15 +706,15 @@ __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
         const int2 q = nb.get(m, j);
         const unsigned ed = (unsigned)(q.x >> 1);
         const bool role = q.x & 1;
-        float v[kSlices];
-        V<KV> to[kSlices];
+        float v[NS];
+        V<KV> to[NS];
 #pragma unroll
-        for (int i = 0; i < kSlices; ++i) {
+        for (int i = 0; i < NS; ++i) {
           v[i] = a.vf[ed * LZ + kk[i]];
           to[i] = ld<KV>(Tg, q.y * LZ + kk[i]);
         }
 #pragma unroll
-        for (int i = 0; i < kSlices; ++i) {
+        for (int i = 0; i < NS; ++i) {
           const float vp = v[i] + fabsf(v[i]), vmn = v[i] - fabsf(v[i]);
           const float cnj = role ? 0.5f * vmn : -0.5f * vp;
           const float coj = role ? 0.5f * vp : -0.5f * vmn;
@@ -663,7 +723,7 @@ __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
         }
       }
 #pragma unroll
-      for (int i = 0; i < kSlices; ++i) {
+      for (int i = 0; i < NS; ++i) {
         if (!in[i]) continue;
         const unsigned k = kk[i];
         const int z = (int)k + 1;
@@ -685,7 +745,7 @@ __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
 // FCT stage 2: bounds a1-a3, antidiffusive sums b1 and limiting factors b2
 // (lib/oce_adv_tra_fct.F90:98-374).
 // ---------------------------------------------------------------------------
-template <int KV>
+template <int KV, int NS>
 __global__ void __launch_bounds__(128, 8) kf_ratio(DMesh m, FastPtrs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
@@ -712,11 +772,11 @@ __global__ void __launch_bounds__(128, 8) kf_ratio(DMesh m, FastPtrs a) {
     stage_v<KV>(sAdv, a.adfv + gi * a.gW, n * LW, nl, lane);
     __syncwarp();
     // cluster bounds per layer
-    for (unsigned base = 0; base < LZ; base += kPass) {
-      unsigned kk[kSlices];
-      V<KV> mx[kSlices], mn[kSlices];
+    for (unsigned base = 0; base < LZ; base += kW * NS) {
+      unsigned kk[NS];
+      V<KV> mx[NS], mn[NS];
 #pragma unroll
-      for (int i = 0; i < kSlices; ++i) {
+      for (int i = 0; i < NS; ++i) {
         const unsigned k = base + lane + kW * i;
         kk[i] = k < LZ ? k : LZ - 1;
         // AUX = -/+1e3 of elements without the layer (lib/oce_adv_tra_fct.F90:139-145)
@@ -727,14 +787,14 @@ __global__ void __launch_bounds__(128, 8) kf_ratio(DMesh m, FastPtrs a) {
 #pragma unroll 2
       for (int j = 0; j < ncl; ++j) {
         const int2 c = cl_staged ? scl[j] : make_int2(m.cl_node[c0 + j], m.cl_lev[c0 + j]);
-        V<KV> lv[kSlices], tv[kSlices];
+        V<KV> lv[NS], tv[NS];
 #pragma unroll
-        for (int i = 0; i < kSlices; ++i) {
+        for (int i = 0; i < NS; ++i) {
           lv[i] = ld<KV>(Lg, c.x * LZ + kk[i]);
           tv[i] = ld<KV>(Tg, c.x * LZ + kk[i]);
         }
 #pragma unroll
-        for (int i = 0; i < kSlices; ++i) {
+        for (int i = 0; i < NS; ++i) {
           if ((int)(base + lane + kW * i) + 1 <= c.y) {
 #pragma unroll
             for (int t = 0; t < KV; ++t) {
@@ -745,7 +805,7 @@ __global__ void __launch_bounds__(128, 8) kf_ratio(DMesh m, FastPtrs a) {
         }
       }
 #pragma unroll
-      for (int i = 0; i < kSlices; ++i) {
+      for (int i = 0; i < NS; ++i) {
         const unsigned k = base + lane + kW * i;
         if (k < LZ) {
           sMx[k] = mx[i];
@@ -755,11 +815,11 @@ __global__ void __launch_bounds__(128, 8) kf_ratio(DMesh m, FastPtrs a) {
     }
     __syncwarp();
     float* __restrict__ Rg = a.rpm + 2 * gi * a.gN;
-    for (unsigned base = 0; base < LZ; base += kPass) {
-      unsigned kk[kSlices];
-      V<KV> pl[kSlices], mi[kSlices];
+    for (unsigned base = 0; base < LZ; base += kW * NS) {
+      unsigned kk[NS];
+      V<KV> pl[NS], mi[NS];
 #pragma unroll
-      for (int i = 0; i < kSlices; ++i) {
+      for (int i = 0; i < NS; ++i) {
         const unsigned k = base + lane + kW * i;
         kk[i] = k < LZ ? k : LZ - 1;
         const V<KV> ad0 = sAdv[kk[i]], ad1 = sAdv[kk[i] + 1];
@@ -774,11 +834,11 @@ __global__ void __launch_bounds__(128, 8) kf_ratio(DMesh m, FastPtrs a) {
         const int2 q = nb.get(m, j);
         const unsigned ed = (unsigned)(q.x >> 1);
         const float sg = (q.x & 1) ? -1.f : 1.f;
-        V<KV> f[kSlices];
+        V<KV> f[NS];
 #pragma unroll
-        for (int i = 0; i < kSlices; ++i) f[i] = ld<KV>(Fg, ed * LZ + kk[i]);
+        for (int i = 0; i < NS; ++i) f[i] = ld<KV>(Fg, ed * LZ + kk[i]);
 #pragma unroll
-        for (int i = 0; i < kSlices; ++i)
+        for (int i = 0; i < NS; ++i)
 #pragma unroll
           for (int t = 0; t < KV; ++t) {
             const float x = sg * f[i].v[t];
@@ -787,7 +847,7 @@ __global__ void __launch_bounds__(128, 8) kf_ratio(DMesh m, FastPtrs a) {
           }
       }
 #pragma unroll
-      for (int i = 0; i < kSlices; ++i) {
+      for (int i = 0; i < NS; ++i) {
         const unsigned k = base + lane + kW * i;
         if (k >= LZ) continue;
         const int z = (int)k + 1;
@@ -861,8 +921,8 @@ __device__ __forceinline__ void finish_node(const DMesh& m, const FastPtrs& a, i
   if (a.TAout) st<KV>(a.TAout + gi * a.gTA, n * LZ + k, tnew);
 }
 
-template <int KV>
-__global__ void __launch_bounds__(128, 6) kf_update(DMesh m, FastPtrs a) {
+template <int KV, int NS>
+__global__ void __launch_bounds__(128, (NS == 1 ? 8 : 6)) kf_update(DMesh m, FastPtrs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
   const int n = blockIdx.x * (blockDim.x / kW) + wib;
@@ -894,11 +954,11 @@ __global__ void __launch_bounds__(128, 6) kf_update(DMesh m, FastPtrs a) {
     }
     __syncwarp();
     const float* __restrict__ Lg = a.lo + gi * a.gN;
-    for (unsigned base = 0; base < LZ; base += kPass) {
-      unsigned kk[kSlices];
-      V<KV> dh[kSlices], rpn[kSlices], rmn[kSlices];
+    for (unsigned base = 0; base < LZ; base += kW * NS) {
+      unsigned kk[NS];
+      V<KV> dh[NS], rpn[NS], rmn[NS];
 #pragma unroll
-      for (int i = 0; i < kSlices; ++i) {
+      for (int i = 0; i < NS; ++i) {
         const unsigned k = base + lane + kW * i;
         kk[i] = k < LZ ? k : LZ - 1;
         dh[i] = splat<KV>(0.f);
@@ -910,15 +970,15 @@ __global__ void __launch_bounds__(128, 6) kf_update(DMesh m, FastPtrs a) {
         const int2 q = nb.get(m, j);
         const unsigned ed = (unsigned)(q.x >> 1);
         const bool role = q.x & 1;
-        V<KV> f[kSlices], rpo[kSlices], rmo[kSlices];
+        V<KV> f[NS], rpo[NS], rmo[NS];
 #pragma unroll
-        for (int i = 0; i < kSlices; ++i) {
+        for (int i = 0; i < NS; ++i) {
           f[i] = ld<KV>(Fg, ed * LZ + kk[i]);
           rpo[i] = ld<KV>(Rg, 2 * (q.y * LZ + kk[i]));
           rmo[i] = ld<KV>(Rg, 2 * (q.y * LZ + kk[i]) + 1);
         }
 #pragma unroll
-        for (int i = 0; i < kSlices; ++i) {
+        for (int i = 0; i < NS; ++i) {
           if (role) {  // this node is the edge's second node
             const V<KV> ae = vsel_min(f[i], rpo[i], rmn[i], rmo[i], rpn[i]);
             dh[i] = sub(dh[i], mul(ae, f[i]));
@@ -929,7 +989,7 @@ __global__ void __launch_bounds__(128, 6) kf_update(DMesh m, FastPtrs a) {
         }
       }
 #pragma unroll
-      for (int i = 0; i < kSlices; ++i) {
+      for (int i = 0; i < NS; ++i) {
         const unsigned k = base + lane + kW * i;
         if (k >= LZ) continue;
         const V<KV> lo = ld<KV>(Lg, n * LZ + k);
@@ -944,7 +1004,7 @@ __global__ void __launch_bounds__(128, 6) kf_update(DMesh m, FastPtrs a) {
 // Without a limiter: vertical HO flux on T_AB with w_e, flux divergence and
 // the tendency update in one pass.
 // ---------------------------------------------------------------------------
-template <int VER, int KV>
+template <int VER, int KV, int NS>
 __global__ void __launch_bounds__(128, 8) kf_nofct(DMesh m, FastPtrs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
@@ -984,11 +1044,11 @@ __global__ void __launch_bounds__(128, 8) kf_nofct(DMesh m, FastPtrs a) {
     stage_v<KV>(sTA, TAg, n * LZ, nz, lane);
     __syncwarp();
     vert_flux<VER, KV>(c, sTA, sD, sTV, nullptr, sF, nl, nzmin, nzmax, a.pv, a.dt, lane);
-    for (unsigned base = 0; base < LZ; base += kPass) {
-      unsigned kk[kSlices];
-      V<KV> dh[kSlices];
+    for (unsigned base = 0; base < LZ; base += kW * NS) {
+      unsigned kk[NS];
+      V<KV> dh[NS];
 #pragma unroll
-      for (int i = 0; i < kSlices; ++i) {
+      for (int i = 0; i < NS; ++i) {
         const unsigned k = base + lane + kW * i;
         kk[i] = k < LZ ? k : LZ - 1;
         dh[i] = splat<KV>(0.f);
@@ -999,13 +1059,13 @@ __global__ void __launch_bounds__(128, 8) kf_nofct(DMesh m, FastPtrs a) {
         const unsigned ed = (unsigned)(q.x >> 1);
         const bool role = q.x & 1;
 #pragma unroll
-        for (int i = 0; i < kSlices; ++i) {
+        for (int i = 0; i < NS; ++i) {
           const V<KV> f = ld<KV>(Fg, ed * LZ + kk[i]);
           dh[i] = role ? sub(dh[i], f) : add(dh[i], f);
         }
       }
 #pragma unroll
-      for (int i = 0; i < kSlices; ++i) {
+      for (int i = 0; i < NS; ++i) {
         const unsigned k = base + lane + kW * i;
         if (k >= LZ) continue;
         finish_node<KV>(m, a, gi, n, k, nzmin, nzmax, dh[i], sub(sF[k], sF[k + 1]), nullptr, false);

@@ -81,6 +81,11 @@ int launch_stages_f32(const DMesh& m, const fgb_step_desc& d, int mask, cudaStre
   L.nw_lo = pick(d.cfg[1], 1, 2, 4, 4);
   L.nw_ratio = pick(d.cfg[2], 1, 2, 4, 4);
   L.nw_upd = pick(d.cfg[3], 1, 2, 4, 4);
+  auto ns = [](int want, int def) { return (want == 1 || want == 2) ? want : def; };
+  L.ns_h = ns(d.cfg[7], 2);
+  L.ns_lo = ns(d.cfg[4], 2);
+  L.ns_ratio = ns(d.cfg[5], 2);
+  L.ns_upd = ns(d.cfg[6], 2);
   L.hor = d.hor;
   L.ver = d.ver;
   L.fct = d.lim == FGB_LIM_FCT;

@@ -18,7 +18,9 @@ def test_candidates_cover_allowed_values():
     assert autotune.chunk_candidates(5) == [1]
     up = autotune.stage_candidates("update", 2)
     assert all(set(c) == {3, 6} for c in up)
-    assert autotune.stage_candidates("ratio", 4, "fp32") == [{2: 1}, {2: 2}, {2: 4}]
+    r32 = autotune.stage_candidates("ratio", 4, "fp32")
+    assert len(r32) == 6 and {2: 4, 5: 1} in r32
+    assert {0: 2, 7: 1} in autotune.stage_candidates("hflux", 4, "fp32")
 
 
 def test_cache_file_round_trip(tmp_path):
@@ -52,9 +54,9 @@ def _case(K, hor, ver, lim, precision="fp64"):
 
 CFGS = [
     [0] * 8,
-    [2, 1, 1, 1, 1, 1, 1, 0],
-    [4, 2, 4, 1, 2, 4, 1, 0],
-    [8, 4, 2, 2, 4, 1, 2, 0],
+    [2, 1, 1, 1, 1, 1, 1, 1],
+    [4, 2, 4, 1, 2, 4, 1, 2],
+    [8, 4, 2, 2, 4, 1, 2, 1],
     [2, 1, 2, 4, 4, 2, 4, 0],
 ]
 
@@ -84,7 +86,7 @@ def test_autotune_returns_valid_config_and_restores_fields(tmp_path):
     cfg = res["cfg"]
     assert cfg[0] in autotune.EDGE_WARPS
     assert all(c in autotune.NODE_WARPS for c in cfg[1:4])
-    assert cfg[4:7] == [0, 0, 0]  # the FP32 form has no chunk knobs
+    assert all(c in autotune.SLICES for c in cfg[4:8])  # FP32: layers per lane per pass
     assert set(res["ms"]) == {"hflux", "lo", "ratio", "update"}
     assert np.array_equal(e.values(), before)
     again = autotune.tune(e, dt=200.0, cache_path=str(tmp_path / "t.json"))
@@ -96,3 +98,20 @@ def test_autotune_returns_valid_config_and_restores_fields(tmp_path):
     # instantiation, so the tuned and default steps agree to FP32 rounding.
     a, b = e.values(), ref.values()
     assert np.abs(a - b).max() <= 1e-5 * max(1.0, np.abs(b).max())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("schemes", [("MUSCL", "PPM", "FCT"), ("UPW1", "QR4C", "NONE")])
+def test_fp32_launch_configurations_agree(schemes):
+    """FP32 form: block sizes and layers per lane change only the split of the
+    work (and at most the compiler's contraction of a few multiply-adds)."""
+    _gpu()
+    out = []
+    for cfg in CFGS:
+        e, T = _case(4, *schemes, precision="fp32")
+        e.set_launch(cfg)
+        e.step(200.0, 3)
+        out.append(e.values())
+    scale = np.abs(out[0]).max()
+    for cfg, v in zip(CFGS[1:], out[1:]):
+        assert np.abs(v - out[0]).max() <= 1e-6 * scale, f"cfg {cfg}"
