@@ -112,25 +112,31 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-# Algorithmic bytes per launch of each stage (per node-layer
-# of N*nz, s bytes per value, K tracers; E/N = 3, M/N = 2 on these meshes).
+# Algorithmic bytes per launch of each stage: per tracer-cell update, the
+# tracer arrays an FCT step must move (A_t passes of s bytes: stage 1 reads T
+# and writes adf_h (E/N = 3 per node), LO and adf_v; stage 2 reads LO, T,
+# adf_h, adf_v and writes R+, R-; stage 3 reads adf_h, R+-, adf_v, LO and T
+# and writes T: 23 passes, +1 per stage-1 read of a separate T_AB) plus the
+# shared fields read once per step (A_s / K: uv 4, helem 2, w, area, hnode,
+# hnode_new, areasvol 1 each, +2 for QR4C's Z and zbar). Without a limiter a
+# fused gather pass needs A_t = 2 (+1 for T_AB) and A_s = 10. Split over this
+# library's kernels as written below; intermediates the kernels add (the
+# edge volume fluxes, repeated geometry reads) are not algorithmic.
 # ---------------------------------------------------------------------------
 def stage_bytes(m, K, s, ver, fct=True, copy_ab=True):
-    cells = m.N * m.nz
+    cells = m.N * m.nz  # node-layers; x K tracer-cells
     ta = 0 if copy_ab else 1
-    e = m.E / m.N
-    el = m.M / m.N
-    colgeo = 5 + (2 if ver == "QR4C" else 0)  # w, area, hnode, hnode_new, areasvol (+ Z_3d_n, zbar_3d_n)
-    b = {
-        "vflux": cells * s * (2 * el + el + e),                    # vel (2 comps), helem -> vf
-        "hflux": cells * s * (e + K * (1 + ta + e)),                # vf, T[,TA] -> adfh
-    }
+    e = 3
+    qr = 2 if ver == "QR4C" else 0
+    b = {"vflux": cells * s * 6}                                   # uv (2 comps x 2 elements), helem
     if fct:
-        b["lo"] = cells * s * (colgeo + e + K * (1 + ta + 2))        # geometry, vf, T[,TA] -> LO, adfv
-        b["ratio"] = cells * s * (1 + K * (2 + 1 + e + 2))          # areasvol; LO, T, adfv, adfh -> R+, R-
-        b["update"] = cells * s * (3 + K * (2 + 1 + e + 1 + 2))     # geometry; R+-, adfv, adfh, LO, T -> T
+        b["hflux"] = cells * s * K * (1 + ta + e)                  # T (+T_AB) -> adf_h
+        b["lo"] = cells * s * (5 + qr + K * 2)                      # w, area, hnode, hnode_new, areasvol -> LO, adf_v
+        b["ratio"] = cells * s * K * (1 + 1 + e + 1 + 2)           # LO, T, adf_h, adf_v -> R+, R-
+        b["update"] = cells * s * K * (e + 2 + 1 + 1 + 2)          # adf_h, R+-, adf_v, LO, T -> T
     else:
-        b["update"] = cells * s * (colgeo + K * (ta + 1 + e + 2))   # geometry; T_AB, adfh, T -> T
+        b["hflux"] = cells * s * K * (1 + ta)                      # T (+T_AB)
+        b["update"] = cells * s * (4 + qr + K * 1)                 # w_e, area, hnode_new, areasvol -> T
     return b
 
 
