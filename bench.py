@@ -32,15 +32,24 @@ METRIC = "tracer-cell updates/s (MUSCL+FCT): FP32/batched vs plain FP64; % HBM r
 UNIT = "tracer-cell updates/s"
 
 WORKLOADS = {
-    # BASELINE configuration 4: the precision form at scale.
-    "precision_2048": dict(nx=2049, ny=2049, L=2048e3, nz=64, K=4, hor="MUSCL", ver="PPM", lim="FCT", dt=400.0,
-                           precision="fp32", compare_fp64=True),
+    # The precision form at scale: 2048^2 x 64 doubly periodic, 4 tracers (default).
+    "precision_2048": dict(kind="flat", nx=2049, L=2048e3, nz=64, K=4, hor="MUSCL", ver="PPM", lim="FCT",
+                           dt=400.0, precision="fp32", compare_fp64=True, report_steps=3),
     # Same configuration on a 512x512 grid (profiling case: a few hundred MB).
-    "precision_512": dict(nx=513, ny=513, L=512e3, nz=64, K=4, hor="MUSCL", ver="PPM", lim="FCT", dt=400.0,
+    "precision_512": dict(kind="flat", nx=513, L=512e3, nz=64, K=4, hor="MUSCL", ver="PPM", lim="FCT", dt=400.0,
                           precision="fp32", compare_fp64=False),
-    # BASELINE configuration 2: the plain FP64 drop-in, MUSCL-FCT + QR4C.
-    "fp64_512": dict(nx=513, ny=513, L=512e3, nz=48, K=2, hor="MUSCL", ver="QR4C", lim="FCT", dt=400.0,
+    # The plain FP64 drop-in: 512^2 x 48 periodic, 2 tracers, MUSCL-FCT + QR4C.
+    "fp64_512": dict(kind="flat", nx=513, L=512e3, nz=48, K=2, hor="MUSCL", ver="QR4C", lim="FCT", dt=400.0,
                      precision="fp64", compare_fp64=False),
+    # Closed ragged basin: 1024^2 with seeded bathymetry (8..64 layers), walls,
+    # MUSCL-FCT + PPM; FP32 form against plain FP64 over 100 steps.
+    "closed_1024": dict(kind="closed", nx=1025, L=1024e3, nz=64, min_layers=8, K=2, hor="MUSCL", ver="PPM",
+                        lim="FCT", dt=400.0, precision="fp32", compare_fp64=True, report_steps=100),
+    # Batching form: 16 periodic meshes of seeded uneven size (64..1024 nodes a
+    # side, 16..64 layers), 8 tracers, one launch per stage over all of them,
+    # 50 steps per CUDA graph; against per-mesh sequential plain FP64 steps.
+    "batch_16": dict(kind="batch", parts=16, K=8, hor="MUSCL", ver="QR4C", lim="FCT", dt=300.0, precision="fp32",
+                     compare_fp64="sequential", graph_steps=50),
 }
 
 
@@ -166,7 +175,46 @@ def load_traffic(workload):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
+def _pad_dim(x, dim, width):
+    import torch
+
+    if x.shape[dim] == width:
+        return x
+    shape = list(x.shape)
+    shape[dim] = width - x.shape[dim]
+    return torch.cat([x, torch.zeros(shape, dtype=x.dtype, device=x.device)], dim=dim)
+
+
+def batch_parts(cfg, seed=20260301):
+    """Seeded part list of the batching form: (nodes per side, layers, CFL)."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    sizes = rng.choice([64, 128, 256, 512, 1024], size=cfg["parts"])
+    layers = rng.integers(16, 65, size=cfg["parts"])
+    cfls = rng.uniform(0.2, 0.5, size=cfg["parts"])
+    return [(int(n), int(z), float(c)) for n, z, c in zip(sizes, layers, cfls)]
+
+
+def _flat_part(n, nz, precision, device, dt, cfl, K, seed, upload=True):
+    import numpy as np
+    import torch
+
+    from fesom2_tracer_dwarf_gb300 import synthetic
+    from fesom2_tracer_dwarf_gb300.mesh import Mesh
+
+    zb = synthetic.stretched_zbar(nz, 5.0, 250.0)
+    m = Mesh(n + 1, n + 1, nz + 1, Lx=n * 1e3, Ly=n * 1e3, depth=-zb[-1], periodic=True, orient_left=True, zbar=zb,
+             upload=upload)
+    dtype = torch.float32 if precision == "fp32" else torch.float64
+    rng = np.random.default_rng(seed)
+    vel, w = synthetic.flat_streamfunction_device(m, rng, dt, dtype, device, cfl=cfl)
+    T = synthetic.tracers_device(m, K, seed, dtype, device)
+    return m, vel, w, T
+
+
 def build_case(cfg, precision, device, seed=20260301):
+    """Mesh, engine and initial tracer values (engine layout) of a workload."""
     import numpy as np
     import torch
 
@@ -174,17 +222,77 @@ def build_case(cfg, precision, device, seed=20260301):
     from fesom2_tracer_dwarf_gb300.engine import TracerAdvection
     from fesom2_tracer_dwarf_gb300.mesh import Mesh
 
-    zb = synthetic.stretched_zbar(cfg["nz"], 5.0, 250.0)
-    m = Mesh(cfg["nx"], cfg["ny"], cfg["nz"] + 1, Lx=cfg["L"], Ly=cfg["L"], depth=-zb[-1], periodic=True,
-             orient_left=True, zbar=zb)
-    dtype = torch.float32 if precision == "fp32" else torch.float64
-    rng = np.random.default_rng(seed)
-    vel, w = synthetic.flat_streamfunction_device(m, rng, cfg["dt"], dtype, device, cfl=0.4)
-    T0 = synthetic.tracers_device(m, cfg["K"], seed, dtype, device)
-    eng = TracerAdvection(m, cfg["K"], precision, cfg["hor"], cfg["ver"], cfg["lim"], copy_ab=True, device=device)
-    eng.load_padded(T=T0, vel=vel, w=w)
-    del T0
-    return m, eng, eng.T.clone()  # initial values in the engine's tracer layout
+    sch = (cfg["hor"], cfg["ver"], cfg["lim"])
+    if cfg["kind"] == "flat":
+        m, vel, w, T0 = _flat_part(cfg["nx"] - 1, cfg["nz"], precision, device, cfg["dt"], 0.4, cfg["K"], seed)
+        eng = TracerAdvection(m, cfg["K"], precision, *sch, copy_ab=True, device=device)
+        eng.load_padded(T=T0, vel=vel, w=w)
+    elif cfg["kind"] == "closed":
+        rng = np.random.default_rng(seed)
+        zb = synthetic.stretched_zbar(cfg["nz"], 5.0, 250.0)
+        en = synthetic.bathymetry_levels(cfg["nx"], cfg["nx"], zb, rng, min_layers=cfg["min_layers"])
+        m = Mesh(cfg["nx"], cfg["nx"], cfg["nz"] + 1, Lx=cfg["L"], Ly=cfg["L"], depth=-zb[-1], periodic=False,
+                 orient_left=True, zbar=zb, elem_nlev=en)
+        vel, w = synthetic.streamfunction_flow(m, rng, cfg["dt"], cfl=0.4, psi_wall_zero=True)
+        T = np.stack([synthetic.gaussian_T(m, rng), synthetic.salinity(m, rng)] +
+                     [synthetic.passive_blob(m, rng) for _ in range(cfg["K"] - 2)])
+        eng = TracerAdvection(m, cfg["K"], precision, *sch, copy_ab=True, device=device)
+        eng.set_velocity(vel, w)
+        eng.set_tracers(T)
+        del vel, w, T
+    else:
+        parts, vels, ws, Ts = [], [], [], []
+        for i, (n, nz, cfl) in enumerate(batch_parts(cfg, seed)):
+            p, v, w, T = _flat_part(n, nz, precision, device, cfg["dt"], cfl, cfg["K"], seed + i, upload=False)
+            parts.append(p)
+            vels.append(v)
+            ws.append(w)
+            Ts.append(T)
+        m = Mesh.union(parts)
+        vel = torch.cat([_pad_dim(v, 1, m.LZ) for v in vels], dim=0)
+        w = torch.cat([_pad_dim(x, 1, m.LW) for x in ws], dim=0)
+        T0 = torch.cat([_pad_dim(t, 2, m.LZ) for t in Ts], dim=1)
+        del vels, ws, Ts
+        eng = TracerAdvection(m, cfg["K"], precision, *sch, copy_ab=True, device=device)
+        eng.load_padded(T=T0, vel=vel, w=w)
+    return m, eng, eng.T.clone()
+
+
+def precision_report(m, e32, T32, e64, T64, dt, steps):
+    """FP32 form against plain FP64 from the same initial values after
+    `steps` steps: per tracer the max-norm error relative to max |T|, the
+    relative change of the volume integral sum(T hnode_new areasvol) of each
+    form, and the FCT extremum violations (wet cells outside the initial
+    [min, max], and the largest excursion relative to the initial range)."""
+    import torch
+
+    e32.T.copy_(T32)
+    e64.T.copy_(T64)
+    e32.step(dt, steps)
+    e64.step(dt, steps)
+    torch.cuda.synchronize()
+    dev = e64.T.device
+    nz = m.nz
+    nlev = torch.as_tensor(m.get("nlevels_nod2D"), device=dev)
+    wet = (torch.arange(nz, device=dev)[None, :] < (nlev - 1)[:, None])
+    vol = torch.as_tensor(m.get("areasvol")[:, :nz] * m.get("hnode_new"), device=dev) * wet
+    init = e64.from_layout(T64)[:, :, :nz]
+    a = e32.from_layout(e32.T)[:, :, :nz].double()
+    b = e64.from_layout(e64.T)[:, :, :nz]
+    out = {"steps": steps, "max_rel_err": [], "sum_rel_err_fp32": [], "sum_rel_err_fp64": [],
+           "violations_fp32": [], "violations_fp64": [], "max_excursion_fp32": [], "max_excursion_fp64": []}
+    for t in range(init.shape[0]):
+        s0 = float((init[t] * vol).sum())
+        lo = float(init[t][wet].min())
+        hi = float(init[t][wet].max())
+        rng = max(hi - lo, 1e-300)
+        out["max_rel_err"].append(float((a[t] - b[t])[wet].abs().max()) / float(b[t][wet].abs().max()))
+        for name, x in (("fp32", a[t]), ("fp64", b[t])):
+            out[f"sum_rel_err_{name}"].append(abs(float((x * vol).sum()) - s0) / abs(s0))
+            xv = x[wet]
+            out[f"violations_{name}"].append(int(((xv < lo) | (xv > hi)).sum()))
+            out[f"max_excursion_{name}"].append(max(0.0, lo - float(xv.min()), float(xv.max()) - hi) / rng)
+    return out
 
 
 def time_engine(eng, T0, dt, steps, warmup, dist_barrier, per_stage=True):
@@ -275,6 +383,29 @@ def cpu_sample(seconds=12.0, nx=129, nz=64, K=4, hor="MUSCL", ver="PPM", lim="FC
     return cells * n / el, f"{nx - 1}x{nx - 1} periodic, {nz} layers, {K} tracers, {hor}/{ver}/{lim}, {n} step(s), {el:.1f} s"
 
 
+def time_graph(eng, T0, dt, graph_steps, replays, warmup, dist_barrier):
+    """The batching form's timing: `graph_steps` steps captured as one CUDA
+    graph, replayed `replays` times between CUDA events."""
+    import torch
+
+    l0 = eng.launches
+    g = eng.capture(dt, graph_steps)  # one eager step, then graph_steps captured steps
+    launches_per_replay = (eng.launches - l0) * graph_steps // (graph_steps + 1)
+    for _ in range(max(1, warmup // graph_steps)):
+        g.replay()
+    eng.T.copy_(T0)
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dist_barrier()
+    start.record()
+    for _ in range(replays):
+        g.replay()
+    end.record()
+    torch.cuda.synchronize()
+    dist_barrier()
+    return start.elapsed_time(end), launches_per_replay
+
+
 def run_gpu(args):
     import torch
 
@@ -291,56 +422,72 @@ def run_gpu(args):
         if dist is not None:
             dist.barrier()
 
-    from fesom2_tracer_dwarf_gb300 import _lib
+    from fesom2_tracer_dwarf_gb300 import _lib, autotune
 
     _lib.load()
     cfg = WORKLOADS[args.workload]
     m, eng, T0 = build_case(cfg, cfg["precision"], device)
-    cells = m.N * m.nz * cfg["K"]
+    K = cfg["K"]
+    cells = m.wet_cells() * K
     tuned = None
     if not args.no_tune:
-        from fesom2_tracer_dwarf_gb300 import autotune
-
         tuned = autotune.tune(eng, cfg["dt"], reps=3)
+    graph = cfg["kind"] == "batch"
     with ClockSampler(local) as clk:
-        total_ms, per, launches = time_engine(eng, T0, cfg["dt"], args.steps, args.warmup, barrier)
+        if graph:
+            replays = max(1, args.steps // cfg["graph_steps"])
+            total_ms, per_replay = time_graph(eng, T0, cfg["dt"], cfg["graph_steps"], replays, args.warmup, barrier)
+            nsteps = replays * cfg["graph_steps"]
+            launches = per_replay * replays
+            per = None
+        else:
+            nsteps = args.steps
+            total_ms, per, launches = time_engine(eng, T0, cfg["dt"], args.steps, args.warmup, barrier)
     clocks = clk.summary()
-    ms = total_ms / args.steps
+    ms = total_ms / nsteps
     t_max = ms
     if dist is not None:
         tt = torch.tensor([ms], device=device)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t_max = float(tt.item())
     value = cells * world / (t_max / 1e3)
-    # roofline of the dominant stage
     s = 4 if cfg["precision"] == "fp32" else 8
-    sb = stage_bytes(m, cfg["K"], s, cfg["ver"], fct=cfg["lim"] == "FCT")
-    dom = max(per, key=per.get)
+    wet_frac = m.wet_cells() / (m.N * m.nz)
+    sb = {k: v * wet_frac for k, v in stage_bytes(m, K, s, cfg["ver"], fct=cfg["lim"] == "FCT").items()}
     peak, peak_kind = load_peaks()
+    step_bytes = sum(sb.values())
+    if per is None:  # graph: per-stage times of one eager step for the roofline split
+        _, per, _ = time_engine(eng, T0, cfg["dt"], 2, 1, barrier)
+    dom = max(per, key=per.get)
     achieved = sb[dom] / (per[dom] / 1e3) / 1e9
     traffic = load_traffic(args.workload).get(dom)
-    step_bytes = sum(sb.values())
-    # e2e through the public API with host buffers
-    e2e_steps = max(2, min(args.steps, 10))
+    e2e_steps = max(2, min(nsteps, 10))
     e2e_ms, h2d, d2h = time_e2e(eng, T0, cfg["dt"], e2e_steps, barrier)
     e2e_value = cells * world / (e2e_ms / e2e_steps / 1e3)
+    if cfg["kind"] == "flat":
+        mesh_desc = f"{cfg['nx'] - 1}x{cfg['nx'] - 1} doubly periodic analytic grid, dx=1 km, {cfg['nz']} layers 5->250 m"
+    elif cfg["kind"] == "closed":
+        mesh_desc = (f"{cfg['nx'] - 1}x{cfg['nx'] - 1} closed basin, seeded bathymetry, "
+                     f"{cfg['min_layers']}..{cfg['nz']} layers 5->250 m")
+    else:
+        mesh_desc = "union of %d periodic meshes (n, layers, CFL): %s" % (
+            cfg["parts"], ", ".join(f"{n}^2/{z}/{c:.2f}" for n, z, c in batch_parts(cfg)))
     result = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": nsteps,
         "warmup": args.warmup, "ms_per_step": t_max, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32" if cfg["precision"] == "fp32" else "f64", "data": "synthetic",
-        "config": {"workload": args.workload,
-                   "mesh": f"{cfg['nx'] - 1}x{cfg['ny'] - 1} doubly periodic analytic grid, dx=1 km, "
-                           f"{cfg['nz']} layers 5->250 m",
-                   "nodes": m.N, "edges": m.E, "elements": m.M, "tracers": cfg["K"],
+        "config": {"workload": args.workload, "mesh": mesh_desc,
+                   "nodes": m.N, "edges": m.E, "elements": m.M, "tracers": K,
                    "schemes": f"{cfg['hor']}/{cfg['ver']}/{cfg['lim']}", "form": cfg["precision"], "dt_s": cfg["dt"],
                    "tracer_cells_per_step": cells, "l2": "inputs larger than L2 (no flush)",
-                   "parallelism": f"replicas x{world}",
+                   "parallelism": f"replicas x{world}", "cuda_graph_steps": cfg.get("graph_steps"),
                    "launch_cfg": tuned["cfg"] if tuned else "default"},
         "stage_ms": {k: round(v, 4) for k, v in per.items()},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "traffic": traffic, "algorithmic_bytes_per_launch": sb[dom]},
         "step_roofline": {"algorithmic_bytes_per_step": step_bytes,
+                          "bytes_per_tracer_cell": step_bytes / cells,
                           "achieved_gbs": step_bytes / (ms / 1e3) / 1e9,
                           "frac": step_bytes / (ms / 1e3) / 1e9 / peak},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -348,9 +495,7 @@ def run_gpu(args):
         "gpu_launches": launches,
         "clocks": clocks,
     }
-    if cfg.get("compare_fp64") and not args.no_fp64:
-        del eng, T0
-        torch.cuda.empty_cache()
+    if cfg.get("compare_fp64") is True and not args.no_fp64:
         m64, e64, T64 = build_case(cfg, "fp64", device)
         if not args.no_tune:
             autotune.tune(e64, cfg["dt"], reps=1)
@@ -361,10 +506,38 @@ def run_gpu(args):
                           "stage_ms": {k: round(v, 3) for k, v in per64.items()}}
         result["fp32_over_fp64"] = value / result["fp64"]["value"]
         result["gpu_launches"] += l64
+        if cfg.get("report_steps"):
+            result["precision_report"] = precision_report(m, eng, T0, e64, T64, cfg["dt"], cfg["report_steps"])
         del e64
+    elif cfg.get("compare_fp64") == "sequential" and not args.no_fp64:
+        # per-mesh sequential plain FP64 steps (eager launches, one mesh after another)
+        from fesom2_tracer_dwarf_gb300.engine import TracerAdvection
+
+        n64 = max(1, min(args.steps, args.fp64_steps))
+        tot64 = 0.0
+        for i, (n, nz, cfl) in enumerate(batch_parts(cfg)):
+            p, v, w, T = _flat_part(n, nz, "fp64", device, cfg["dt"], cfl, K, 20260301 + i)
+            e = TracerAdvection(p, K, "fp64", cfg["hor"], cfg["ver"], cfg["lim"], copy_ab=True, device=device)
+            e.load_padded(T=T, vel=v, w=w)
+            e.step(cfg["dt"])
+            torch.cuda.synchronize()
+            t0 = torch.cuda.Event(enable_timing=True)
+            t1 = torch.cuda.Event(enable_timing=True)
+            t0.record()
+            e.step(cfg["dt"], n64)
+            t1.record()
+            torch.cuda.synchronize()
+            tot64 += t0.elapsed_time(t1)
+            result["gpu_launches"] += e.launches
+            del e, p, v, w, T
+        ms64 = tot64 / n64
+        result["fp64"] = {"value": cells * world / (ms64 / 1e3), "ms_per_step": ms64, "steps": n64,
+                          "mode": "per-mesh sequential eager launches"}
+        result["fp32_over_fp64"] = value / result["fp64"]["value"]
     if rank == 0 and not args.no_cpu:
-        v, sample = cpu_sample(seconds=args.cpu_seconds, K=cfg["K"], nz=cfg["nz"], hor=cfg["hor"], ver=cfg["ver"],
-                               lim=cfg["lim"], dt=cfg["dt"])
+        nz = cfg.get("nz", 64)
+        v, sample = cpu_sample(seconds=args.cpu_seconds, K=K, nz=nz, hor=cfg["hor"], ver=cfg["ver"], lim=cfg["lim"],
+                               dt=cfg["dt"])
         result["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample}
     if rank == 0:
         print(json.dumps(result), flush=True)

@@ -141,6 +141,20 @@ int fgb_hmesh_analytic(int nx, int ny, int nl, double Lx, double Ly, double dept
   return 0;
 }
 
+int fgb_hmesh_union(const fgb_hmesh* const* parts, int count, fgb_hmesh** out) {
+  if (!parts || !out || count < 1) { set_error("bad argument"); return -1; }
+  std::vector<const HostMesh*> ps(count);
+  for (int i = 0; i < count; ++i) {
+    if (!parts[i]) { set_error("null part"); return -1; }
+    ps[i] = parts[i]->m;
+  }
+  std::string err;
+  HostMesh* m = union_meshes(ps.data(), count, &err);
+  if (!m) { set_error(err); return -1; }
+  *out = new fgb_hmesh{m};
+  return 0;
+}
+
 void fgb_hmesh_free(fgb_hmesh* h) {
   if (!h) return;
   delete h->m;

@@ -907,9 +907,10 @@ __device__ __forceinline__ void finish_node(const DMesh& m, const FastPtrs& a, i
     const float r = a.dt / av;
     V<KV> dv;
     if (fct) {
-      const float hn = g.hnode[n * LZ + k];
-      dv = fmas(*lo_or_null, hnn, muls(Tn, -hn));
-      dv = fmas(dvflux, r, dv);
+      // -T hnode + LO hnode_new as hnode_new (LO - T hnode / hnode_new): exactly
+      // zero when LO equals T and the layer keeps its thickness
+      const float ra = g.hnode[n * LZ + k] / hnn;
+      dv = fmas(sub(*lo_or_null, muls(Tn, ra)), hnn, muls(dvflux, r));
     } else {
       dv = muls(dvflux, r);
     }

@@ -555,3 +555,85 @@ void build_tables(HostMesh& m) {
 }
 
 }  // namespace fgb
+
+namespace fgb {
+
+namespace {
+template <typename T>
+void append_shift(std::vector<T>& dst, const std::vector<T>& src, T shift, bool keep_negative) {
+  for (T v : src) dst.push_back((keep_negative && v < 0) ? v : v + shift);
+}
+// rows x ncol -> rows x ld, zero padding
+void append_rows(std::vector<double>& dst, const std::vector<double>& src, size_t rows, int ncol, int ld) {
+  for (size_t r = 0; r < rows; ++r) {
+    dst.insert(dst.end(), src.begin() + r * ncol, src.begin() + (r + 1) * ncol);
+    dst.insert(dst.end(), (size_t)(ld - ncol), 0.0);
+  }
+}
+}  // namespace
+
+HostMesh* union_meshes(const HostMesh* const* parts, int count, std::string* err) {
+  if (count < 1 || !parts) {
+    if (err) *err = "union of no meshes";
+    return nullptr;
+  }
+  auto* up = new HostMesh();
+  HostMesh& u = *up;
+  const HostMesh* deepest = parts[0];
+  u.periodic = 1;
+  for (int p = 0; p < count; ++p) {
+    const HostMesh& m = *parts[p];
+    u.N += m.N;
+    u.E += m.E;
+    u.M += m.M;
+    u.edge2D_in += m.edge2D_in;
+    u.max_nie = std::max(u.max_nie, m.max_nie);
+    if (m.nl > deepest->nl) deepest = &m;
+    u.periodic = u.periodic && m.periodic;
+  }
+  u.nl = deepest->nl;
+  u.nz = u.nl - 1;
+  u.cluster_full = parts[0]->cluster_full;
+  u.orient_left = parts[0]->orient_left;
+  u.zbar = deepest->zbar;
+  u.Z = deepest->Z;
+  u.nie.assign((size_t)u.N * u.max_nie, -1);
+  int no = 0, mo = 0;
+  for (int p = 0; p < count; ++p) {
+    const HostMesh& m = *parts[p];
+    u.coord.insert(u.coord.end(), m.coord.begin(), m.coord.end());
+    append_shift(u.elem_nodes, m.elem_nodes, no, false);
+    append_shift(u.edges, m.edges, no, false);
+    append_shift(u.edge_tri, m.edge_tri, mo, true);
+    u.nlevels.insert(u.nlevels.end(), m.nlevels.begin(), m.nlevels.end());
+    u.ulevels.insert(u.ulevels.end(), m.ulevels.begin(), m.ulevels.end());
+    u.nlev_nod.insert(u.nlev_nod.end(), m.nlev_nod.begin(), m.nlev_nod.end());
+    u.ulev_nod.insert(u.ulev_nod.end(), m.ulev_nod.begin(), m.ulev_nod.end());
+    u.nlev_nod_min.insert(u.nlev_nod_min.end(), m.nlev_nod_min.begin(), m.nlev_nod_min.end());
+    u.ulev_nod_max.insert(u.ulev_nod_max.end(), m.ulev_nod_max.begin(), m.ulev_nod_max.end());
+    u.nie_num.insert(u.nie_num.end(), m.nie_num.begin(), m.nie_num.end());
+    for (int n = 0; n < m.N; ++n)
+      for (int k = 0; k < m.nie_num[n]; ++k)
+        u.nie[(size_t)(no + n) * u.max_nie + k] = m.nie[(size_t)n * m.max_nie + k] + mo;
+    u.elem_area.insert(u.elem_area.end(), m.elem_area.begin(), m.elem_area.end());
+    append_rows(u.area, m.area, m.N, m.nl, u.nl);
+    append_rows(u.areasvol, m.areasvol, m.N, m.nl, u.nl);
+    u.edge_dxdy.insert(u.edge_dxdy.end(), m.edge_dxdy.begin(), m.edge_dxdy.end());
+    u.edge_cross.insert(u.edge_cross.end(), m.edge_cross.begin(), m.edge_cross.end());
+    u.elem_cos.insert(u.elem_cos.end(), m.elem_cos.begin(), m.elem_cos.end());
+    u.grad_sca.insert(u.grad_sca.end(), m.grad_sca.begin(), m.grad_sca.end());
+    append_rows(u.hnode, m.hnode, m.N, m.nz, u.nz);
+    append_rows(u.hnode_new, m.hnode_new, m.N, m.nz, u.nz);
+    append_rows(u.helem, m.helem, m.M, m.nz, u.nz);
+    append_rows(u.Z3, m.Z3, m.N, m.nz, u.nz);
+    append_rows(u.zbar3, m.zbar3, m.N, m.nl, u.nl);
+    append_shift(u.edge_updn, m.edge_updn, mo, true);
+    u.nboundary_lay.insert(u.nboundary_lay.end(), m.nboundary_lay.begin(), m.nboundary_lay.end());
+    no += m.N;
+    mo += m.M;
+  }
+  build_tables(u);
+  return up;
+}
+
+}  // namespace fgb

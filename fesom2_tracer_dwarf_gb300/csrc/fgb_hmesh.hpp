@@ -77,6 +77,13 @@ void build_tables(HostMesh& m);
 // Recompute the vertical arrays from zbar (the analytic driver's ALE set-up).
 void ale_from_zbar(HostMesh& m);
 
+// Disjoint union of independent meshes (the batching form: one launch
+// advances all of them). Node, edge and element arrays are concatenated in
+// part order with index offsets; per-layer arrays are padded to the largest
+// nl, whose extra layers lie below every column of the shallower parts.
+// Derived tables are rebuilt, so each part's gathers keep their order.
+HostMesh* union_meshes(const HostMesh* const* parts, int count, std::string* err);
+
 constexpr double kREarth = 6367500.0;   // lib/oce_modules.F90:24
 constexpr double kPiRef = 3.14159265358979;  // lib/oce_modules.F90:19
 

@@ -181,6 +181,20 @@ class TracerAdvection:
             _lib.check(L.fgb_adv_stages(self.mesh.handle, ctypes.byref(d), stages, stream), "fgb_adv_stages")
             self.launches += L.fgb_last_launch_count()
 
+    def capture(self, dt: float, nsteps: int = 1):
+        """Record ``nsteps`` steps as one CUDA graph (torch.cuda.CUDAGraph);
+        ``graph.replay()`` then advances the tracers by nsteps steps with one
+        launch of the graph. Capturing runs one eager step first (kernel
+        attributes and lazy initialisation happen outside the capture), so the
+        tracer values advance by one step: reset them before replaying if
+        needed."""
+        self.step(dt)
+        torch.cuda.synchronize(self.device)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.step(dt, nsteps)
+        return g
+
     # ---- outputs -----------------------------------------------------------
     def values(self) -> np.ndarray:
         """(K, N, nz) tracer values as float64."""

@@ -40,14 +40,65 @@ class Mesh:
                                   None if zb is None else zb.ctypes.data_as(_lib._dp),
                                   None if en is None else en.ctypes.data_as(_lib._ip), ctypes.byref(h))
         _lib.check(rc, "fgb_hmesh_analytic")
+        self.parts = None
+        self._attach(h, upload)
+
+    def _attach(self, h, upload):
+        L = _lib.load()
         self._h = h
         s = (ctypes.c_longlong * 8)()
         _lib.check(L.fgb_hmesh_sizes(h, s), "fgb_hmesh_sizes")
         self.N, self.E, self.M, self.nl, self.max_nie, self.edge2D_in = (int(v) for v in s[:6])
         self.nz = self.nl - 1
+        self.LZ, self.LW = (self.nz + 3) // 4 * 4, (self.nl + 3) // 4 * 4  # padded layers / interfaces
         self._d = None
         if upload:
             self.upload()
+
+    @classmethod
+    def union(cls, parts, upload: bool = True) -> "Mesh":
+        """Disjoint union of independent meshes (``fgb_hmesh_union``), one
+        mesh that a single launch per stage advances. ``parts`` keeps, per
+        part, its node/edge/element offsets and layer count (``part_view``)."""
+        L = _lib.load()
+        arr = (ctypes.c_void_p * len(parts))(*[p._h.value for p in parts])
+        h = ctypes.c_void_p()
+        _lib.check(L.fgb_hmesh_union(arr, len(parts), ctypes.byref(h)), "fgb_hmesh_union")
+        self = cls.__new__(cls)
+        self.nx = self.ny = None
+        self.Lx = self.Ly = self.depth = None
+        self.periodic = all(p.periodic for p in parts)
+        self.cluster_full, self.orient_left = parts[0].cluster_full, parts[0].orient_left
+        offs, no, eo, mo = [], 0, 0, 0
+        for p in parts:
+            offs.append(dict(node=no, edge=eo, elem=mo, N=p.N, E=p.E, M=p.M, nz=p.nz, nl=p.nl))
+            no, eo, mo = no + p.N, eo + p.E, mo + p.M
+        self.parts = offs
+        self._attach(h, upload)
+        return self
+
+    def join_parts(self, arrays, axis: int = 0, layer_axis: int | None = None, layers: str = "nz"):
+        """Concatenate one array per part along the part axis (nodes or
+        elements: axis 0, or 1 for (K, N, nz) tracer stacks), zero-padding the
+        layer axis to this mesh's nz (layers="nz") or nl ("nl")."""
+        width = self.nz if layers == "nz" else self.nl
+        out = []
+        for a in arrays:
+            a = np.asarray(a)
+            if layer_axis is not None:
+                pad = [(0, 0)] * a.ndim
+                pad[layer_axis] = (0, width - a.shape[layer_axis])
+                a = np.pad(a, pad)
+            out.append(a)
+        return np.concatenate(out, axis=axis)
+
+    def part_view(self, a, i: int, kind: str = "node", axis: int = 0):
+        """Part i's slice of a node or element array of this union mesh."""
+        p = self.parts[i]
+        lo, n = (p["node"], p["N"]) if kind == "node" else (p["elem"], p["M"])
+        idx = [slice(None)] * np.ndim(a)
+        idx[axis] = slice(lo, lo + n)
+        return a[tuple(idx)]
 
     # ---- host arrays -------------------------------------------------------
     def get(self, name: str) -> np.ndarray:

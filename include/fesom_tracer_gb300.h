@@ -133,6 +133,11 @@ enum { FGB_MESH_CLUSTER_FULL = 1, FGB_MESH_ORIENT_LEFT = 2 };
 int fgb_hmesh_analytic(int nx, int ny, int nl, double Lx, double Ly, double depth, int periodic, int flags,
                        const double* zbar, const int* elem_nlev, fgb_hmesh** out);
 void fgb_hmesh_free(fgb_hmesh* h);
+/* No counterpart in the reference (the batching form): the disjoint union of
+ * `count` host meshes as one mesh, parts in order (node, edge and element
+ * indices offset by the sizes of the parts before). Layers are padded to the
+ * deepest part; each part keeps its own levels. */
+int fgb_hmesh_union(const fgb_hmesh* const* parts, int count, fgb_hmesh** out);
 /* out[0..7] = N, E, M, nl, max_nie, edge2D_in, incident-edge entries, cluster entries */
 int fgb_hmesh_sizes(const fgb_hmesh* h, long long* out8);
 /* Copies a named array (0-based indices) into out; returns its element
