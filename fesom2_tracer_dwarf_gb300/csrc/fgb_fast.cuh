@@ -36,6 +36,7 @@ namespace fast {
 constexpr int kW = 32;
 // Each kernel handles NS (1 or 2) layers per lane per pass: a warp covers
 // 32 * NS layers of a column or edge per pass.
+constexpr int kColChunk = 3 * kW;  // layers / interfaces per unrolled column round
 constexpr int kMaxDegF = 16;            // incident edges staged per node
 constexpr int kMaxClF = 24;             // cluster nodes staged per node
 
@@ -137,6 +138,10 @@ __device__ __forceinline__ V<KV> muls(const V<KV>& a, float s) {
 }
 #undef FGB_F2
 
+// Division by the fast single-precision reciprocal (about 2 ulp); the FP32
+// form's bar is a tolerance against FP64, not bit parity.
+__device__ __forceinline__ float fdv(float a, float b) { return __fdividef(a, b); }
+
 __device__ __forceinline__ float max3f(float a, float b, float c) {
   float d;
   asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
@@ -230,7 +235,7 @@ __device__ __forceinline__ void node_grad(const DMesh& m, const float* __restric
     tx = fmas(ex, ar, tx);
     ty = fmas(ey, ar, ty);
   }
-  const float inv = 1.f / tvol;
+  const float inv = fdv(1.f, tvol);
   gx = muls(tx, inv);
   gy = muls(ty, inv);
 }
@@ -424,9 +429,9 @@ __device__ __forceinline__ void stage_v(V<KV>* dst, const float* __restrict__ sr
 template <int KV>
 __device__ __forceinline__ V<KV> ppm_slope(const V<KV>* T, const float* hnn, int j) {
   const float dzm = hnn[j - 1], dz = hnn[j], dzp = hnn[j + 1];
-  const float f = dz / (dzm + dz + dzp);
-  const float s1 = f * ((2.f * dzm + dz) / (dzp + dz));
-  const float s0 = f * ((dz + 2.f * dzp) / (dzm + dz));
+  const float f = fdv(dz, dzm + dz + dzp);
+  const float s1 = f * fdv(2.f * dzm + dz, dzp + dz);
+  const float s0 = f * fdv(dz + 2.f * dzp, dzm + dz);
   V<KV> r;
 #pragma unroll
   for (int t = 0; t < KV; ++t) {
@@ -445,12 +450,12 @@ __device__ __forceinline__ V<KV> ppm_edge(const V<KV>* T, const V<KV>* D, const 
   if (z >= nzmin + 2 && z <= nzmax - 2) {
     const int j0 = z - 2;  // layer above the interface
     const float dzm = c.hnn[j0 - 1], dz = c.hnn[j0], dzp = c.hnn[j0 + 1], dzpp = c.hnn[j0 + 2];
-    const float c0 = dz / (dz + dzp);
-    const float c1 = ((2.f * dzp) * dz / (dz + dzp)) * ((dzm + dz) / (2.f * dz + dzp) - (dzpp + dzp) / (2.f * dzp + dz));
-    const float ci = 1.f / (dzm + dz + dzp + dzpp);
+    const float c0 = fdv(dz, dz + dzp);
+    const float c1 = fdv((2.f * dzp) * dz, dz + dzp) * (fdv(dzm + dz, 2.f * dz + dzp) - fdv(dzpp + dzp, 2.f * dzp + dz));
+    const float ci = fdv(1.f, dzm + dz + dzp + dzpp);
     const float P = c0 + ci * c1;
-    const float Q2 = ci * (dz * (dzm + dz) / (2.f * dz + dzp));
-    const float Q3 = ci * (dzp * (dzp + dzpp) / (dz + 2.f * dzp));
+    const float Q2 = ci * fdv(dz * (dzm + dz), 2.f * dz + dzp);
+    const float Q3 = ci * fdv(dzp * (dzp + dzpp), dz + 2.f * dzp);
     const V<KV> d = sub(T[j0 + 1], T[j0]);
     return fmas(D[j0], Q3, fmas(D[j0 + 1], -Q2, fmas(d, P, T[j0])));
   }
@@ -535,7 +540,7 @@ __device__ void vert_flux(const ColF& c, const V<KV>* T, V<KV>* D, V<KV>* TV, co
           if (nzmin + 1 == nzmax - 1) r = sub(x, r);  // written twice (lib/oce_adv_tra_ver.F90:405-411)
         } else {
           const float Z0 = c.Z[z - 1], Zm1 = c.Z[z - 2], Zm2 = c.Z[z - 3], Zp1 = c.Z[z];
-          const float ic = 1.f / (Zm1 - Z0), iu = 1.f / (Z0 - Zp1), idn = 1.f / (Zm2 - Zm1);
+          const float ic = fdv(1.f, Zm1 - Z0), iu = fdv(1.f, Z0 - Zp1), idn = fdv(1.f, Zm2 - Zm1);
           const float zb = c.zb[z - 1];
           const float a1 = (zb - Z0) * (1.f / 3.f), a2 = (zb - Zm1) * (1.f / 3.f);
           const float wp = W + fabsf(W), wm = W - fabsf(W);
@@ -557,10 +562,10 @@ __device__ void vert_flux(const ColF& c, const V<KV>* T, V<KV>* D, V<KV>* TV, co
           tvert = muls(TV[nzmin - 1], -(W * ar));
         } else if (z < nzmax) {
           if (W > 0.f) {
-            const float x = fminf(W * dt / c.hn[z - 1], 1.f);
+            const float x = fminf(fdv(W * dt, c.hn[z - 1]), 1.f);
             tvert = ppm_flux<KV>(TV[z - 1], TV[z], T[z - 1], x, true, ar * W);
           } else if (W < 0.f) {
-            const float x = fminf(-(W * dt / c.hn[z - 2]), 1.f);
+            const float x = fminf(-fdv(W * dt, c.hn[z - 2]), 1.f);
             tvert = ppm_flux<KV>(TV[z - 2], TV[z - 1], T[z - 2], x, false, ar * W);
           }
         }
@@ -660,25 +665,55 @@ __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
   V<KV>* sTA = ta_sep ? wm.v<KV>(LW) : sT;
   V<KV>* sFho = sD;
   const NbrF nb = stage_nbrs_f(m, n, reinterpret_cast<int2*>(wm.p), lane);
-  stage_f(sW, a.w + n * LW, nl, lane);
-  if (we_sep) stage_f(sWE, a.we + n * LW, nl, lane);
-  stage_f(sA, g.area + n * LW, nl, lane);
-  if (VER == 3) {
-    stage_f(sHn, g.hnode + n * LZ, nz, lane);
-    stage_f(sHnn, g.hnode_new + n * LZ, nz, lane);
-  }
-  if (VER == 1) {
-    stage_f(sZ, g.Z3 + n * LZ, nz, lane);
-    stage_f(sZb, g.zbar3 + n * LW, nl, lane);
-  }
   const int nzmin = m.ulev[n], nzmax = m.nlev[n];
   const float dt = a.dt;
   const ColF clo{sWE, sA, sHn, sHnn, sZ, sZb};
   const ColF cho{sW, sA, sHn, sHnn, sZ, sZb};
   for (int gi = 0; gi < a.G; ++gi) {
     const float* __restrict__ Tg = a.T + gi * a.gT;
-    stage_v<KV>(sT, Tg, n * LZ, LZ, lane);
-    if (ta_sep) stage_v<KV>(sTA, a.TA + gi * a.gTA, n * LZ, nz, lane);
+    const float* __restrict__ TAg = ta_sep ? a.TA + gi * a.gTA : Tg;
+    // the column (geometry with the first group) in one round of loads
+    for (int c0 = 0; c0 < (int)LW; c0 += kColChunk) {
+      float w[3], we[3], ar[3], h1[3], h2[3], z1[3], z2[3];
+      V<KV> t[3], ta[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const int k = c0 + lane + kW * c;
+        const int kw = k < nl ? k : nl - 1, kz = k < nz ? k : nz - 1, kt = k < (int)LZ ? k : LZ - 1;
+        if (gi == 0) {
+          w[c] = a.w[n * LW + kw];
+          we[c] = we_sep ? a.we[n * LW + kw] : 0.f;
+          ar[c] = g.area[n * LW + kw];
+          h1[c] = VER == 3 ? g.hnode[n * LZ + kz] : 0.f;
+          h2[c] = VER == 3 ? g.hnode_new[n * LZ + kz] : 0.f;
+          z1[c] = VER == 1 ? g.Z3[n * LZ + kz] : 0.f;
+          z2[c] = VER == 1 ? g.zbar3[n * LW + kw] : 0.f;
+        }
+        t[c] = ld<KV>(Tg, n * LZ + kt);
+        ta[c] = ta_sep ? ld<KV>(TAg, n * LZ + kt) : t[c];
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const int k = c0 + lane + kW * c;
+        if (gi == 0 && k < nl) {
+          sW[k] = w[c];
+          if (we_sep) sWE[k] = we[c];
+          sA[k] = ar[c];
+          if (VER == 1) sZb[k] = z2[c];
+        }
+        if (gi == 0 && k < nz) {
+          if (VER == 3) {
+            sHn[k] = h1[c];
+            sHnn[k] = h2[c];
+          }
+          if (VER == 1) sZ[k] = z1[c];
+        }
+        if (k < (int)LZ) {
+          sT[k] = t[c];
+          if (ta_sep) sTA[k] = ta[c];
+        }
+      }
+    }
     __syncwarp();
     // LO vertical flux: upwind with w_e on T.
     vert_flux<0, KV>(clo, sT, nullptr, nullptr, nullptr, sFlo, nl, nzmin, nzmax, 1.f, dt, lane);
@@ -694,14 +729,18 @@ __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
       float cn[NS];
       V<KV> acc[NS];
 #pragma unroll
+      float hnv[NS], hnnv[NS], avv[NS];
       for (int i = 0; i < NS; ++i) {
         const unsigned k = base + lane + kW * i;
         in[i] = k < LZ;
         kk[i] = in[i] ? k : LZ - 1;
         cn[i] = 0.f;
         acc[i] = splat<KV>(0.f);
+        hnv[i] = g.hnode[n * LZ + kk[i]];
+        hnnv[i] = g.hnode_new[n * LZ + kk[i]];
+        avv[i] = g.areasvol[n * LZ + kk[i]];
       }
-#pragma unroll 2
+#pragma unroll 3
       for (int j = 0; j < nb.deg; ++j) {
         const int2 q = nb.get(m, j);
         const unsigned ed = (unsigned)(q.x >> 1);
@@ -730,8 +769,8 @@ __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
         const V<KV> tn = sT[k];
         V<KV> l = fmas(tn, cn[i], acc[i]);
         if (z >= nzmin && z <= nzmax - 1) {
-          const float hn = g.hnode[n * LZ + k], hnn = g.hnode_new[n * LZ + k], av = g.areasvol[n * LZ + k];
-          const float ra = hn / hnn, rb = dt / (av * hnn);
+          const float hn = hnv[i], hnn = hnnv[i], av = avv[i];
+          const float ra = hn / hnn, rb = fdv(dt, av * hnn);  // ra IEEE: exactly 1 for an unchanged layer
           l = fmas(add(l, sub(sFlo[k], sFlo[k + 1])), rb, muls(tn, ra));
         }
         st<KV>(lo, n * LZ + k, l);
@@ -746,7 +785,7 @@ __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
 // (lib/oce_adv_tra_fct.F90:98-374).
 // ---------------------------------------------------------------------------
 template <int KV, int NS>
-__global__ void __launch_bounds__(128, 8) kf_ratio(DMesh m, FastPtrs a) {
+__global__ void __launch_bounds__(128, (NS == 1 ? 8 : 7)) kf_ratio(DMesh m, FastPtrs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
   const int n = blockIdx.x * (blockDim.x / kW) + wib;
@@ -853,7 +892,7 @@ __global__ void __launch_bounds__(128, 8) kf_ratio(DMesh m, FastPtrs a) {
         const int z = (int)k + 1;
         V<KV> rp = splat<KV>(0.f), rm = rp;
         if (z >= nzmin && z <= nzmax - 1) {
-          const float r = dt / g.areasvol[n * LZ + k];
+          const float r = fdv(dt, g.areasvol[n * LZ + k]);
           const V<KV> lv = ld<KV>(Lg, n * LZ + k);
           const bool edge = z == nzmax - 1 || z == nzmin;
 #pragma unroll
@@ -904,48 +943,72 @@ __device__ __forceinline__ void finish_node(const DMesh& m, const FastPtrs& a, i
   V<KV> tnew = Tn, enew = d0;
   if (act) {
     const float av = g.areasvol[n * LZ + k], hnn = g.hnode_new[n * LZ + k];
-    const float r = a.dt / av;
+    const float r = fdv(a.dt, av);
     V<KV> dv;
     if (fct) {
       // -T hnode + LO hnode_new as hnode_new (LO - T hnode / hnode_new): exactly
       // zero when LO equals T and the layer keeps its thickness
-      const float ra = g.hnode[n * LZ + k] / hnn;
+      const float ra = g.hnode[n * LZ + k] / hnn;  // IEEE: exactly 1 for an unchanged layer
       dv = fmas(sub(*lo_or_null, muls(Tn, ra)), hnn, muls(dvflux, r));
     } else {
       dv = muls(dvflux, r);
     }
     enew = add(add(d0, muls(dh, r)), dv);
-    tnew = fmas(enew, 1.f / hnn, Tn);
+    tnew = fmas(enew, fdv(1.f, hnn), Tn);
   }
   st<KV>(T, n * LZ + k, tnew);
   if (del) st<KV>(del, n * LZ + k, enew);
   if (a.TAout) st<KV>(a.TAout + gi * a.gTA, n * LZ + k, tnew);
 }
 
+// The kernel is written so that each node needs few dependent rounds of
+// memory traffic: the node's own limiting factors and vertical fluxes arrive in
+// one round (all layers at once), the values the final update needs are
+// fetched together with the first neighbours, and three incident edges are in
+// flight per round.
 template <int KV, int NS>
-__global__ void __launch_bounds__(128, (NS == 1 ? 8 : 6)) kf_update(DMesh m, FastPtrs a) {
+__global__ void __launch_bounds__(128, (NS == 1 ? 6 : 4)) kf_update(DMesh m, FastPtrs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
   const int n = blockIdx.x * (blockDim.x / kW) + wib;
   if (n >= m.N) return;
+  const GeoPtrs<float>& g = m.g32;
   const unsigned LZ = m.LZ, LW = m.LW;
   const int nl = m.nl, nz = m.nz;
   WarpMem wm{smem_raw + (size_t)wib * warp_bytes<KV>(0, kUpdVec, LW)};
   V<KV>*sLv = wm.v<KV>(LW), *sRp = wm.v<KV>(LW), *sRm = wm.v<KV>(LW);
   const NbrF nb = stage_nbrs_f(m, n, reinterpret_cast<int2*>(wm.p), lane);
   const int nzmin = m.ulev[n], nzmax = m.nlev[n];
+  const float dt = a.dt;
   for (int gi = 0; gi < a.G; ++gi) {
     const float* __restrict__ Rg = a.rpm + 2 * gi * a.gN;
     const float* __restrict__ Fg = a.adfh + gi * a.gE;
-    for (int k = lane; k < nz; k += kW) {
-      sRp[k] = ld<KV>(Rg, 2 * (n * LZ + k));
-      sRm[k] = ld<KV>(Rg, 2 * (n * LZ + k) + 1);
+    const float* __restrict__ adfv = a.adfv + gi * a.gW;
+    // own R+, R- (layers) and vertical antidiffusive fluxes (interfaces), all in one round
+    for (int c0 = 0; c0 < nl; c0 += kColChunk) {
+      V<KV> rp[3], rm[3], fv[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const int k = c0 + lane + kW * c;
+        const int kr = k < nz ? k : nz - 1, kv = k < nl ? k : nl - 1;
+        rp[c] = ld<KV>(Rg, 2 * (n * LZ + kr));
+        rm[c] = ld<KV>(Rg, 2 * (n * LZ + kr) + 1);
+        fv[c] = ld<KV>(adfv, n * LW + kv);
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const int k = c0 + lane + kW * c;
+        if (k < nz) {
+          sRp[k] = rp[c];
+          sRm[k] = rm[c];
+        }
+        if (k < nl) sLv[k] = fv[c];
+      }
     }
     __syncwarp();
-    const float* __restrict__ adfv = a.adfv + gi * a.gW;
     for (int iz = lane; iz < nl; iz += kW) {
       const int z = iz + 1;
-      V<KV> f = ld<KV>(adfv, n * LW + iz);
+      V<KV> f = sLv[iz];
       if (z == nzmin) {
         f = mul(f, vsel_min(f, splat<KV>(1.f), sRp[iz], splat<KV>(1.f), sRm[iz]));
       } else if (z > nzmin && z <= nzmax - 1) {
@@ -955,18 +1018,29 @@ __global__ void __launch_bounds__(128, (NS == 1 ? 8 : 6)) kf_update(DMesh m, Fas
     }
     __syncwarp();
     const float* __restrict__ Lg = a.lo + gi * a.gN;
+    float* __restrict__ Tg = a.T + gi * a.gT;
+    float* del = a.del ? a.del + gi * a.gN : nullptr;
     for (unsigned base = 0; base < LZ; base += kW * NS) {
       unsigned kk[NS];
-      V<KV> dh[NS], rpn[NS], rmn[NS];
+      V<KV> dh[NS], rpn[NS], rmn[NS], lo[NS], Tn[NS], d0[NS];
+      float av[NS], hnn[NS], hn[NS];
 #pragma unroll
       for (int i = 0; i < NS; ++i) {
         const unsigned k = base + lane + kW * i;
         kk[i] = k < LZ ? k : LZ - 1;
+        const unsigned kr = kk[i] < (unsigned)nz ? kk[i] : (unsigned)nz - 1;
         dh[i] = splat<KV>(0.f);
-        rpn[i] = ld<KV>(Rg, 2 * (n * LZ + kk[i]));
-        rmn[i] = ld<KV>(Rg, 2 * (n * LZ + kk[i]) + 1);
+        rpn[i] = sRp[kr];
+        rmn[i] = sRm[kr];
+        // the final update's inputs travel with the first neighbours
+        lo[i] = ld<KV>(Lg, n * LZ + kk[i]);
+        Tn[i] = ld<KV>(Tg, n * LZ + kk[i]);
+        d0[i] = del ? ld<KV>(del, n * LZ + kk[i]) : splat<KV>(0.f);
+        av[i] = g.areasvol[n * LZ + kk[i]];
+        hnn[i] = g.hnode_new[n * LZ + kk[i]];
+        hn[i] = g.hnode[n * LZ + kk[i]];
       }
-#pragma unroll 2
+#pragma unroll 3
       for (int j = 0; j < nb.deg; ++j) {
         const int2 q = nb.get(m, j);
         const unsigned ed = (unsigned)(q.x >> 1);
@@ -993,8 +1067,20 @@ __global__ void __launch_bounds__(128, (NS == 1 ? 8 : 6)) kf_update(DMesh m, Fas
       for (int i = 0; i < NS; ++i) {
         const unsigned k = base + lane + kW * i;
         if (k >= LZ) continue;
-        const V<KV> lo = ld<KV>(Lg, n * LZ + k);
-        finish_node<KV>(m, a, gi, n, k, nzmin, nzmax, dh[i], sub(sLv[k], sLv[k + 1]), &lo, true);
+        const int z = (int)k + 1;
+        V<KV> tnew = Tn[i], enew = d0[i];
+        if (z >= nzmin && z <= nzmax - 1) {
+          const float r = fdv(dt, av[i]);
+          const float ra = hn[i] / hnn[i];  // IEEE: exactly 1 for an unchanged layer
+          // -T hnode + LO hnode_new as hnode_new (LO - T hnode / hnode_new): exactly
+          // zero when LO equals T and the layer keeps its thickness
+          const V<KV> dv = fmas(sub(lo[i], muls(Tn[i], ra)), hnn[i], muls(sub(sLv[k], sLv[k + 1]), r));
+          enew = add(add(d0[i], muls(dh[i], r)), dv);
+          tnew = fmas(enew, fdv(1.f, hnn[i]), Tn[i]);
+        }
+        st<KV>(Tg, n * LZ + k, tnew);
+        if (del) st<KV>(del, n * LZ + k, enew);
+        if (a.TAout) st<KV>(a.TAout + gi * a.gTA, n * LZ + k, tnew);
       }
     }
     __syncwarp();
