@@ -568,7 +568,8 @@ def run_reference(args):
     O.build()
     with ctx.Pool(cores) as pool:
         t0 = time.perf_counter()
-        res = pool.map(_ref_worker, [(args.cpu_seconds, 65, cfg["nz"], cfg["K"], cfg["hor"], cfg["ver"],
+        nz = cfg.get("nz", 48)  # the batching form's parts have 16..64 layers
+        res = pool.map(_ref_worker, [(args.cpu_seconds, 65, nz, cfg["K"], cfg["hor"], cfg["ver"],
                                       cfg["lim"], cfg["dt"], 100 + i) for i in range(cores)])
         el = time.perf_counter() - t0
     value = sum(r[0] for r in res)
@@ -578,7 +579,7 @@ def run_reference(args):
            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "config": {"workload": args.workload, "schemes": f"{cfg['hor']}/{cfg['ver']}/{cfg['lim']}",
-                      "layers": cfg["nz"], "tracers": cfg["K"], "wall_s": el},
+                      "layers": nz, "tracers": cfg["K"], "wall_s": el},
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)

@@ -728,8 +728,8 @@ __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
       bool in[NS];
       float cn[NS];
       V<KV> acc[NS];
-#pragma unroll
       float hnv[NS], hnnv[NS], avv[NS];
+#pragma unroll
       for (int i = 0; i < NS; ++i) {
         const unsigned k = base + lane + kW * i;
         in[i] = k < LZ;
@@ -823,7 +823,7 @@ __global__ void __launch_bounds__(128, (NS == 1 ? 8 : 7)) kf_ratio(DMesh m, Fast
         mx[i] = splat<KV>(m0);
         mn[i] = splat<KV>(-m0);
       }
-#pragma unroll 2
+#pragma unroll (NS == 1 ? 8 : 4)
       for (int j = 0; j < ncl; ++j) {
         const int2 c = cl_staged ? scl[j] : make_int2(m.cl_node[c0 + j], m.cl_lev[c0 + j]);
         V<KV> lv[NS], tv[NS];
@@ -868,7 +868,7 @@ __global__ void __launch_bounds__(128, (NS == 1 ? 8 : 7)) kf_ratio(DMesh m, Fast
           mi[i].v[t] = fminf(0.f, ad0.v[t]) + fminf(0.f, -ad1.v[t]);
         }
       }
-#pragma unroll 2
+#pragma unroll (NS == 1 ? 6 : 3)
       for (int j = 0; j < nb.deg; ++j) {
         const int2 q = nb.get(m, j);
         const unsigned ed = (unsigned)(q.x >> 1);
@@ -1040,7 +1040,7 @@ __global__ void __launch_bounds__(128, (NS == 1 ? 6 : 4)) kf_update(DMesh m, Fas
         hnn[i] = g.hnode_new[n * LZ + kk[i]];
         hn[i] = g.hnode[n * LZ + kk[i]];
       }
-#pragma unroll 3
+#pragma unroll (NS == 1 ? 6 : 3)
       for (int j = 0; j < nb.deg; ++j) {
         const int2 q = nb.get(m, j);
         const unsigned ed = (unsigned)(q.x >> 1);
