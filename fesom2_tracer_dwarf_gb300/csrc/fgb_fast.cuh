@@ -785,7 +785,7 @@ __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
 // (lib/oce_adv_tra_fct.F90:98-374).
 // ---------------------------------------------------------------------------
 template <int KV, int NS>
-__global__ void __launch_bounds__(128, (NS == 1 ? 8 : 7)) kf_ratio(DMesh m, FastPtrs a) {
+__global__ void __launch_bounds__(128, (NS == 1 ? 10 : 7)) kf_ratio(DMesh m, FastPtrs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
   const int n = blockIdx.x * (blockDim.x / kW) + wib;
@@ -966,8 +966,9 @@ __device__ __forceinline__ void finish_node(const DMesh& m, const FastPtrs& a, i
 // one round (all layers at once), the values the final update needs are
 // fetched together with the first neighbours, and three incident edges are in
 // flight per round.
-template <int KV, int NS>
-__global__ void __launch_bounds__(128, (NS == 1 ? 6 : 4)) kf_update(DMesh m, FastPtrs a) {
+// DEL: a persistent del_ttf is read and written (the reference C interface).
+template <int KV, int NS, bool DEL>
+__global__ void __launch_bounds__(128, (NS == 1 ? 9 : 4)) kf_update(DMesh m, FastPtrs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
   const int n = blockIdx.x * (blockDim.x / kW) + wib;
@@ -1019,7 +1020,7 @@ __global__ void __launch_bounds__(128, (NS == 1 ? 6 : 4)) kf_update(DMesh m, Fas
     __syncwarp();
     const float* __restrict__ Lg = a.lo + gi * a.gN;
     float* __restrict__ Tg = a.T + gi * a.gT;
-    float* del = a.del ? a.del + gi * a.gN : nullptr;
+    float* del = DEL ? a.del + gi * a.gN : nullptr;
     for (unsigned base = 0; base < LZ; base += kW * NS) {
       unsigned kk[NS];
       V<KV> dh[NS], rpn[NS], rmn[NS], lo[NS], Tn[NS], d0[NS];
@@ -1035,12 +1036,12 @@ __global__ void __launch_bounds__(128, (NS == 1 ? 6 : 4)) kf_update(DMesh m, Fas
         // the final update's inputs travel with the first neighbours
         lo[i] = ld<KV>(Lg, n * LZ + kk[i]);
         Tn[i] = ld<KV>(Tg, n * LZ + kk[i]);
-        d0[i] = del ? ld<KV>(del, n * LZ + kk[i]) : splat<KV>(0.f);
+        d0[i] = DEL ? ld<KV>(del, n * LZ + kk[i]) : splat<KV>(0.f);
         av[i] = g.areasvol[n * LZ + kk[i]];
         hnn[i] = g.hnode_new[n * LZ + kk[i]];
         hn[i] = g.hnode[n * LZ + kk[i]];
       }
-#pragma unroll (NS == 1 ? 6 : 3)
+#pragma unroll 2
       for (int j = 0; j < nb.deg; ++j) {
         const int2 q = nb.get(m, j);
         const unsigned ed = (unsigned)(q.x >> 1);
@@ -1079,7 +1080,7 @@ __global__ void __launch_bounds__(128, (NS == 1 ? 6 : 4)) kf_update(DMesh m, Fas
           tnew = fmas(enew, fdv(1.f, hnn[i]), Tn[i]);
         }
         st<KV>(Tg, n * LZ + k, tnew);
-        if (del) st<KV>(del, n * LZ + k, enew);
+        if (DEL) st<KV>(del, n * LZ + k, enew);
         if (a.TAout) st<KV>(a.TAout + gi * a.gTA, n * LZ + k, tnew);
       }
     }

@@ -55,8 +55,13 @@ void launch_ratio_f(const DMesh& m, const FastPtrs& a, int nw, cudaStream_t s) {
 template <int KV, int NS>
 void launch_update_f(const DMesh& m, const FastPtrs& a, int nw, cudaStream_t s) {
   const size_t sm = nw * warp_bytes<KV>(0, kUpdVec, m.LW);
-  allow_smem_f(kf_update<KV, NS>, sm);
-  kf_update<KV, NS><<<(m.N + nw - 1) / nw, nw * kW, sm, s>>>(m, a);
+  if (a.del) {
+    allow_smem_f(kf_update<KV, NS, true>, sm);
+    kf_update<KV, NS, true><<<(m.N + nw - 1) / nw, nw * kW, sm, s>>>(m, a);
+  } else {
+    allow_smem_f(kf_update<KV, NS, false>, sm);
+    kf_update<KV, NS, false><<<(m.N + nw - 1) / nw, nw * kW, sm, s>>>(m, a);
+  }
 }
 
 template <int KV, int VER>
