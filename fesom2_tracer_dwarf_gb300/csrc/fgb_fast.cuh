@@ -911,6 +911,145 @@ __global__ void __launch_bounds__(128, (NS == 1 ? 10 : 7)) kf_ratio(DMesh m, Fas
   }
 }
 
+// Columns of at most 64 layers: one warp holds the whole column (lanes own
+// layers l and l + 32), so the vertical bound window (layers k-1, k, k+1) comes
+// from neighbouring lanes by shuffles and the kernel needs no shared memory;
+// the edge and cluster lists are read through L1. Fewer resources per warp,
+// more resident warps.
+template <int KV>
+__device__ __forceinline__ V<KV> shfl_v(const V<KV>& x, int src) {
+  V<KV> r;
+#pragma unroll
+  for (int t = 0; t < KV; ++t) r.v[t] = __shfl_sync(0xffffffffu, x.v[t], src);
+  return r;
+}
+
+template <int KV>
+__global__ void __launch_bounds__(128, 7) kf_ratio64(DMesh m, FastPtrs a) {
+  const int lane = threadIdx.x & (kW - 1);
+  const int n = blockIdx.x * (blockDim.x / kW) + threadIdx.x / kW;
+  if (n >= m.N) return;
+  const GeoPtrs<float>& g = m.g32;
+  const unsigned LZ = m.LZ, LW = m.LW;
+  const int j0 = m.ne_ptr[n], deg = m.ne_ptr[n + 1] - j0;
+  const int c0 = m.cl_ptr[n], ncl = m.cl_ptr[n + 1] - c0, minlev = m.cl_minlev[n];
+  const int nzmin = m.ulev[n], nzmax = m.nlev[n];
+  const float dt = a.dt;
+  unsigned kk[2];
+  int z[2];
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const unsigned k = lane + kW * i;
+    kk[i] = k < LZ ? k : LZ - 1;
+    z[i] = (int)k + 1;
+  }
+  for (int gi = 0; gi < a.G; ++gi) {
+    const float* __restrict__ Tg = a.T + gi * a.gT;
+    const float* __restrict__ Lg = a.lo + gi * a.gN;
+    const float* __restrict__ Fg = a.adfh + gi * a.gE;
+    const float* __restrict__ adfv = a.adfv + gi * a.gW;
+    // bounds a1-a3 over the cluster (lib/oce_adv_tra_fct.F90:105-184)
+    V<KV> mx[2], mn[2], lo[2];
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      // AUX = -/+1e3 of elements without the layer (lib/oce_adv_tra_fct.F90:139-145)
+      const float m0 = z[i] > minlev ? -1e3f : -INFINITY;
+      mx[i] = splat<KV>(m0);
+      mn[i] = splat<KV>(-m0);
+      lo[i] = ld<KV>(Lg, n * LZ + kk[i]);
+    }
+#pragma unroll 2
+    for (int j = 0; j < ncl; ++j) {
+      const int c = m.cl_node[c0 + j], lev = m.cl_lev[c0 + j];
+      V<KV> lv[2], tv[2];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        lv[i] = ld<KV>(Lg, c * LZ + kk[i]);
+        tv[i] = ld<KV>(Tg, c * LZ + kk[i]);
+      }
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+        if (z[i] <= lev) {
+#pragma unroll
+          for (int t = 0; t < KV; ++t) {
+            mx[i].v[t] = max3f(mx[i].v[t], lv[i].v[t], tv[i].v[t]);
+            mn[i].v[t] = min3f(mn[i].v[t], lv[i].v[t], tv[i].v[t]);
+          }
+        }
+    }
+    // vertical window: layer k-1 from lane - 1 (lane 31 of the first slice for the
+    // second), layer k+1 from lane + 1 (lane 0 of the second slice for the first)
+    V<KV> bmax[2], bmin[2];
+    {
+      const int up = (lane + kW - 1) & (kW - 1), dn = (lane + 1) & (kW - 1);
+      const bool first = lane == 0, last = lane == kW - 1;
+      const bool edge0 = z[0] == nzmax - 1 || z[0] == nzmin, edge1 = z[1] == nzmax - 1 || z[1] == nzmin;
+      {
+        const V<KV> u0 = shfl_v(mx[0], up), u1 = shfl_v(mx[1], up), d0 = shfl_v(mx[0], dn), d1 = shfl_v(mx[1], dn);
+#pragma unroll
+        for (int t = 0; t < KV; ++t) {
+          bmax[0].v[t] = (edge0 ? mx[0].v[t] : max3f(u0.v[t], mx[0].v[t], last ? d1.v[t] : d0.v[t])) - lo[0].v[t];
+          bmax[1].v[t] = (edge1 ? mx[1].v[t] : max3f(first ? u0.v[t] : u1.v[t], mx[1].v[t], d1.v[t])) - lo[1].v[t];
+        }
+      }
+      {
+        const V<KV> u0 = shfl_v(mn[0], up), u1 = shfl_v(mn[1], up), d0 = shfl_v(mn[0], dn), d1 = shfl_v(mn[1], dn);
+#pragma unroll
+        for (int t = 0; t < KV; ++t) {
+          bmin[0].v[t] = (edge0 ? mn[0].v[t] : min3f(u0.v[t], mn[0].v[t], last ? d1.v[t] : d0.v[t])) - lo[0].v[t];
+          bmin[1].v[t] = (edge1 ? mn[1].v[t] : min3f(first ? u0.v[t] : u1.v[t], mn[1].v[t], d1.v[t])) - lo[1].v[t];
+        }
+      }
+    }
+    // antidiffusive sums b1 (lib/oce_adv_tra_fct.F90:255-346)
+    V<KV> pl[2], mi[2];
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const V<KV> ad0 = ld<KV>(adfv, n * LW + kk[i]), ad1 = ld<KV>(adfv, n * LW + kk[i] + 1);
+#pragma unroll
+      for (int t = 0; t < KV; ++t) {
+        pl[i].v[t] = fmaxf(0.f, ad0.v[t]) + fmaxf(0.f, -ad1.v[t]);
+        mi[i].v[t] = fminf(0.f, ad0.v[t]) + fminf(0.f, -ad1.v[t]);
+      }
+    }
+#pragma unroll 2
+    for (int j = 0; j < deg; ++j) {
+      const int code = m.ne_code[j0 + j];
+      const unsigned ed = (unsigned)(code >> 1);
+      const float sg = (code & 1) ? -1.f : 1.f;
+      V<KV> f[2];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) f[i] = ld<KV>(Fg, ed * LZ + kk[i]);
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int t = 0; t < KV; ++t) {
+          const float x = sg * f[i].v[t];
+          pl[i].v[t] += fmaxf(0.f, x);
+          mi[i].v[t] += fminf(0.f, x);
+        }
+    }
+    // factors b2 (lib/oce_adv_tra_fct.F90:363-374)
+    float* __restrict__ Rg = a.rpm + 2 * gi * a.gN;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const unsigned k = lane + kW * i;
+      if (k >= LZ) continue;
+      V<KV> rp = splat<KV>(0.f), rm = rp;
+      if (z[i] >= nzmin && z[i] <= nzmax - 1) {
+        const float r = fdv(dt, g.areasvol[n * LZ + k]);
+#pragma unroll
+        for (int t = 0; t < KV; ++t) {
+          rp.v[t] = fminf(1.f, fdv(bmax[i].v[t], pl[i].v[t] * r + 1e-16f));
+          rm.v[t] = fminf(1.f, fdv(bmin[i].v[t], mi[i].v[t] * r - 1e-16f));
+        }
+      }
+      st<KV>(Rg, 2 * (n * LZ + k), rp);
+      st<KV>(Rg, 2 * (n * LZ + k) + 1, rm);
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // FCT stage 3: limiting b3 (lib/oce_adv_tra_fct.F90:396-471), flux divergence
 // (lib/oce_adv_tra_driver.F90:298-450) and the tendency update

@@ -100,8 +100,14 @@ int launch_fast(const DMesh& m, const FastPtrs& a, const LaunchArgs& L, cudaStre
       ++launches;
     }
     if (L.mask & FGB_STAGE_RATIO) {
-      if (L.ns_ratio == 1) launch_ratio_f<KV, 1>(m, a, L.nw_ratio, s);
-      else launch_ratio_f<KV, 2>(m, a, L.nw_ratio, s);
+      if (m.LZ <= 2 * kW && L.ns_ratio != 1) {
+        // whole column per warp, no shared memory
+        kf_ratio64<KV><<<(m.N + L.nw_ratio - 1) / L.nw_ratio, L.nw_ratio * kW, 0, s>>>(m, a);
+      } else if (L.ns_ratio == 1) {
+        launch_ratio_f<KV, 1>(m, a, L.nw_ratio, s);
+      } else {
+        launch_ratio_f<KV, 2>(m, a, L.nw_ratio, s);
+      }
       ++launches;
     }
     if (L.mask & FGB_STAGE_UPDATE) {
