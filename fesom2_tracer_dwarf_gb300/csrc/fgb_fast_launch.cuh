@@ -100,7 +100,7 @@ int launch_fast(const DMesh& m, const FastPtrs& a, const LaunchArgs& L, cudaStre
       ++launches;
     }
     if (L.mask & FGB_STAGE_RATIO) {
-      if (m.LZ <= 2 * kW && L.ns_ratio != 1) {
+      if (m.LZ <= 2 * kW && (L.ns_ratio == 0 || L.ns_ratio == 3)) {
         // whole column per warp, no shared memory
         kf_ratio64<KV><<<(m.N + L.nw_ratio - 1) / L.nw_ratio, L.nw_ratio * kW, 0, s>>>(m, a);
       } else if (L.ns_ratio == 1) {
@@ -111,8 +111,8 @@ int launch_fast(const DMesh& m, const FastPtrs& a, const LaunchArgs& L, cudaStre
       ++launches;
     }
     if (L.mask & FGB_STAGE_UPDATE) {
-      if (L.ns_upd == 1) launch_update_f<KV, 1>(m, a, L.nw_upd, s);
-      else launch_update_f<KV, 2>(m, a, L.nw_upd, s);
+      if (L.ns_upd == 2) launch_update_f<KV, 2>(m, a, L.nw_upd, s);
+      else launch_update_f<KV, 1>(m, a, L.nw_upd, s);
       ++launches;
     }
   } else if (L.mask & FGB_STAGE_UPDATE) {

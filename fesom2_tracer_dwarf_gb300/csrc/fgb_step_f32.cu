@@ -84,8 +84,10 @@ int launch_stages_f32(const DMesh& m, const fgb_step_desc& d, int mask, cudaStre
   auto ns = [](int want, int def) { return (want == 1 || want == 2) ? want : def; };
   L.ns_h = ns(d.cfg[7], 2);
   L.ns_lo = ns(d.cfg[4], 2);
-  L.ns_ratio = ns(d.cfg[5], 2);
-  L.ns_upd = ns(d.cfg[6], 2);
+  // ratio: 1 or 2 layers per lane with shared-memory staging, or 3 (the default)
+  // the whole column per warp without shared memory
+  L.ns_ratio = (d.cfg[5] >= 1 && d.cfg[5] <= 3) ? d.cfg[5] : 0;
+  L.ns_upd = ns(d.cfg[6], 1);
   L.hor = d.hor;
   L.ver = d.ver;
   L.fct = d.lim == FGB_LIM_FCT;

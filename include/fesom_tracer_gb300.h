@@ -199,8 +199,12 @@ typedef struct {
    *            kernels: 1, 2, 4 (default 4)
    * cfg[4..6]  FP64 form: tracers per chunk of the same three kernels: 1, 2,
    *            4, used when it divides ntracers (default: the largest of 4, 2,
-   *            1 that does). The FP32 form works one tracer group at a time.
-   * cfg[7]     reserved, 0 */
+   *            1 that does). FP32 form (one tracer group at a time): layers
+   *            per lane per pass, 1 or 2 with the column staged in shared
+   *            memory (defaults: LO 2, update 1), or 3 for the ratio kernel
+   *            without shared memory (its default; columns of at most 64
+   *            layers).
+   * cfg[7]     FP32 form: layers per lane per pass of the edge-flux kernel, 1 or 2 */
   int cfg[8];
 } fgb_step_desc;
 
