@@ -295,7 +295,10 @@ def precision_report(m, e32, T32, e64, T64, dt, steps):
     return out
 
 
-def time_engine(eng, T0, dt, steps, warmup, dist_barrier, per_stage=True):
+def time_engine(eng, T0, dt, steps, warmup, dist_barrier, stage_steps=5):
+    """Full steps between CUDA events (the timed region), then a per-stage
+    breakdown on separate steps that launch one stage at a time (stages that
+    overlap inside a full step are timed apart there)."""
     import torch
 
     from fesom2_tracer_dwarf_gb300 import _lib
@@ -309,23 +312,30 @@ def time_engine(eng, T0, dt, steps, warmup, dist_barrier, per_stage=True):
         eng.step(dt)
     eng.T.copy_(T0)
     torch.cuda.synchronize()
-    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(len(stages) + 1)] for _ in range(steps)]
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     launches0 = eng.launches
     dist_barrier()
     torch.cuda.synchronize()
     start.record()
-    for k in range(steps):
-        ev[k][0].record()
-        for i, st in enumerate(stages):
-            eng.step(dt, stages=st)
-            ev[k][i + 1].record()
+    for _ in range(steps):
+        eng.step(dt)
     end.record()
     torch.cuda.synchronize()
     dist_barrier()
     total_ms = start.elapsed_time(end)
-    per = {n: statistics.mean(ev[k][i].elapsed_time(ev[k][i + 1]) for k in range(steps)) for i, n in enumerate(names)}
-    return total_ms, per, eng.launches - launches0
+    launches = eng.launches - launches0
+    # stage breakdown
+    nst = max(1, min(steps, stage_steps))
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(len(stages) + 1)] for _ in range(nst)]
+    for k in range(nst):
+        ev[k][0].record()
+        for i, st in enumerate(stages):
+            eng.step(dt, stages=st)
+            ev[k][i + 1].record()
+    torch.cuda.synchronize()
+    per = {n: statistics.mean(ev[k][i].elapsed_time(ev[k][i + 1]) for k in range(nst)) for i, n in enumerate(names)}
+    eng.T.copy_(T0)
+    return total_ms, per, launches
 
 
 def time_e2e(eng, T0, dt, steps, dist_barrier):

@@ -49,8 +49,8 @@ def stage_candidates(stage: str, K: int, precision: str = "fp64"):
         return [{0: w} for w in EDGE_WARPS]
     slot = {"lo": 0, "ratio": 1, "update": 2}[stage]
     if precision == "fp32":
-        # the ratio kernel also has a variant without shared memory (3)
-        slices = SLICES + ((3,) if stage == "ratio" else ())
+        # the ratio kernel also has variants without shared memory (3; 4: fewer registers)
+        slices = SLICES + ((3, 4) if stage == "ratio" else ())
         return [{1 + slot: w, 4 + slot: ns} for w, ns in product(NODE_WARPS, slices)]
     return [{1 + slot: w, 4 + slot: c} for w, c in product(NODE_WARPS, chunk_candidates(K))]
 

@@ -924,8 +924,9 @@ __device__ __forceinline__ V<KV> shfl_v(const V<KV>& x, int src) {
   return r;
 }
 
-template <int KV>
-__global__ void __launch_bounds__(128, 7) kf_ratio64(DMesh m, FastPtrs a) {
+// LEAN: fewer registers (64, one cluster node in flight) for more resident warps.
+template <int KV, bool LEAN>
+__global__ void __launch_bounds__(128, LEAN ? 8 : 7) kf_ratio64(DMesh m, FastPtrs a) {
   const int lane = threadIdx.x & (kW - 1);
   const int n = blockIdx.x * (blockDim.x / kW) + threadIdx.x / kW;
   if (n >= m.N) return;
@@ -958,7 +959,7 @@ __global__ void __launch_bounds__(128, 7) kf_ratio64(DMesh m, FastPtrs a) {
       mn[i] = splat<KV>(-m0);
       lo[i] = ld<KV>(Lg, n * LZ + kk[i]);
     }
-#pragma unroll 2
+#pragma unroll(LEAN ? 1 : 2)
     for (int j = 0; j < ncl; ++j) {
       const int c = m.cl_node[c0 + j], lev = m.cl_lev[c0 + j];
       V<KV> lv[2], tv[2];

@@ -100,9 +100,11 @@ int launch_fast(const DMesh& m, const FastPtrs& a, const LaunchArgs& L, cudaStre
       ++launches;
     }
     if (L.mask & FGB_STAGE_RATIO) {
-      if (m.LZ <= 2 * kW && (L.ns_ratio == 0 || L.ns_ratio == 3)) {
+      if (m.LZ <= 2 * kW && (L.ns_ratio == 0 || L.ns_ratio >= 3)) {
         // whole column per warp, no shared memory
-        kf_ratio64<KV><<<(m.N + L.nw_ratio - 1) / L.nw_ratio, L.nw_ratio * kW, 0, s>>>(m, a);
+        const unsigned grid = (m.N + L.nw_ratio - 1) / L.nw_ratio;
+        if (L.ns_ratio == 4) kf_ratio64<KV, true><<<grid, L.nw_ratio * kW, 0, s>>>(m, a);
+        else kf_ratio64<KV, false><<<grid, L.nw_ratio * kW, 0, s>>>(m, a);
       } else if (L.ns_ratio == 1) {
         launch_ratio_f<KV, 1>(m, a, L.nw_ratio, s);
       } else {

@@ -86,7 +86,7 @@ int launch_stages_f32(const DMesh& m, const fgb_step_desc& d, int mask, cudaStre
   L.ns_lo = ns(d.cfg[4], 2);
   // ratio: 1 or 2 layers per lane with shared-memory staging, or 3 (the default)
   // the whole column per warp without shared memory
-  L.ns_ratio = (d.cfg[5] >= 1 && d.cfg[5] <= 3) ? d.cfg[5] : 0;
+  L.ns_ratio = (d.cfg[5] >= 1 && d.cfg[5] <= 4) ? d.cfg[5] : 0;
   L.ns_upd = ns(d.cfg[6], 1);
   L.hor = d.hor;
   L.ver = d.ver;

@@ -201,9 +201,9 @@ typedef struct {
    *            4, used when it divides ntracers (default: the largest of 4, 2,
    *            1 that does). FP32 form (one tracer group at a time): layers
    *            per lane per pass, 1 or 2 with the column staged in shared
-   *            memory (defaults: LO 2, update 1), or 3 for the ratio kernel
-   *            without shared memory (its default; columns of at most 64
-   *            layers).
+   *            memory (defaults: LO 2, update 1), or for the ratio kernel
+   *            3 (its default) / 4 without shared memory, 4 with fewer
+   *            registers (columns of at most 64 layers).
    * cfg[7]     FP32 form: layers per lane per pass of the edge-flux kernel, 1 or 2 */
   int cfg[8];
 } fgb_step_desc;

@@ -19,7 +19,7 @@ def test_candidates_cover_allowed_values():
     up = autotune.stage_candidates("update", 2)
     assert all(set(c) == {3, 6} for c in up)
     r32 = autotune.stage_candidates("ratio", 4, "fp32")
-    assert len(r32) == 9 and {2: 4, 5: 1} in r32 and {2: 2, 5: 3} in r32
+    assert len(r32) == 12 and {2: 4, 5: 1} in r32 and {2: 2, 5: 3} in r32 and {2: 1, 5: 4} in r32
     assert {0: 2, 7: 1} in autotune.stage_candidates("hflux", 4, "fp32")
 
 
@@ -59,6 +59,7 @@ CFGS = [
     [8, 4, 2, 2, 4, 1, 2, 1],
     [2, 1, 2, 4, 4, 2, 4, 0],
     [4, 2, 2, 2, 1, 3, 3, 2],
+    [2, 4, 1, 4, 2, 4, 2, 1],
 ]
 
 
@@ -87,7 +88,7 @@ def test_autotune_returns_valid_config_and_restores_fields(tmp_path):
     cfg = res["cfg"]
     assert cfg[0] in autotune.EDGE_WARPS
     assert all(c in autotune.NODE_WARPS for c in cfg[1:4])
-    assert all(c in autotune.SLICES + (3,) for c in cfg[4:8])  # FP32: layers per lane per pass
+    assert all(c in autotune.SLICES + (3, 4) for c in cfg[4:8])  # FP32: layers per lane per pass
     assert set(res["ms"]) == {"hflux", "lo", "ratio", "update"}
     assert np.array_equal(e.values(), before)
     again = autotune.tune(e, dt=200.0, cache_path=str(tmp_path / "t.json"))
