@@ -49,6 +49,7 @@ class StepDesc(ctypes.Structure):
         ("workspace_bytes", ctypes.c_longlong),
         ("tracer_vec", ctypes.c_int),
         ("cfg", ctypes.c_int * 8),
+        ("wi", _vp),
     ]
 
 

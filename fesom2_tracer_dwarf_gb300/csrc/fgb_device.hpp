@@ -67,6 +67,7 @@ struct StepPtrs {
   const R* vel;     // (M,LZ,2) horizontal velocity on elements
   const R* w;       // (N,LW) vertical velocity used by the high-order flux under FCT
   const R* we;      // (N,LW) explicit vertical velocity
+  const R* wi;      // optional (N,LW) implicit vertical velocity (w_split)
   R* vf;            // (E,LZ) volume flux through the edge segments
   R* adfh;          // (K,E,LZ) antidiffusive (FCT) or high-order horizontal flux
   R* lo;            // (K,N,LZ) low-order solution fct_LO
@@ -88,6 +89,7 @@ struct FastPtrs {
   const float* vel;  // (M,LZ,2)
   const float* w;    // (N,LW)
   const float* we;   // (N,LW)
+  const float* wi;   // optional (N,LW): w_split
   float* vf;         // (E,LZ)
   float* adfh;       // (G,E,LZ,KV)
   float* lo;         // (G,N,LZ,KV)

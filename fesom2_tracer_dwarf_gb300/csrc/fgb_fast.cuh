@@ -639,7 +639,7 @@ struct WarpMem {
 // node: role 0 -(vp T_n + vm T_o)/2, role 1 +(vp T_o + vm T_n)/2, with
 // vp = v + |v|, vm = v - |v|; the T_n coefficients are summed first.
 // ---------------------------------------------------------------------------
-template <int VER, int KV, int NS>
+template <int VER, int KV, int NS, bool WSPLIT>
 __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
@@ -715,13 +715,16 @@ __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
       }
     }
     __syncwarp();
-    // LO vertical flux: upwind with w_e on T.
-    vert_flux<0, KV>(clo, sT, nullptr, nullptr, nullptr, sFlo, nl, nzmin, nzmax, 1.f, dt, lane);
+    // LO vertical flux: upwind on T with w_e; under w_split the antidiffusive
+    // flux takes the upwind flux of the full w instead
+    // (lib/oce_adv_tra_driver.F90:221-231).
+    vert_flux<0, KV>(WSPLIT ? cho : clo, sT, nullptr, nullptr, nullptr, sFlo, nl, nzmin, nzmax, 1.f, dt, lane);
     // HO vertical flux on T_AB with w; adf_v = HO - LO.
     vert_flux<VER, KV>(cho, sTA, sD, sTV, sFlo, sFho, nl, nzmin, nzmax, a.pv, dt, lane);
     float* __restrict__ adfv = a.adfv + gi * a.gW;
     for (int iz = lane; iz < nl - 1; iz += kW) st<KV>(adfv, n * LW + iz, sFho[iz]);
     if (lane == 0) st<KV>(adfv, n * LW + nl - 1, sFho[nl - 1]);
+    if (WSPLIT) vert_flux<0, KV>(clo, sT, nullptr, nullptr, nullptr, sFlo, nl, nzmin, nzmax, 1.f, dt, lane);
     float* __restrict__ lo = a.lo + gi * a.gN;
     for (unsigned base = 0; base < LZ; base += kW * NS) {
       unsigned kk[NS];

@@ -33,8 +33,13 @@ template <int KV, int VER, int NS>
 void launch_lo_f(const DMesh& m, const FastPtrs& a, int nw, cudaStream_t s) {
   const LoCols c = lo_cols(VER, a.we != a.w, a.TA != a.T);
   const size_t sm = nw * warp_bytes<KV>(c.scal, c.vec, m.LW);
-  allow_smem_f(kf_lo<VER, KV, NS>, sm);
-  kf_lo<VER, KV, NS><<<(m.N + nw - 1) / nw, nw * kW, sm, s>>>(m, a);
+  if (a.wi) {
+    allow_smem_f(kf_lo<VER, KV, NS, true>, sm);
+    kf_lo<VER, KV, NS, true><<<(m.N + nw - 1) / nw, nw * kW, sm, s>>>(m, a);
+  } else {
+    allow_smem_f(kf_lo<VER, KV, NS, false>, sm);
+    kf_lo<VER, KV, NS, false><<<(m.N + nw - 1) / nw, nw * kW, sm, s>>>(m, a);
+  }
 }
 
 template <int KV, int VER, int NS>

@@ -26,11 +26,11 @@ template <typename R>
 struct GeoSel;
 template <>
 struct GeoSel<double> {
-  __device__ static const GeoPtrs<double>& get(const DMesh& m) { return m.g64; }
+  __host__ __device__ static const GeoPtrs<double>& get(const DMesh& m) { return m.g64; }
 };
 template <>
 struct GeoSel<float> {
-  __device__ static const GeoPtrs<float>& get(const DMesh& m) { return m.g32; }
+  __host__ __device__ static const GeoPtrs<float>& get(const DMesh& m) { return m.g32; }
 };
 
 template <typename R>
@@ -646,6 +646,14 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_fct_lo(DMesh 
       }
     }
     __syncwarp();  // every lane has read the LO fluxes before they are overwritten
+    if (a.wi) {
+      // w_split: the antidiffusive flux takes the upwind flux of the full w
+      // (lib/oce_adv_tra_driver.F90:221-231)
+      for (int i = 0; i < KC; ++i) {
+        Col<R> clw{sT + i * LW, sW, sA, sHn, sHnn, sZ, sX, nullptr};
+        column_ver_flux<R, 0>(clw, nullptr, nullptr, sFv + i * LW, nl, nzmin, nzmax, R(1), dt, lane);
+      }
+    }
     // HO vertical flux on T_AB with w; adf_v = HO - LO ("X - flux").
     for (int i = 0; i < KC; ++i) {
       Col<R> cho{(ta_sep ? sTA : sT) + i * LW, sW, sA, sHn, sHnn, sZ, sX, nullptr};

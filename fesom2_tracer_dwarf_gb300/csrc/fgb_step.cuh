@@ -9,6 +9,7 @@
 #include "fesom_tracer_gb300.h"
 #include "fgb_internal.hpp"
 #include "fgb_kernels.cuh"
+#include "fgb_vimpl.cuh"
 
 namespace fgb {
 
@@ -105,6 +106,11 @@ int launch_stages(const DMesh& m, const fgb_step_desc& d, int mask, cudaStream_t
     *err = "QR4C/PPM need at least two layers in every column";
     return -1;
   }
+  const bool fct = d.lim == FGB_LIM_FCT;
+  const bool wsplit = fct && d.wi;
+  if (wsplit) {
+    if (const char* why = vert_impl_check<R>(m)) { *err = why; return -1; }
+  }
   char* ws = static_cast<char*>(d.workspace);
   StepPtrs<R> a;
   a.T = static_cast<R*>(d.T);
@@ -113,6 +119,7 @@ int launch_stages(const DMesh& m, const fgb_step_desc& d, int mask, cudaStream_t
   a.vel = static_cast<const R*>(d.vel);
   a.w = static_cast<const R*>(d.w);
   a.we = static_cast<const R*>(d.we);
+  a.wi = wsplit ? static_cast<const R*>(d.wi) : nullptr;
   a.vf = reinterpret_cast<R*>(ws + wl.off[0]);
   a.adfh = reinterpret_cast<R*>(ws + wl.off[2]);
   a.lo = reinterpret_cast<R*>(ws + wl.off[3]);
@@ -128,7 +135,6 @@ int launch_stages(const DMesh& m, const fgb_step_desc& d, int mask, cudaStream_t
   a.ph = (R)d.ph;
   a.pv = (R)d.pv;
   a.K = K;
-  const bool fct = d.lim == FGB_LIM_FCT;
   auto pick_w = [](int want, int a, int b, int c, int def) {
     return (want == a || want == b || want == c) ? want : def;
   };
@@ -155,6 +161,10 @@ int launch_stages(const DMesh& m, const fgb_step_desc& d, int mask, cudaStream_t
       else if (kc_lo == 2) launch_lo_ver<R, 2>(m, a, d.ver, nw_lo, s);
       else launch_lo_ver<R, 1>(m, a, d.ver, nw_lo, s);
       ++launches;
+      if (wsplit) {
+        launch_vert_impl<R>(m, GeoSel<R>::get(m), a.lo, a.wi, K, 1, a.sN, a.dt, s);
+        ++launches;
+      }
     }
     if (mask & FGB_STAGE_RATIO) {
       if (kc_ratio == 4) launch_ratio<R, 4>(m, a, nw_ratio, s);

@@ -3,6 +3,7 @@
 #include <cstdint>
 
 #include "fgb_internal.hpp"
+#include "fgb_vimpl.cuh"
 
 namespace fgb {
 namespace fast {
@@ -51,6 +52,11 @@ int launch_stages_f32(const DMesh& m, const fgb_step_desc& d, int mask, cudaStre
     *err = "FP32 tracer arrays must be aligned to their group (4 * tracer_vec bytes, strides multiples of tracer_vec)";
     return -1;
   }
+  const bool wsplit = d.lim == FGB_LIM_FCT && d.wi;
+  if (wsplit) {
+    if (const char* why = vert_impl_check<float>(m)) { *err = why; return -1; }
+    if (reinterpret_cast<uintptr_t>(d.wi) % 4 != 0) { *err = "wi must be 4-byte aligned"; return -1; }
+  }
   char* ws = static_cast<char*>(d.workspace);
   FastPtrs a;
   a.T = static_cast<float*>(d.T);
@@ -59,6 +65,7 @@ int launch_stages_f32(const DMesh& m, const fgb_step_desc& d, int mask, cudaStre
   a.vel = static_cast<const float*>(d.vel);
   a.w = static_cast<const float*>(d.w);
   a.we = static_cast<const float*>(d.we);
+  a.wi = wsplit ? static_cast<const float*>(d.wi) : nullptr;
   a.vf = reinterpret_cast<float*>(ws + wl.off[0]);
   a.adfh = reinterpret_cast<float*>(ws + wl.off[2]);
   a.lo = reinterpret_cast<float*>(ws + wl.off[3]);
@@ -91,10 +98,23 @@ int launch_stages_f32(const DMesh& m, const fgb_step_desc& d, int mask, cudaStre
   L.hor = d.hor;
   L.ver = d.ver;
   L.fct = d.lim == FGB_LIM_FCT;
+  auto run = [&](int stage_mask) {
+    LaunchArgs Ls = L;
+    Ls.mask = stage_mask;
+    if (KV == 4) return launch_fast_kv4(m, a, Ls, s);
+    if (KV == 2) return launch_fast_kv2(m, a, Ls, s);
+    return launch_fast_kv1(m, a, Ls, s);
+  };
   int n = 0;
-  if (KV == 4) n = launch_fast_kv4(m, a, L, s);
-  else if (KV == 2) n = launch_fast_kv2(m, a, L, s);
-  else n = launch_fast_kv1(m, a, L, s);
+  if (wsplit && (mask & FGB_STAGE_LO)) {
+    // the implicit vertical step on the LO solution, between the LO and ratio kernels
+    n += run(mask & (FGB_STAGE_VFLUX | FGB_STAGE_HFLUX | FGB_STAGE_LO));
+    launch_vert_impl<float>(m, m.g32, a.lo, a.wi, K, KV, a.gN, a.dt, s);
+    ++n;
+    n += run(mask & (FGB_STAGE_RATIO | FGB_STAGE_UPDATE));
+  } else {
+    n = run(mask);
+  }
   *nlaunch = n;
   cudaError_t ce = cudaGetLastError();
   if (ce != cudaSuccess) {

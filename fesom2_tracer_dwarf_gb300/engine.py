@@ -58,6 +58,7 @@ class TracerAdvection:
         self.vel = z(m.M, m.LZ, 2)
         self.w = z(m.N, m.LW)
         self.we = self.w
+        self.wi = None  # w_split off
         L = _lib.load()
         nbytes = L.fgb_workspace_bytes(m.handle, _PREC[precision], self.K)
         if nbytes < 0:
@@ -124,8 +125,13 @@ class TracerAdvection:
             vab = v if values_ab is None else self._pad_nodes(values_ab, m.nz, m.LZ).reshape(self.K, m.N, m.LZ)
             self.TA.copy_(self.to_layout(vab) if values_ab is not None else v)
 
-    def set_velocity(self, vel, w, we=None):
-        """vel: (M, nz, 2) on elements; w, we: (N, nl) at node interfaces."""
+    def set_velocity(self, vel, w, we=None, wi=None):
+        """vel: (M, nz, 2) on elements; w, we, wi: (N, nl) at node interfaces.
+
+        wi switches w_split on (dynamics%use_wsplit): under FCT the low-order
+        solution gets the implicit vertical step with wi and the explicit
+        low-order flux uses we (lib/oce_adv_tra_driver.F90:191-231). None
+        switches it off."""
         m = self.mesh
         v = torch.zeros(m.M, m.LZ, 2, dtype=self.dtype)
         v[:, : m.nz, :] = torch.as_tensor(np.asarray(vel) if not torch.is_tensor(vel) else vel.cpu(), dtype=self.dtype)
@@ -135,10 +141,11 @@ class TracerAdvection:
             self.we = self.w
         else:
             self.we = self._pad_nodes(we, m.nl, m.LW)
+        self.wi = None if wi is None else self._pad_nodes(wi, m.nl, m.LW)
 
-    def load_padded(self, T=None, TA=None, vel=None, w=None, we=None):
+    def load_padded(self, T=None, TA=None, vel=None, w=None, we=None, wi=None):
         """Copy device tensors that already have the padded layouts
-        (K,N,LZ), (M,LZ,2), (N,LW)."""
+        (K,N,LZ), (M,LZ,2), (N,LW). wi (w_split) is kept until replaced."""
         if T is not None:
             self.T.copy_(self.to_layout(T))
         if TA is not None and self.TA is not None:
@@ -150,6 +157,8 @@ class TracerAdvection:
             self.we = self.w
         if we is not None:
             self.we = we.to(self.dtype).contiguous()
+        if wi is not None:
+            self.wi = wi.to(self.dtype).contiguous()
 
     # ---- step --------------------------------------------------------------
     def _desc(self, dt):
@@ -166,6 +175,7 @@ class TracerAdvection:
         d.tracer_vec = self.V
         d.TAout = None
         d.vel, d.w, d.we = self.vel.data_ptr(), self.w.data_ptr(), self.we.data_ptr()
+        d.wi = None if self.wi is None else self.wi.data_ptr()
         d.del_ = None
         d.workspace = self.workspace.data_ptr()
         d.workspace_bytes = self.workspace.numel()

@@ -206,6 +206,13 @@ typedef struct {
    *            registers (columns of at most 64 layers).
    * cfg[7]     FP32 form: layers per lane per pass of the edge-flux kernel, 1 or 2 */
   int cfg[8];
+  /* w_split (dynamics%use_wsplit, lib/oce_adv_tra_driver.F90:221-231): NULL
+   * for off, else the implicit vertical velocity wi (N,LW). Under FCT the
+   * low-order solution then gets the implicit vertical step with wi
+   * (adv_tra_vert_impl, lib/oce_adv_tra_ver.F90:90-244; columns of at least
+   * two layers) and the antidiffusive vertical flux takes the upwind flux of
+   * w instead of we. Without FCT it has no effect, as in the reference. */
+  const void* wi;
 } fgb_step_desc;
 
 /* Full step: vflux, hflux, and the FCT (lo, ratio, update) or plain update. */

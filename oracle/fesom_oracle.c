@@ -1286,6 +1286,74 @@ static void flux2dtracer(const omesh* m, double dt, double* dttf_h, double* dttf
   }
 }
 
+/* adv_tra_vert_impl, lib/oce_adv_tra_ver.F90:90-244: implicit upwind
+ * vertical advection with W (the w_split part) applied to ttf in place, one
+ * tridiagonal (Thomas) solve per column. Columns need at least two layers
+ * (with one, the reference reads ttf(nzmin-1)). The zbar_n / Z_n profile the
+ * reference computes first is not used by the coefficients and is omitted. */
+static void vert_impl(const omesh* m, double dt, const double* W, double* ttf) {
+  const int nl = m->nl, nzl = nl - 1;
+  double* a = (double*)xcalloc(nl + 1, sizeof(double));
+  double* b = (double*)xcalloc(nl + 1, sizeof(double));
+  double* c = (double*)xcalloc(nl + 1, sizeof(double));
+  double* tr = (double*)xcalloc(nl + 1, sizeof(double));
+  double* cp = (double*)xcalloc(nl + 1, sizeof(double));
+  double* tp = (double*)xcalloc(nl + 1, sizeof(double));
+  for (int n = 1; n <= m->nod2D; ++n) {
+    for (int k = 0; k <= nl; ++k) a[k] = b[k] = c[k] = tr[k] = tp[k] = cp[k] = 0.0;
+    const int nzmax = m->nlevels_nod2D[n - 1], nzmin = m->ulevels_nod2D[n - 1];
+    const double zinv = 1.0 * dt;
+    double v_adv;
+    int nz = nzmin;
+    a[nz] = 0.0;
+    v_adv = zinv * A2(m->area, nl, nz, n) / A2(m->areasvol, nl, nz, n);
+    b[nz] = A2(m->hnode_new, nzl, nz, n) + A2(W, nl, nz, n) * v_adv;
+    v_adv = zinv * A2(m->area, nl, nz + 1, n) / A2(m->areasvol, nl, nz, n);
+    b[nz] = b[nz] - dmin(0.0, A2(W, nl, nz + 1, n)) * v_adv;
+    c[nz] = -(dmax(0.0, A2(W, nl, nz + 1, n)) * v_adv);
+    for (nz = nzmin + 1; nz <= nzmax - 2; ++nz) {
+      v_adv = zinv * A2(m->area, nl, nz, n) / A2(m->areasvol, nl, nz, n);
+      a[nz] = dmin(0.0, A2(W, nl, nz, n)) * v_adv;
+      b[nz] = A2(m->hnode_new, nzl, nz, n) + dmax(0.0, A2(W, nl, nz, n)) * v_adv;
+      v_adv = zinv * A2(m->area, nl, nz + 1, n) / A2(m->areasvol, nl, nz, n);
+      b[nz] = b[nz] - dmin(0.0, A2(W, nl, nz + 1, n)) * v_adv;
+      c[nz] = -(dmax(0.0, A2(W, nl, nz + 1, n)) * v_adv);
+    }
+    nz = nzmax - 1;
+    v_adv = zinv * A2(m->area, nl, nz, n) / A2(m->areasvol, nl, nz, n);
+    a[nz] = dmin(0.0, A2(W, nl, nz, n)) * v_adv;
+    b[nz] = A2(m->hnode_new, nzl, nz, n) + dmax(0.0, A2(W, nl, nz, n)) * v_adv;
+    c[nz] = 0.0;
+    nz = nzmin;
+    double dz = A2(m->hnode_new, nzl, nz, n);
+    tr[nz] = -((b[nz] - dz) * A2(ttf, nzl, nz, n)) - c[nz] * A2(ttf, nzl, nz + 1, n);
+    for (nz = nzmin + 1; nz <= nzmax - 2; ++nz) {
+      dz = A2(m->hnode_new, nzl, nz, n);
+      tr[nz] = -(a[nz] * A2(ttf, nzl, nz - 1, n)) - (b[nz] - dz) * A2(ttf, nzl, nz, n) - c[nz] * A2(ttf, nzl, nz + 1, n);
+    }
+    nz = nzmax - 1;
+    dz = A2(m->hnode_new, nzl, nz, n);
+    tr[nz] = -(a[nz] * A2(ttf, nzl, nz - 1, n)) - (b[nz] - dz) * A2(ttf, nzl, nz, n);
+    nz = nzmin;
+    cp[nz] = c[nz] / b[nz];
+    tp[nz] = tr[nz] / b[nz];
+    for (nz = nzmin + 1; nz <= nzmax - 1; ++nz) {
+      const double mm = b[nz] - cp[nz - 1] * a[nz];
+      cp[nz] = c[nz] / mm;
+      tp[nz] = (tr[nz] - tp[nz - 1] * a[nz]) / mm;
+    }
+    tr[nzmax - 1] = tp[nzmax - 1];
+    for (nz = nzmax - 2; nz >= nzmin; --nz) tr[nz] = tp[nz] - cp[nz] * tr[nz + 1];
+    for (nz = nzmin; nz <= nzmax - 1; ++nz) A2(ttf, nzl, nz, n) = A2(ttf, nzl, nz, n) + tr[nz];
+  }
+  free(a);
+  free(b);
+  free(c);
+  free(tr);
+  free(cp);
+  free(tp);
+}
+
 /* ------------------------------------------------------------------------- */
 /* do_oce_adv_tra, lib/oce_adv_tra_driver.F90:23-294                           */
 /* ------------------------------------------------------------------------- */
@@ -1293,10 +1361,12 @@ static void flux2dtracer(const omesh* m, double dt, double* dttf_h, double* dttf
 int om_do_oce_adv_tra(const omesh* m, omwork* wk, double dt, const double* vel, const double* w,
                       const double* wi, const double* we, const double* ttf, const double* ttfAB, int hor,
                       int ver, int lim, double ph, double pv, int use_wsplit, double* dttf_h, double* dttf_v) {
-  (void)wi;
   const int nl = m->nl, nzl = nl - 1;
-  if (use_wsplit) return -2; /* adv_tra_vert_impl is not restated */
   if (hor < 0 || hor > 2 || ver < 0 || ver > 3 || lim < 0 || lim > 1) return -1;
+  if (use_wsplit && lim == OM_LIM_FCT) {
+    for (int n = 1; n <= m->nod2D; ++n)
+      if (m->nlevels_nod2D[n - 1] - m->ulevels_nod2D[n - 1] < 2) return -2; /* see vert_impl */
+  }
   double *LO = wk->fct_LO, *Fh = wk->adv_flux_hor, *Fv = wk->adv_flux_ver;
   if (lim == OM_LIM_FCT) {
     hor_upw1(m, vel, ttf, Fh, 1);
@@ -1316,6 +1386,12 @@ int om_do_oce_adv_tra(const omesh* m, omwork* wk, double dt, const double* vel, 
             (A2(ttf, nzl, nz, n) * A2(m->hnode, nzl, nz, n) +
              ((A2(LO, nzl, nz, n) + (A2(Fv, nl, nz, n) - A2(Fv, nl, nz + 1, n))) * dt) / A2(m->areasvol, nl, nz, n)) /
             A2(m->hnode_new, nzl, nz, n);
+    if (use_wsplit) {
+      /* implicit part with wi, then the LO vertical flux of the full w for the
+       * antidiffusive vertical flux (lib/oce_adv_tra_driver.F90:221-231) */
+      vert_impl(m, dt, wi, LO);
+      ver_upw1(m, w, ttf, Fv, 1);
+    }
   }
   int zero = (lim != OM_LIM_FCT);
   if (hor == OM_HOR_UPW1) {
@@ -1350,6 +1426,14 @@ int om_do_oce_adv_tra(const omesh* m, omwork* wk, double dt, const double* vel, 
 int om_analytic_step(const omesh* m, omwork* wk, int ntr, double dt, const double* vel, const double* w,
                      double* values, double* valuesAB, const int* hor, const int* ver, const int* lim,
                      const double* ph, const double* pv, int copy_ab, double* del_ttf) {
+  return om_analytic_step_split(m, wk, ntr, dt, vel, w, w, w, 0, values, valuesAB, hor, ver, lim, ph, pv, copy_ab,
+                                del_ttf);
+}
+
+int om_analytic_step_split(const omesh* m, omwork* wk, int ntr, double dt, const double* vel, const double* w,
+                           const double* wi, const double* we, int use_wsplit, double* values, double* valuesAB,
+                           const int* hor, const int* ver, const int* lim, const double* ph, const double* pv,
+                           int copy_ab, double* del_ttf) {
   const int nzl = m->nl - 1, N = m->nod2D;
   const size_t blk = (size_t)nzl * N;
   double* dh = (double*)xcalloc(blk, sizeof(double));
@@ -1361,7 +1445,8 @@ int om_analytic_step(const omesh* m, omwork* wk, int ntr, double dt, const doubl
     memset(del_ttf, 0, blk * sizeof(double));
     double* val = values + t * blk;
     double* vab = valuesAB + t * blk;
-    rc = om_do_oce_adv_tra(m, wk, dt, vel, w, w, w, val, vab, hor[t], ver[t], lim[t], ph[t], pv[t], 0, dh, dv);
+    rc = om_do_oce_adv_tra(m, wk, dt, vel, w, wi, we, val, vab, hor[t], ver[t], lim[t], ph[t], pv[t], use_wsplit, dh,
+                           dv);
     for (int k = 1; k <= N; ++k)
       for (int kz = m->ulevels_nod2D[k - 1]; kz <= m->nlevels_nod2D[k - 1] - 1; ++kz)
         A2(del_ttf, nzl, kz, k) = A2(del_ttf, nzl, kz, k) + A2(dh, nzl, kz, k) + A2(dv, nzl, kz, k);

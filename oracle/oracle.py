@@ -67,6 +67,10 @@ def lib():
         L.om_analytic_step.restype = ctypes.c_int
         L.om_analytic_step.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_double,
                                        _dp, _dp, _dp, _dp, _ip, _ip, _ip, _dp, _dp, ctypes.c_int, _dp]
+        L.om_analytic_step_split.restype = ctypes.c_int
+        L.om_analytic_step_split.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_double,
+                                             _dp, _dp, _dp, _dp, ctypes.c_int, _dp, _dp, _ip, _ip, _ip, _dp, _dp,
+                                             ctypes.c_int, _dp]
         L.om_cabi_step.restype = ctypes.c_int
         L.om_cabi_step.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, _dp, _dp, _dp, _dp,
                                    _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
@@ -185,21 +189,27 @@ class Work:
 
 def do_oce_adv_tra(mesh, work, dt, vel, w, ttf, ttfAB, hor="UPW1", ver="UPW1", lim="NONE",
                    ph=1.0, pv=1.0, wi=None, we=None):
-    """One call of do_oce_adv_tra; returns (dttf_h, dttf_v) as (nod2D, nl-1)."""
+    """One call of do_oce_adv_tra; returns (dttf_h, dttf_v) as (nod2D, nl-1).
+
+    wi given switches w_split on: the FCT low-order solution gets the implicit
+    vertical step with wi (adv_tra_vert_impl); we (default w) is the explicit
+    vertical velocity of the low-order flux."""
     vel, w, ttf, ttfAB = _f64(vel), _f64(w), _f64(ttf), _f64(ttfAB)
+    split = wi is not None
     wi = w if wi is None else _f64(wi)
     we = w if we is None else _f64(we)
     dh = np.zeros((mesh.nod2D, mesh.nl - 1))
     dv = np.zeros_like(dh)
     rc = lib().om_do_oce_adv_tra(mesh.h, work.h, dt, _p(vel), _p(w), _p(wi), _p(we), _p(ttf), _p(ttfAB),
-                                 HOR[hor], VER[ver], LIM[lim], ph, pv, 0, _p(dh), _p(dv))
+                                 HOR[hor], VER[ver], LIM[lim], ph, pv, int(split), _p(dh), _p(dv))
     if rc != 0:
         raise RuntimeError(f"om_do_oce_adv_tra failed: {rc}")
     return dh, dv
 
 
-def analytic_step(mesh, work, dt, vel, w, values, valuesAB, schemes, copy_ab=False):
-    """One driver step for all tracers, in place. schemes: list of (hor, ver, lim[, ph, pv])."""
+def analytic_step(mesh, work, dt, vel, w, values, valuesAB, schemes, copy_ab=False, wi=None, we=None):
+    """One driver step for all tracers, in place. schemes: list of (hor, ver, lim[, ph, pv]).
+    wi / we as for do_oce_adv_tra."""
     ntr = len(schemes)
     assert values.flags.c_contiguous and values.dtype == np.float64
     assert valuesAB.flags.c_contiguous and valuesAB.dtype == np.float64
@@ -210,9 +220,12 @@ def analytic_step(mesh, work, dt, vel, w, values, valuesAB, schemes, copy_ab=Fal
     ph = np.array([s[3] if len(s) > 3 else 1.0 for s in schemes])
     pv = np.array([s[4] if len(s) > 4 else 1.0 for s in schemes])
     del_ttf = np.zeros((mesh.nod2D, mesh.nl - 1))
-    rc = lib().om_analytic_step(mesh.h, work.h, ntr, dt, _p(vel), _p(w), _p(values), _p(valuesAB),
-                                _p(hor, _ip), _p(ver, _ip), _p(lim, _ip), _p(ph), _p(pv), int(copy_ab),
-                                _p(del_ttf))
+    split = wi is not None
+    wi = w if wi is None else _f64(wi)
+    we = w if we is None else _f64(we)
+    rc = lib().om_analytic_step_split(mesh.h, work.h, ntr, dt, _p(vel), _p(w), _p(wi), _p(we), int(split),
+                                      _p(values), _p(valuesAB), _p(hor, _ip), _p(ver, _ip), _p(lim, _ip),
+                                      _p(ph), _p(pv), int(copy_ab), _p(del_ttf))
     if rc != 0:
         raise RuntimeError(f"om_analytic_step failed: {rc}")
 

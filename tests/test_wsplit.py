@@ -1,0 +1,296 @@
+"""w_split: the implicit vertical step of the FCT low-order solution
+(adv_tra_vert_impl, lib/oce_adv_tra_ver.F90:90-244, called from
+lib/oce_adv_tra_driver.F90:221-231).
+
+The vertical velocity is split as w = we + wi: the explicit low-order flux
+uses we, the low-order solution then gets the implicit upwind step with wi
+(a tridiagonal solve per column), and the antidiffusive vertical flux takes
+the upwind flux of the full w.
+
+The reference's own tests do not exercise this option, so the oracle's
+restatement is pinned here by properties: wi = 0 reproduces the unsplit step
+bit for bit; the low-order solution after the step solves the implicit system
+built independently with numpy; a uniform tracer stays uniform for any split
+of a continuity-consistent w; the volume integral is conserved; FCT still
+creates no new extrema. The GPU forms are compared with the oracle: FP64
+bit-exact, FP32 within 1e-5 relative max-norm.
+"""
+import itertools
+import zlib
+
+import numpy as np
+import pytest
+
+SPLIT_SCHEMES = [("MUSCL", "PPM", "FCT"), ("MFCT", "QR4C", "FCT"), ("UPW1", "CDIFF", "FCT"), ("UPW1", "UPW1", "FCT")]
+
+
+def _ragged_kw(nx=14, ny=12, nl=12, seed=3):
+    from fesom2_tracer_dwarf_gb300 import synthetic
+
+    rng = np.random.default_rng(seed)
+    zb = synthetic.stretched_zbar(nl - 1, 5.0, 120.0)
+    en = synthetic.bathymetry_levels(nx, ny, zb, rng, min_layers=3)
+    return dict(nx=nx, ny=ny, nl=nl, periodic=False, zbar=zb, elem_nlev=en, orient_left=True)
+
+
+def split(w, q=0.5):
+    """w = we + wi with we clipped at the q-quantile of |w| (most wet
+    interfaces get a nonzero implicit part)."""
+    c = float(np.quantile(np.abs(w[w != 0]), q)) if np.any(w != 0) else 0.0
+    we = np.clip(w, -c, c)
+    return we, w - we
+
+
+def _wet(m):
+    nlev = m.get("nlevels_nod2D")
+    return np.arange(m.nz)[None, :] < (nlev - 1)[:, None]
+
+
+def _volume(m):
+    return m.get("areasvol")[:, : m.nz] * m.get("hnode_new") * _wet(m)
+
+
+def _steps(O, om, vel, w, T, sch, steps, dt, wi=None, we=None):
+    vals = np.ascontiguousarray(T.copy())
+    vab = vals.copy()
+    W = O.Work(om)
+    for _ in range(steps):
+        O.analytic_step(om, W, dt, vel, w, vals, vab, [sch] * vals.shape[0], copy_ab=True, wi=wi, we=we)
+    return vals
+
+
+def _pair(O, kw):
+    from fesom2_tracer_dwarf_gb300.mesh import Mesh
+
+    return O.Mesh(**kw), Mesh(**kw, upload=False)
+
+
+# ---------------------------------------------------------------------------
+# Oracle (CPU)
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("sch", SPLIT_SCHEMES)
+def test_oracle_zero_wi_is_the_unsplit_step(oracle_mod, sch):
+    from fesom2_tracer_dwarf_gb300 import synthetic
+
+    om, m = _pair(oracle_mod, _ragged_kw())
+    rng = np.random.default_rng(21)
+    vel, w = synthetic.random_flow(m, rng)
+    T = synthetic.random_field(m, rng, 2)
+    a = _steps(oracle_mod, om, vel, w, T, sch, 2, 300.0)
+    b = _steps(oracle_mod, om, vel, w, T, sch, 2, 300.0, wi=np.zeros_like(w), we=w)
+    assert np.array_equal(a, b)
+
+
+def test_oracle_lo_solves_the_implicit_system(oracle_mod):
+    """fct_LO after the split step solves A x = hnode_new * LO_explicit per
+    column, A the implicit upwind matrix of wi assembled here with numpy."""
+    from fesom2_tracer_dwarf_gb300 import synthetic
+
+    O = oracle_mod
+    om, m = _pair(O, _ragged_kw())
+    rng = np.random.default_rng(22)
+    vel, w = synthetic.random_flow(m, rng)
+    we, wi = split(w)
+    T = synthetic.random_field(m, rng, 1)[0]
+    dt = 300.0
+    W0 = O.Work(om)
+    O.do_oce_adv_tra(om, W0, dt, vel, w, T, T, "MUSCL", "PPM", "FCT", we=we)
+    lo_exp = W0.get("fct_LO")
+    W1 = O.Work(om)
+    O.do_oce_adv_tra(om, W1, dt, vel, w, T, T, "MUSCL", "PPM", "FCT", wi=wi, we=we)
+    lo_imp = W1.get("fct_LO")
+    area, av, hnn = m.get("area"), m.get("areasvol"), m.get("hnode_new")
+    nlev, ulev = m.get("nlevels_nod2D"), m.get("ulevels_nod2D")
+    worst = 0.0
+    for n in range(m.N):
+        k0, k1 = ulev[n] - 1, nlev[n] - 2
+        L = k1 - k0 + 1
+        A = np.zeros((L, L))
+        for j, k in enumerate(range(k0, k1 + 1)):
+            v0 = dt * area[n, k] / av[n, k]
+            v1 = dt * area[n, k + 1] / av[n, k]
+            wt, wb = wi[n, k], wi[n, k + 1]
+            A[j, j] = hnn[n, k] + (wt if k == k0 else max(wt, 0.0)) * v0
+            if k > k0:
+                A[j, j - 1] = min(wt, 0.0) * v0
+            if k < k1:
+                A[j, j] -= min(wb, 0.0) * v1
+                A[j, j + 1] = -max(wb, 0.0) * v1
+        rhs = hnn[n, k0:k1 + 1] * lo_exp[n, k0:k1 + 1]
+        res = A @ lo_imp[n, k0:k1 + 1] - rhs
+        worst = max(worst, float(np.abs(res).max() / np.abs(rhs).max()))
+    assert worst <= 1e-13
+    assert not np.array_equal(lo_exp, lo_imp)
+
+
+@pytest.mark.parametrize("sch", SPLIT_SCHEMES)
+def test_oracle_split_uniform_conservation_bounds(oracle_mod, sch):
+    """Continuity-consistent flow, w split in two: a uniform tracer stays
+    uniform, the volume integral is conserved, FCT keeps the initial range."""
+    from fesom2_tracer_dwarf_gb300 import synthetic
+
+    om, m = _pair(oracle_mod, _ragged_kw())
+    rng = np.random.default_rng(23)
+    vel, w = synthetic.streamfunction_flow(m, rng, 300.0, cfl=0.4, psi_wall_zero=True)
+    we, wi = split(w)
+    assert np.count_nonzero(wi) > 0.3 * np.count_nonzero(w)
+    T = np.concatenate([np.full((1, m.N, m.nz), 7.25), synthetic.random_field(m, rng, 2)])
+    wet, vol = _wet(m), _volume(m)
+    out = _steps(oracle_mod, om, vel, w, T, sch, 4, 300.0, wi=wi, we=we)
+    assert np.abs(out[0] - 7.25)[wet].max() <= 1e-12 * 7.25
+    before, after = (T * vol).sum(axis=(1, 2)), (out * vol).sum(axis=(1, 2))
+    assert np.all(np.abs(after - before) <= 1e-12 * np.abs(before))
+    for t in (1, 2):
+        lo, hi = T[t][wet].min(), T[t][wet].max()
+        assert out[t][wet].min() >= lo - 1e-12 * abs(lo) and out[t][wet].max() <= hi + 1e-12 * abs(hi)
+
+
+def test_oracle_split_ignored_without_fct(oracle_mod):
+    """Without FCT the reference never reads wi."""
+    from fesom2_tracer_dwarf_gb300 import synthetic
+
+    om, m = _pair(oracle_mod, _ragged_kw())
+    rng = np.random.default_rng(24)
+    vel, w = synthetic.random_flow(m, rng)
+    we, wi = split(w)
+    T = synthetic.random_field(m, rng, 2)
+    a = _steps(oracle_mod, om, vel, w, T, ("MUSCL", "QR4C", "NONE"), 2, 300.0, we=we)
+    b = _steps(oracle_mod, om, vel, w, T, ("MUSCL", "QR4C", "NONE"), 2, 300.0, wi=wi, we=we)
+    assert np.array_equal(a, b)
+
+
+# ---------------------------------------------------------------------------
+# GPU
+# ---------------------------------------------------------------------------
+torch = pytest.importorskip("torch")
+
+MESHES = {
+    "periodic": dict(nx=11, ny=9, nl=8, periodic=True),
+    "closed_left": dict(nx=10, ny=8, nl=9, periodic=False, orient_left=True),
+}
+
+
+def _gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA GPU")
+
+
+def _rel(a, b):
+    return float(np.max(np.abs(a - b))) / max(1.0, float(np.max(np.abs(b))))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("meshname", ["periodic", "closed_left", "ragged"])
+@pytest.mark.parametrize("hor,ver", list(itertools.product(["UPW1", "MUSCL", "MFCT"], ["UPW1", "QR4C", "CDIFF", "PPM"])))
+def test_gpu_split_step_all_schemes(oracle_mod, precision, meshname, hor, ver):
+    _gpu()
+    from fesom2_tracer_dwarf_gb300 import engine, synthetic
+
+    O = oracle_mod
+    kw = _ragged_kw(12, 10, 12) if meshname == "ragged" else MESHES[meshname]
+    om, m = _pair(O, kw)
+    rng = np.random.default_rng(zlib.crc32(f"wsplit/{meshname}/{hor}/{ver}".encode()))
+    vel, w = synthetic.random_flow(m, rng)
+    we, wi = split(w)
+    K = 4
+    T = synthetic.random_field(m, rng, K)
+    TA = T + rng.normal(0, 0.05, size=T.shape)
+    dt = 400.0
+    vals, vab = np.ascontiguousarray(T.copy()), np.ascontiguousarray(TA.copy())
+    O.analytic_step(om, O.Work(om), dt, vel, w, vals, vab, [(hor, ver, "FCT", 0.7, 0.6)] * K, wi=wi, we=we)
+    eng = engine.TracerAdvection(m, K, precision, hor, ver, "FCT", ph=0.7, pv=0.6)
+    eng.set_tracers(T, TA)
+    eng.set_velocity(vel, w, we=we, wi=wi)
+    eng.step(dt)
+    torch.cuda.synchronize()
+    got = eng.values()
+    if precision == "fp64":
+        assert np.array_equal(got, vals), f"max |diff| {np.abs(got - vals).max():.3g}"
+    else:
+        assert _rel(got, vals) <= 1e-5
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,K,V", [("fp64", 9, 1), ("fp64", 1, 1), ("fp32", 12, 4), ("fp32", 6, 2),
+                                           ("fp32", 3, 1)])
+def test_gpu_split_multistep_tracer_counts(oracle_mod, precision, K, V):
+    """More tracers than one pass of the implicit kernel stages (8), tracer
+    groups, 10 steps."""
+    _gpu()
+    from fesom2_tracer_dwarf_gb300 import engine, synthetic
+
+    O = oracle_mod
+    om, m = _pair(O, _ragged_kw(16, 12, 14, seed=K))
+    rng = np.random.default_rng(30 + K)
+    dt = 300.0
+    vel, w = synthetic.streamfunction_flow(m, rng, dt, cfl=0.4, psi_wall_zero=True)
+    we, wi = split(w, 0.3)
+    T = synthetic.random_field(m, rng, K)
+    sch = ("MUSCL", "PPM", "FCT")
+    vals = _steps(O, om, vel, w, T, sch, 10, dt, wi=wi, we=we)
+    eng = engine.TracerAdvection(m, K, precision, *sch, copy_ab=True, tracer_vec=V)
+    eng.set_tracers(T)
+    eng.set_velocity(vel, w, we=we, wi=wi)
+    eng.step(dt, 10)
+    torch.cuda.synchronize()
+    got = eng.values()
+    if precision == "fp64":
+        assert np.array_equal(got, vals)
+    else:
+        assert _rel(got, vals) <= 1e-5
+
+
+@pytest.mark.gpu
+def test_gpu_split_workspace_lo(oracle_mod):
+    """The LO stage leaves the implicit low-order solution and the
+    antidiffusive vertical flux HO(w) - LO(w) in the workspace (FP64:
+    bit-exact with the oracle's fct_LO and adf_v)."""
+    _gpu()
+    from fesom2_tracer_dwarf_gb300 import _lib, engine, synthetic
+
+    O = oracle_mod
+    om, m = _pair(O, _ragged_kw())
+    rng = np.random.default_rng(40)
+    vel, w = synthetic.random_flow(m, rng)
+    we, wi = split(w)
+    T = synthetic.random_field(m, rng, 2)
+    eng = engine.TracerAdvection(m, 2, "fp64", "MUSCL", "QR4C", "FCT")
+    eng.set_tracers(T)
+    eng.set_velocity(vel, w, we=we, wi=wi)
+    eng.step(300.0, stages=_lib.STAGE_VFLUX | _lib.STAGE_HFLUX | _lib.STAGE_LO)
+    torch.cuda.synchronize()
+    lo = eng.workspace_view("lo")[:, :, : m.nz].cpu().numpy()
+    adfv = eng.workspace_view("adfv")[:, :, : m.nl].cpu().numpy()
+    for t in range(2):
+        W = O.Work(om)
+        O.do_oce_adv_tra(om, W, 300.0, vel, w, T[t], T[t], "MUSCL", "QR4C", "FCT", wi=wi, we=we)
+        assert np.array_equal(lo[t], W.get("fct_LO"))
+        assert np.array_equal(adfv[t], W.get("adf_v_raw"))
+
+
+@pytest.mark.gpu
+def test_gpu_split_rejects_single_layer_columns():
+    """Columns of one layer: the implicit step is refused on the host, before
+    any launch (the reference's right-hand side would read above the column)."""
+    _gpu()
+    from fesom2_tracer_dwarf_gb300 import engine, synthetic
+    from fesom2_tracer_dwarf_gb300.mesh import Mesh
+
+    nx, ny, nl = 8, 8, 6
+    zb = synthetic.stretched_zbar(nl - 1, 5.0, 120.0)
+    en = np.full(2 * (nx - 1) * (ny - 1), nl, dtype=np.int32)
+    en[:12] = 2  # a patch of one-layer elements
+    m = Mesh(nx=nx, ny=ny, nl=nl, periodic=False, zbar=zb, elem_nlev=en)
+    assert (m.get("nlevels_nod2D") - m.get("ulevels_nod2D")).min() == 1
+    rng = np.random.default_rng(41)
+    vel, w = synthetic.random_flow(m, rng)
+    for precision in ("fp64", "fp32"):
+        eng = engine.TracerAdvection(m, 1, precision, "UPW1", "UPW1", "FCT")
+        eng.set_tracers(synthetic.random_field(m, rng, 1))
+        eng.set_velocity(vel, w, we=w, wi=np.zeros_like(w))
+        with pytest.raises(RuntimeError, match="two layers"):
+            eng.step(300.0)
+        eng.set_velocity(vel, w)  # w_split off: the step runs
+        eng.step(300.0)
+    torch.cuda.synchronize()
