@@ -35,6 +35,13 @@ WORKLOADS = {
     # The precision form at scale: 2048^2 x 64 doubly periodic, 4 tracers (default).
     "precision_2048": dict(kind="flat", nx=2049, L=2048e3, nz=64, K=4, hor="MUSCL", ver="PPM", lim="FCT",
                            dt=400.0, precision="fp32", compare_fp64=True, report_steps=3),
+    # The default workload with w_split: w = we + wi, we clipped at a quarter of
+    # max |w|; the LO stage adds the implicit vertical solve with wi.
+    "wsplit_2048": dict(kind="flat", nx=2049, L=2048e3, nz=64, K=4, hor="MUSCL", ver="PPM", lim="FCT",
+                        dt=400.0, precision="fp32", compare_fp64=False, wsplit=0.25),
+    # The same on a 512x512 grid (profiling case of the implicit kernel).
+    "wsplit_512": dict(kind="flat", nx=513, L=512e3, nz=64, K=4, hor="MUSCL", ver="PPM", lim="FCT", dt=400.0,
+                       precision="fp32", compare_fp64=False, wsplit=0.25),
     # Same configuration on a 512x512 grid (profiling case: a few hundred MB).
     "precision_512": dict(kind="flat", nx=513, L=512e3, nz=64, K=4, hor="MUSCL", ver="PPM", lim="FCT", dt=400.0,
                           precision="fp32", compare_fp64=False),
@@ -132,7 +139,7 @@ class ClockSampler:
 # library's kernels as written below; intermediates the kernels add (the
 # edge volume fluxes, repeated geometry reads) are not algorithmic.
 # ---------------------------------------------------------------------------
-def stage_bytes(m, K, s, ver, fct=True, copy_ab=True):
+def stage_bytes(m, K, s, ver, fct=True, copy_ab=True, wsplit=False):
     cells = m.N * m.nz  # node-layers; x K tracer-cells
     ta = 0 if copy_ab else 1
     e = 3
@@ -141,6 +148,8 @@ def stage_bytes(m, K, s, ver, fct=True, copy_ab=True):
     if fct:
         b["hflux"] = cells * s * K * (1 + ta + e)                  # T (+T_AB) -> adf_h
         b["lo"] = cells * s * (5 + qr + K * 2)                      # w, area, hnode, hnode_new, areasvol -> LO, adf_v
+        if wsplit:
+            b["lo"] += cells * s * 2                                # w_e, w_i (the implicit solve on LO in place)
         b["ratio"] = cells * s * K * (1 + 1 + e + 1 + 2)           # LO, T, adf_h, adf_v -> R+, R-
         b["update"] = cells * s * K * (e + 2 + 1 + 1 + 2)          # adf_h, R+-, adf_v, LO, T -> T
     else:
@@ -227,6 +236,11 @@ def build_case(cfg, precision, device, seed=20260301):
         m, vel, w, T0 = _flat_part(cfg["nx"] - 1, cfg["nz"], precision, device, cfg["dt"], 0.4, cfg["K"], seed)
         eng = TracerAdvection(m, cfg["K"], precision, *sch, copy_ab=True, device=device)
         eng.load_padded(T=T0, vel=vel, w=w)
+        if cfg.get("wsplit"):
+            c = float(w.abs().max()) * cfg["wsplit"]
+            we = w.clamp(-c, c)
+            eng.load_padded(we=we, wi=w - we)
+            del we
     elif cfg["kind"] == "closed":
         rng = np.random.default_rng(seed)
         zb = synthetic.stretched_zbar(cfg["nz"], 5.0, 250.0)
@@ -463,7 +477,8 @@ def run_gpu(args):
     value = cells * world / (t_max / 1e3)
     s = 4 if cfg["precision"] == "fp32" else 8
     wet_frac = m.wet_cells() / (m.N * m.nz)
-    sb = {k: v * wet_frac for k, v in stage_bytes(m, K, s, cfg["ver"], fct=cfg["lim"] == "FCT").items()}
+    sb = {k: v * wet_frac for k, v in stage_bytes(m, K, s, cfg["ver"], fct=cfg["lim"] == "FCT",
+                                                  wsplit=bool(cfg.get("wsplit"))).items()}
     peak, peak_kind = load_peaks()
     step_bytes = sum(sb.values())
     if per is None:  # graph: per-stage times of one eager step for the roofline split
@@ -491,7 +506,9 @@ def run_gpu(args):
                    "schemes": f"{cfg['hor']}/{cfg['ver']}/{cfg['lim']}", "form": cfg["precision"], "dt_s": cfg["dt"],
                    "tracer_cells_per_step": cells, "l2": "inputs larger than L2 (no flush)",
                    "parallelism": f"replicas x{world}", "cuda_graph_steps": cfg.get("graph_steps"),
-                   "launch_cfg": tuned["cfg"] if tuned else "default"},
+                   "launch_cfg": tuned["cfg"] if tuned else "default",
+                   "w_split": (f"we = w clipped at {cfg['wsplit']} max|w|, wi = w - we" if cfg.get("wsplit")
+                               else None)},
         "stage_ms": {k: round(v, 4) for k, v in per.items()},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,

@@ -15,6 +15,7 @@ HOR = {"UPW1": 0, "MUSCL": 1, "MFCT": 2}
 VER = {"UPW1": 0, "QR4C": 1, "CDIFF": 2, "PPM": 3}
 LIM = {"NONE": 0, "FCT": 1}
 FP64, FP32 = 0, 1
+NCFG = 12  # launch knobs of fgb_step_desc.cfg
 STAGE_VFLUX, STAGE_HFLUX, STAGE_LO, STAGE_RATIO, STAGE_UPDATE = 1, 2, 4, 8, 16
 STAGE_ALL = 31
 
@@ -48,7 +49,7 @@ class StepDesc(ctypes.Structure):
         ("workspace", _vp),
         ("workspace_bytes", ctypes.c_longlong),
         ("tracer_vec", ctypes.c_int),
-        ("cfg", ctypes.c_int * 8),
+        ("cfg", ctypes.c_int * NCFG),
         ("wi", _vp),
     ]
 

@@ -39,10 +39,11 @@ def chunk_candidates(K: int):
     return [c for c in CHUNKS if K % c == 0]
 
 
-def stage_candidates(stage: str, K: int, precision: str = "fp64"):
+def stage_candidates(stage: str, K: int, precision: str = "fp64", wsplit: bool = False):
     """Candidate knob values per tuned stage: a list of dicts of cfg index -> value.
     FP64: block size and tracers per chunk. FP32 (one tracer group at a time):
-    block size and layers per lane per pass."""
+    block size and layers per lane per pass, and under w_split the solver of
+    the implicit vertical step (part of the LO stage)."""
     if stage == "hflux":
         if precision == "fp32":
             return [{0: w, 7: ns} for w, ns in product(EDGE_WARPS, SLICES)]
@@ -51,7 +52,10 @@ def stage_candidates(stage: str, K: int, precision: str = "fp64"):
     if precision == "fp32":
         # the ratio kernel also has variants without shared memory (3; 4: fewer registers)
         slices = SLICES + ((3, 4) if stage == "ratio" else ())
-        return [{1 + slot: w, 4 + slot: ns} for w, ns in product(NODE_WARPS, slices)]
+        cands = [{1 + slot: w, 4 + slot: ns} for w, ns in product(NODE_WARPS, slices)]
+        if stage == "lo" and wsplit:
+            cands = [{**c, 8: solver} for c in cands for solver in (0, 1)]
+        return cands
     return [{1 + slot: w, 4 + slot: c} for w, c in product(NODE_WARPS, chunk_candidates(K))]
 
 
@@ -61,7 +65,7 @@ def cache_key(engine) -> str:
     m = engine.mesh
     dev = torch.cuda.get_device_name(engine.device)
     return "|".join(str(x) for x in (dev, engine.precision, engine.K, engine.V, engine.hor, engine.ver, engine.lim,
-                                     m.N, m.E, m.nz))
+                                     m.N, m.E, m.nz, "wsplit" if engine.wi is not None else "w"))
 
 
 def _load_file(path):
@@ -99,7 +103,7 @@ def _time_stage(engine, mask, dt, reps):
 def tune(engine, dt: float = 1.0, reps: int = 5, cache_path: str | None = None, force: bool = False):
     """Pick the fastest launch configuration for ``engine`` and apply it.
 
-    Returns {"cfg": [8 ints], "ms": {stage: best ms}, "cached": bool}.
+    Returns {"cfg": [12 ints], "ms": {stage: best ms}, "cached": bool}.
     """
     import torch
 
@@ -117,13 +121,13 @@ def tune(engine, dt: float = 1.0, reps: int = 5, cache_path: str | None = None, 
     stages = [("hflux", _lib.STAGE_HFLUX)]
     stages += [("lo", _lib.STAGE_LO), ("ratio", _lib.STAGE_RATIO)] if fct else []
     stages += [("update", _lib.STAGE_UPDATE)]
-    cfg = [0] * 8
+    cfg = [0] * _lib.NCFG
     engine.set_launch(cfg)
     engine.step(dt, 1)  # fills every workspace array the stages read
     best_ms = {}
     for name, mask in stages:
         best = None
-        for cand in stage_candidates(name, engine.K, engine.precision):
+        for cand in stage_candidates(name, engine.K, engine.precision, engine.wi is not None):
             trial = list(cfg)
             for i, v in cand.items():
                 trial[i] = v

@@ -101,10 +101,28 @@ struct FastPtrs {
   float dt, ph, pv;
 };
 
+// Shared-memory shape of the w_split kernel (kf_vert_impl): a warp holds
+// 32 / KV node columns, one lane per (node, tracer of the group).
+template <int KV>
+struct VimplShape {
+  static constexpr int NPW = 32 / KV;  // node columns per warp
+  static constexpr int CS = NPW + 1;   // row stride of the per-node arrays (odd: conflict-free)
+  static constexpr int RS = 32 + KV;   // row stride of the per-lane array (conflict-free V<KV> rows)
+  // floats of one warp: the per-lane array, then a, b, c and the cp ratios
+  __host__ __device__ static constexpr size_t warp_floats(int LZ) { return (size_t)LZ * (RS + 4 * CS); }
+};
+constexpr int kVimplWarpsF = 4;  // warps per block
+inline size_t vimpl_block_bytes(int LZ, int KV) {
+  const size_t w = KV == 4 ? VimplShape<4>::warp_floats(LZ)
+                           : (KV == 2 ? VimplShape<2>::warp_floats(LZ) : VimplShape<1>::warp_floats(LZ));
+  return kVimplWarpsF * w * sizeof(float);
+}
+
 // Launch shape of one FP32 call.
 struct LaunchArgs {
   int mask, edge_warps, nw_lo, nw_ratio, nw_upd, hor, ver, fct;
   int ns_h, ns_lo, ns_ratio, ns_upd;  // layers per lane per pass (1 or 2)
+  int vimpl_thomas;  // w_split: lane-per-column Thomas sweeps also for columns of <= 64 layers
 };
 }  // namespace fast
 

@@ -1306,5 +1306,215 @@ __global__ void __launch_bounds__(128, 8) kf_nofct(DMesh m, FastPtrs a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// w_split: implicit vertical advection of the low-order solution with wi
+// (adv_tra_vert_impl, lib/oce_adv_tra_ver.F90:90-244), in place, between the
+// LO and ratio kernels. Per column the system A y = hnode_new * LO over the
+// layers nzmin..nzmax-1 is solved for the new values y directly (the
+// reference solves A x = -(A - diag(hnode_new)) LO for the increment x = y - LO;
+// the two agree to rounding).
+//
+// One lane per (node, tracer of the group): a warp holds 32 / KV node
+// columns, so the serial Thomas sweeps run on all 32 lanes. The coefficients
+// (per node) and the right-hand sides (per lane) are formed layer-parallel
+// and staged in shared memory, transposed so that the sweeps read one row of
+// consecutive words per layer; the KV lanes of a node repeat the
+// tracer-independent pivots in parallel.
+// ---------------------------------------------------------------------------
+template <int KV>
+__global__ void __launch_bounds__(kVimplWarpsF * kW) kf_vert_impl(DMesh m, FastPtrs a) {
+  using S = VimplShape<KV>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
+  const int n0 = (blockIdx.x * kVimplWarpsF + wib) * S::NPW;
+  if (n0 >= m.N) return;
+  const int LZ = m.LZ, LW = m.LW;
+  const int nn = m.N - n0 < S::NPW ? m.N - n0 : S::NPW;  // columns of this warp
+  float* sY = reinterpret_cast<float*>(smem_raw) + (size_t)wib * S::warp_floats(LZ);  // (LZ, RS)
+  float* sA = sY + (size_t)LZ * S::RS;                                                // (LZ, CS) each
+  float* sB = sA + (size_t)LZ * S::CS;
+  float* sC = sB + (size_t)LZ * S::CS;
+  float* sCP = sC + (size_t)LZ * S::CS;
+  const GeoPtrs<float>& g = m.g32;
+  const float dt = a.dt;
+  // Tridiagonal coefficients per node and layer (lib/oce_adv_tra_ver.F90:
+  // 158-190). Every row is loaded and stored (rows outside a column are
+  // never read), so the loads of several iterations are in flight together.
+#pragma unroll 8
+  for (int i = lane; i < nn * LZ; i += kW) {
+    const int j = i / LZ, k = i - j * LZ, n = n0 + j;
+    const int k0 = m.ulev[n] - 1, k1 = m.nlev[n] - 2;
+    const unsigned iw = (unsigned)n * LW + k, iz = (unsigned)n * LZ + k;
+    const unsigned iw1 = iw + (k + 1 < LW ? 1u : 0u);
+    const float W0 = a.wi[iw], W1 = a.wi[iw1], ar0 = g.area[iw], ar1 = g.area[iw1];
+    const float rav = fdv(dt, g.areasvol[iz]), hnn = g.hnode_new[iz];
+    const float v0 = ar0 * rav, v1 = ar1 * rav;
+    const float ak = k == k0 ? 0.f : fminf(W0, 0.f) * v0;
+    float bk = hnn + (k == k0 ? W0 : fmaxf(W0, 0.f)) * v0, ck = 0.f;
+    if (k != k1) {
+      bk -= fminf(W1, 0.f) * v1;
+      ck = -fmaxf(W1, 0.f) * v1;
+    }
+    sA[k * S::CS + j] = ak;
+    sB[k * S::CS + j] = bk;
+    sC[k * S::CS + j] = ck;
+  }
+  const int j = lane / KV;
+  const bool own = j < nn;
+  const int k0 = own ? m.ulev[n0 + j] - 1 : 0, k1 = own ? m.nlev[n0 + j] - 2 : -1;
+  for (int gi = 0; gi < a.G; ++gi) {
+    float* __restrict__ lo = a.lo + gi * a.gN;
+    __syncwarp();
+    // right-hand sides hnode_new * LO, rows of consecutive node-layers
+#pragma unroll 8
+    for (int i = lane; i < nn * LZ; i += kW) {
+      const int jj = i / LZ, k = i - jj * LZ;
+      const unsigned iz = (unsigned)(n0 + jj) * LZ + k;
+      *reinterpret_cast<V<KV>*>(sY + k * S::RS + jj * KV) = muls(ld<KV>(lo, iz), g.hnode_new[iz]);
+    }
+    __syncwarp();
+    if (own) {
+      // forward sweep: pivots m = b - cp * a, cp = c / m, tp = (d - tp * a) / m
+      float cp = 0.f, tp = 0.f;
+#pragma unroll 4
+      for (int k = k0; k <= k1; ++k) {
+        const float ak = sA[k * S::CS + j];
+        const float rm = fdv(1.f, sB[k * S::CS + j] - cp * ak);
+        cp = sC[k * S::CS + j] * rm;
+        tp = (sY[k * S::RS + lane] - tp * ak) * rm;
+        sY[k * S::RS + lane] = tp;
+        if (lane % KV == 0) sCP[k * S::CS + j] = cp;
+      }
+    }
+    __syncwarp();
+    if (own) {
+      // back substitution: y = tp - cp * y(below)
+      float y = sY[k1 * S::RS + lane];
+#pragma unroll 4
+      for (int k = k1 - 1; k >= k0; --k) {
+        y = sY[k * S::RS + lane] - sCP[k * S::CS + j] * y;
+        sY[k * S::RS + lane] = y;
+      }
+    }
+    __syncwarp();
+#pragma unroll 4
+    for (int i = lane; i < nn * LZ; i += kW) {
+      const int jj = i / LZ, k = i - jj * LZ, n = n0 + jj;
+      if (k >= m.ulev[n] - 1 && k <= m.nlev[n] - 2)
+        st<KV>(lo, (unsigned)n * LZ + k, *reinterpret_cast<const V<KV>*>(sY + k * S::RS + jj * KV));
+    }
+  }
+}
+
+// The same solve for columns of at most 64 layers: one warp per node, rows
+// k = lane and lane + 32 in registers, parallel cyclic reduction (six steps
+// coupling rows 1, 2, 4, ..., 32 apart; stable for these diagonally dominant
+// systems). No shared memory, all 32 lanes busy. Each row carries its scaled
+// couplings A = a / b, C = c / b and D = d / b; a step with distance h forms
+//   a' = -a A(k-h), c' = -c C(k+h), b' = b - a C(k-h) - c A(k+h),
+//   d' = d - a D(k-h) - c D(k+h),
+// rows outside the column being identity rows (a = c = d = 0, b = 1); after
+// the last step D is the solution.
+template <int KV>
+struct PcrRow {
+  float A, C;
+  V<KV> D;
+};
+
+template <int KV>
+__device__ __forceinline__ PcrRow<KV> pcr_shfl(const PcrRow<KV>& r, int src) {
+  return PcrRow<KV>{__shfl_sync(0xffffffffu, r.A, src), __shfl_sync(0xffffffffu, r.C, src), shfl_v<KV>(r.D, src)};
+}
+
+template <int KV>
+__device__ __forceinline__ void pcr_update(float& a, float& b, float& c, V<KV>& d, PcrRow<KV>& row, bool hm,
+                                           const PcrRow<KV>& m, bool hp, const PcrRow<KV>& p) {
+  const float Am = hm ? m.A : 0.f, Cm = hm ? m.C : 0.f, Ap = hp ? p.A : 0.f, Cp = hp ? p.C : 0.f;
+  const float na = -a, nc = -c;
+  b = fmaf(nc, Ap, fmaf(na, Cm, b));
+  V<KV> dd = d;
+  if (hm) dd = fmas(m.D, na, dd);
+  if (hp) dd = fmas(p.D, nc, dd);
+  d = dd;
+  a = na * Am;
+  c = nc * Cp;
+  const float rb = fdv(1.f, b);
+  row.A = a * rb;
+  row.C = c * rb;
+  row.D = muls(d, rb);
+}
+
+template <int KV>
+__global__ void __launch_bounds__(256) kf_vert_pcr(DMesh m, FastPtrs a) {
+  const int lane = threadIdx.x & (kW - 1);
+  const int n = blockIdx.x * (blockDim.x / kW) + threadIdx.x / kW;
+  if (n >= m.N) return;
+  const unsigned LZ = m.LZ, LW = m.LW;
+  const int k0 = m.ulev[n] - 1, k1 = m.nlev[n] - 2;
+  const GeoPtrs<float>& g = m.g32;
+  const float dt = a.dt;
+  // coefficients of rows lane and lane + 32 (lib/oce_adv_tra_ver.F90:158-190)
+  float a0[2], b0[2], c0[2], hn[2];
+  bool act[2];
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const int k = lane + kW * r;
+    act[r] = k >= k0 && k <= k1;
+    const int kk = act[r] ? k : k0;
+    const unsigned iw = (unsigned)n * LW + kk, iz = (unsigned)n * LZ + kk;
+    const unsigned iw1 = iw + (kk < k1 ? 1u : 0u);
+    const float W0 = a.wi[iw], W1 = a.wi[iw1], ar0 = g.area[iw], ar1 = g.area[iw1];
+    const float rav = fdv(dt, g.areasvol[iz]), hnn = g.hnode_new[iz];
+    const float v0 = ar0 * rav, v1 = ar1 * rav;
+    float ak = kk == k0 ? 0.f : fminf(W0, 0.f) * v0;
+    float bk = hnn + (kk == k0 ? W0 : fmaxf(W0, 0.f)) * v0, ck = 0.f;
+    if (kk != k1) {
+      bk -= fminf(W1, 0.f) * v1;
+      ck = -fmaxf(W1, 0.f) * v1;
+    }
+    a0[r] = act[r] ? ak : 0.f;
+    b0[r] = act[r] ? bk : 1.f;
+    c0[r] = act[r] ? ck : 0.f;
+    hn[r] = act[r] ? hnn : 0.f;
+  }
+  for (int gi = 0; gi < a.G; ++gi) {
+    float* __restrict__ lo = a.lo + gi * a.gN;
+    float av[2], bv[2], cv[2];
+    V<KV> dv[2];
+    PcrRow<KV> row[2];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const unsigned k = lane + kW * r;
+      dv[r] = act[r] ? muls(ld<KV>(lo, (unsigned)n * LZ + k), hn[r]) : splat<KV>(0.f);
+      av[r] = a0[r];
+      bv[r] = b0[r];
+      cv[r] = c0[r];
+      const float rb = fdv(1.f, bv[r]);
+      row[r] = PcrRow<KV>{av[r] * rb, cv[r] * rb, muls(dv[r], rb)};
+    }
+#pragma unroll
+    for (int h = 1; h < kW; h *= 2) {
+      const int sm = (lane - h) & (kW - 1), sp = (lane + h) & (kW - 1);
+      const PcrRow<KV> m0 = pcr_shfl(row[0], sm), m1 = pcr_shfl(row[1], sm);
+      const PcrRow<KV> p0 = pcr_shfl(row[0], sp), p1 = pcr_shfl(row[1], sp);
+      const bool lo_in = lane >= h, hi_in = lane + h < kW;
+      // row lane: k - h from lane - h (row 0) if lane >= h; k + h from lane + h
+      // (row 0) or, past 31, from lane + h - 32 (row 1)
+      pcr_update(av[0], bv[0], cv[0], dv[0], row[0], lo_in, m0, true, hi_in ? p0 : p1);
+      // row lane + 32: k - h from lane - h (row 1) or lane - h + 32 (row 0);
+      // k + h from lane + h (row 1) while below 64
+      pcr_update(av[1], bv[1], cv[1], dv[1], row[1], true, lo_in ? m1 : m0, hi_in, p1);
+    }
+    {  // h = 32: the two rows of a lane couple to each other
+      const PcrRow<KV> r0 = row[0], r1 = row[1];
+      pcr_update(av[0], bv[0], cv[0], dv[0], row[0], false, r0, true, r1);
+      pcr_update(av[1], bv[1], cv[1], dv[1], row[1], true, r0, false, r1);
+    }
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+      if (act[r]) st<KV>(lo, (unsigned)n * LZ + lane + kW * r, row[r].D);
+  }
+}
+
 }  // namespace fast
 }  // namespace fgb

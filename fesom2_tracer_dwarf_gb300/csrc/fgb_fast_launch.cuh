@@ -103,6 +103,18 @@ int launch_fast(const DMesh& m, const FastPtrs& a, const LaunchArgs& L, cudaStre
         default: launch_lo_ns<KV, 0>(m, a, L, s); break;
       }
       ++launches;
+      if (a.wi) {
+        // w_split: the implicit vertical step on the LO solution
+        if (m.LZ <= 2 * kW && !L.vimpl_thomas) {
+          kf_vert_pcr<KV><<<(m.N + 7) / 8, 8 * kW, 0, s>>>(m, a);
+        } else {
+          const size_t sm = vimpl_block_bytes(m.LZ, KV);
+          allow_smem_f(kf_vert_impl<KV>, sm);
+          const int per_block = kVimplWarpsF * VimplShape<KV>::NPW;
+          kf_vert_impl<KV><<<(m.N + per_block - 1) / per_block, kVimplWarpsF * kW, sm, s>>>(m, a);
+        }
+        ++launches;
+      }
     }
     if (L.mask & FGB_STAGE_RATIO) {
       if (m.LZ <= 2 * kW && (L.ns_ratio == 0 || L.ns_ratio >= 3)) {

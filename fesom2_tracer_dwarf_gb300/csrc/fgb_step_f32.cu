@@ -3,7 +3,6 @@
 #include <cstdint>
 
 #include "fgb_internal.hpp"
-#include "fgb_vimpl.cuh"
 
 namespace fgb {
 namespace fast {
@@ -54,7 +53,8 @@ int launch_stages_f32(const DMesh& m, const fgb_step_desc& d, int mask, cudaStre
   }
   const bool wsplit = d.lim == FGB_LIM_FCT && d.wi;
   if (wsplit) {
-    if (const char* why = vert_impl_check<float>(m)) { *err = why; return -1; }
+    if (m.min_layers < 2) { *err = "w_split needs at least two layers in every column"; return -1; }
+    if (vimpl_block_bytes(m.LZ, KV) > 227 * 1024) { *err = "w_split: too many layers for one block"; return -1; }
     if (reinterpret_cast<uintptr_t>(d.wi) % 4 != 0) { *err = "wi must be 4-byte aligned"; return -1; }
   }
   char* ws = static_cast<char*>(d.workspace);
@@ -95,26 +95,14 @@ int launch_stages_f32(const DMesh& m, const fgb_step_desc& d, int mask, cudaStre
   // the whole column per warp without shared memory
   L.ns_ratio = (d.cfg[5] >= 1 && d.cfg[5] <= 4) ? d.cfg[5] : 0;
   L.ns_upd = ns(d.cfg[6], 1);
+  L.vimpl_thomas = d.cfg[8] == 1;
   L.hor = d.hor;
   L.ver = d.ver;
   L.fct = d.lim == FGB_LIM_FCT;
-  auto run = [&](int stage_mask) {
-    LaunchArgs Ls = L;
-    Ls.mask = stage_mask;
-    if (KV == 4) return launch_fast_kv4(m, a, Ls, s);
-    if (KV == 2) return launch_fast_kv2(m, a, Ls, s);
-    return launch_fast_kv1(m, a, Ls, s);
-  };
   int n = 0;
-  if (wsplit && (mask & FGB_STAGE_LO)) {
-    // the implicit vertical step on the LO solution, between the LO and ratio kernels
-    n += run(mask & (FGB_STAGE_VFLUX | FGB_STAGE_HFLUX | FGB_STAGE_LO));
-    launch_vert_impl<float>(m, m.g32, a.lo, a.wi, K, KV, a.gN, a.dt, s);
-    ++n;
-    n += run(mask & (FGB_STAGE_RATIO | FGB_STAGE_UPDATE));
-  } else {
-    n = run(mask);
-  }
+  if (KV == 4) n = launch_fast_kv4(m, a, L, s);
+  else if (KV == 2) n = launch_fast_kv2(m, a, L, s);
+  else n = launch_fast_kv1(m, a, L, s);
   *nlaunch = n;
   cudaError_t ce = cudaGetLastError();
   if (ce != cudaSuccess) {

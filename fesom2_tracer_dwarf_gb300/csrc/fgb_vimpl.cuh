@@ -5,12 +5,13 @@
 // velocity wi is a tridiagonal system over the layers nzmin..nzmax-1, solved
 // by the Thomas algorithm in the reference's operation order.
 //
-// One warp per node. Lanes build the coefficients and right-hand sides layer
-// by layer in parallel; the pivots m = b - cp*a and the ratios cp = c/m do not
-// depend on the tracer and are formed once per node by lane 0; then lane i
-// runs the forward and backward sweeps of staged tracer i. Included by the
-// FP64 translation unit (built with -fmad=false: bit-identical to the
-// reference's arithmetic) and by the FP32 one.
+// FP64 form (built with -fmad=false: bit-identical to the reference's
+// arithmetic, including the solve for the increment). One warp per node.
+// Lanes build the coefficients and right-hand sides layer by layer in
+// parallel; the pivots m = b - cp*a and the ratios cp = c/m do not depend on
+// the tracer and are formed once per node by lane 0; then lane i runs the
+// forward and backward sweeps of staged tracer i. (The FP32 form has its own
+// kernel with one lane per node column, kf_vert_impl.)
 #pragma once
 #include <cuda_runtime.h>
 

@@ -68,19 +68,19 @@ class TracerAdvection:
                                           device=self.device)
         self._stats_out = torch.zeros(self.K, 4, dtype=torch.float64, device=self.device)
         self.launches = 0
-        self.cfg = [0] * 8  # launch configuration, see set_launch
+        self.cfg = [0] * _lib.NCFG  # launch configuration, see set_launch
 
     def set_launch(self, cfg):
-        """Launch configuration (fgb_step_desc.cfg): a list of up to 8 ints or a
+        """Launch configuration (fgb_step_desc.cfg): a list of up to 12 ints or a
         dict with keys edge_warps, node_warps (lo, ratio, update), chunk (lo,
         ratio, update). Zeros pick the library defaults; results do not depend on it."""
         if isinstance(cfg, dict):
             nw = list(cfg.get("node_warps", (0, 0, 0)))
             kc = list(cfg.get("chunk", (0, 0, 0)))
             cfg = [int(cfg.get("edge_warps", 0)), *nw, *kc, 0]
-        cfg = [int(c) for c in cfg] + [0] * (8 - len(cfg))
-        if len(cfg) != 8:
-            raise ValueError("a launch configuration has 8 entries")
+        cfg = [int(c) for c in cfg] + [0] * (_lib.NCFG - len(cfg))
+        if len(cfg) != _lib.NCFG:
+            raise ValueError(f"a launch configuration has at most {_lib.NCFG} entries")
         self.cfg = cfg
 
     # ---- layout ------------------------------------------------------------

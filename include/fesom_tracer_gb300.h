@@ -204,8 +204,12 @@ typedef struct {
    *            memory (defaults: LO 2, update 1), or for the ratio kernel
    *            3 (its default) / 4 without shared memory, 4 with fewer
    *            registers (columns of at most 64 layers).
-   * cfg[7]     FP32 form: layers per lane per pass of the edge-flux kernel, 1 or 2 */
-  int cfg[8];
+   * cfg[7]     FP32 form: layers per lane per pass of the edge-flux kernel, 1 or 2
+   * cfg[8]     FP32 form, w_split: 0 parallel cyclic reduction, one warp per
+   *            column (columns of at most 64 layers; deeper ones always use
+   *            the other solver), 1 Thomas sweeps, one lane per column
+   * cfg[9..11] unused, 0 */
+  int cfg[12];
   /* w_split (dynamics%use_wsplit, lib/oce_adv_tra_driver.F90:221-231): NULL
    * for off, else the implicit vertical velocity wi (N,LW). Under FCT the
    * low-order solution then gets the implicit vertical step with wi

@@ -294,3 +294,74 @@ def test_gpu_split_rejects_single_layer_columns():
         eng.set_velocity(vel, w)  # w_split off: the step runs
         eng.step(300.0)
     torch.cuda.synchronize()
+
+
+def _scale_wi(m, w, we, wi, dt, cfl):
+    """Rescale the implicit part so that max |wi| dt / (layer thickness) = cfl;
+    returns the new (w, we, wi)."""
+    h = m.get("hnode")
+    hmin = np.minimum(np.concatenate([h[:, :1], h], axis=1), np.concatenate([h, h[:, -1:]], axis=1))
+    c = float(np.max(np.abs(wi) * dt / hmin))
+    wi = wi * (cfl / c)
+    return we + wi, we, wi
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("solver", [0, 1])
+@pytest.mark.parametrize("cfl", [0.5, 20.0])
+def test_gpu_fp32_split_solvers_and_strong_implicit(oracle_mod, solver, cfl):
+    """Both FP32 solvers of the implicit step (cfg[8]: 0 cyclic reduction, 1
+    Thomas sweeps) at a moderate and a strongly implicit vertical Courant
+    number (max |wi| dt / h)."""
+    _gpu()
+    from fesom2_tracer_dwarf_gb300 import engine, synthetic
+
+    O = oracle_mod
+    om, m = _pair(O, _ragged_kw(14, 12, 18, seed=5))
+    rng = np.random.default_rng(50)
+    dt = 300.0
+    vel, w = synthetic.random_flow(m, rng)
+    we, wi = split(w)
+    w, we, wi = _scale_wi(m, w, we, wi, dt, cfl)
+    K = 4
+    T = synthetic.random_field(m, rng, K)
+    sch = ("MUSCL", "PPM", "FCT")
+    vals = _steps(O, om, vel, w, T, sch, 3, dt, wi=wi, we=we)
+    eng = engine.TracerAdvection(m, K, "fp32", *sch, copy_ab=True)
+    eng.set_launch([0] * 8 + [solver])
+    eng.set_tracers(T)
+    eng.set_velocity(vel, w, we=we, wi=wi)
+    eng.step(dt, 3)
+    torch.cuda.synchronize()
+    assert _rel(eng.values(), vals) <= 1e-5
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,V", [("fp64", 1), ("fp32", 4), ("fp32", 1)])
+def test_gpu_split_deep_columns(oracle_mod, precision, V):
+    """Columns of more than 64 layers (the FP32 form then always takes the
+    Thomas solver)."""
+    _gpu()
+    from fesom2_tracer_dwarf_gb300 import engine, synthetic
+
+    O = oracle_mod
+    om, m = _pair(O, _ragged_kw(10, 8, 80, seed=9))
+    assert m.LZ > 64
+    rng = np.random.default_rng(51)
+    dt = 300.0
+    vel, w = synthetic.random_flow(m, rng)
+    we, wi = split(w)
+    K = 4
+    T = synthetic.random_field(m, rng, K)
+    sch = ("MFCT", "QR4C", "FCT")
+    vals = _steps(O, om, vel, w, T, sch, 2, dt, wi=wi, we=we)
+    eng = engine.TracerAdvection(m, K, precision, *sch, copy_ab=True, tracer_vec=V)
+    eng.set_tracers(T)
+    eng.set_velocity(vel, w, we=we, wi=wi)
+    eng.step(dt, 2)
+    torch.cuda.synchronize()
+    got = eng.values()
+    if precision == "fp64":
+        assert np.array_equal(got, vals)
+    else:
+        assert _rel(got, vals) <= 1e-5
