@@ -51,6 +51,8 @@ class StepDesc(ctypes.Structure):
         ("tracer_vec", ctypes.c_int),
         ("cfg", ctypes.c_int * NCFG),
         ("wi", _vp),
+        ("ab_order", ctypes.c_int),
+        ("ab_eps", ctypes.c_double),
     ]
 
 

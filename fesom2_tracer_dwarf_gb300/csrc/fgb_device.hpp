@@ -77,6 +77,8 @@ struct StepPtrs {
   long long sT, sTA, sE, sN, sW;  // strides between tracers (elements)
   int K;            // tracers in this launch
   R dt, ph, pv;
+  int ab2;          // TAout = ab_old * T_old + ab_new * T_new (else T_new)
+  R ab_old, ab_new;
 };
 
 namespace fast {
@@ -99,6 +101,8 @@ struct FastPtrs {
   long long gT, gTA, gE, gN, gW;  // group strides (floats)
   int G;
   float dt, ph, pv;
+  int ab2;  // TAout = ab_old * T_old + ab_new * T_new (else T_new)
+  float ab_old, ab_new;
 };
 
 // Shared-memory shape of the w_split kernel (kf_vert_impl): a warp holds

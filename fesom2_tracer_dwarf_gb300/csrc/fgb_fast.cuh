@@ -1101,7 +1101,7 @@ __device__ __forceinline__ void finish_node(const DMesh& m, const FastPtrs& a, i
   }
   st<KV>(T, n * LZ + k, tnew);
   if (del) st<KV>(del, n * LZ + k, enew);
-  if (a.TAout) st<KV>(a.TAout + gi * a.gTA, n * LZ + k, tnew);
+  if (a.TAout) st<KV>(a.TAout + gi * a.gTA, n * LZ + k, a.ab2 ? fmas(Tn, a.ab_old, muls(tnew, a.ab_new)) : tnew);
 }
 
 // The kernel is written so that each node needs few dependent rounds of
@@ -1224,7 +1224,8 @@ __global__ void __launch_bounds__(128, (NS == 1 ? 9 : 4)) kf_update(DMesh m, Fas
         }
         st<KV>(Tg, n * LZ + k, tnew);
         if (DEL) st<KV>(del, n * LZ + k, enew);
-        if (a.TAout) st<KV>(a.TAout + gi * a.gTA, n * LZ + k, tnew);
+        if (a.TAout)
+          st<KV>(a.TAout + gi * a.gTA, n * LZ + k, a.ab2 ? fmas(Tn[i], a.ab_old, muls(tnew, a.ab_new)) : tnew);
       }
     }
     __syncwarp();

@@ -918,7 +918,11 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_fct_update(DM
         const R n0 = w0 ? Tn.x + fdiv(e0, hnn.x) : Tn.x, n1v = w1 ? Tn.y + fdiv(e1, hnn.y) : Tn.y;
         st2(T, n0, n1v);
         if (del) st2(del, w0 ? e0 : d0.x, w1 ? e1 : d0.y);
-        if (a.TAout) st2(a.TAout + (t0 + i) * a.sTA + n * LZ + k0, n0, n1v);
+        if (a.TAout) {
+          R* ta = a.TAout + (t0 + i) * a.sTA + n * LZ + k0;
+          if (a.ab2) st2(ta, a.ab_old * Tn.x + a.ab_new * n0, a.ab_old * Tn.y + a.ab_new * n1v);
+          else st2(ta, n0, n1v);
+        }
       }
     }
     __syncwarp();
@@ -1002,7 +1006,11 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_nofct_update(
         const R n0 = w0 ? Tn.x + fdiv(e0, hnn.x) : Tn.x, n1v = w1 ? Tn.y + fdiv(e1, hnn.y) : Tn.y;
         st2(T, n0, n1v);
         if (del) st2(del, w0 ? e0 : d0.x, w1 ? e1 : d0.y);
-        if (a.TAout) st2(a.TAout + (t0 + i) * a.sTA + n * LZ + k0, n0, n1v);
+        if (a.TAout) {
+          R* ta = a.TAout + (t0 + i) * a.sTA + n * LZ + k0;
+          if (a.ab2) st2(ta, a.ab_old * Tn.x + a.ab_new * n0, a.ab_old * Tn.y + a.ab_new * n1v);
+          else st2(ta, n0, n1v);
+        }
       }
     }
     __syncwarp();

@@ -100,6 +100,7 @@ int launch_stages(const DMesh& m, const fgb_step_desc& d, int mask, cudaStream_t
     return -1;
   }
   if (!d.T || !d.vel || !d.w || !d.we || !d.workspace) { *err = "null device pointer"; return -1; }
+  if (d.ab_order < 0 || d.ab_order > 2) { *err = "ab_order must be 0, 1 or 2"; return -1; }
   const WorkspaceLayout wl = workspace_layout<R>(m, K);
   if (d.workspace_bytes < wl.total) { *err = "workspace too small"; return -1; }
   if ((d.ver == FGB_VER_QR4C || d.ver == FGB_VER_PPM) && m.min_layers < 2) {
@@ -135,6 +136,9 @@ int launch_stages(const DMesh& m, const fgb_step_desc& d, int mask, cudaStream_t
   a.ph = (R)d.ph;
   a.pv = (R)d.pv;
   a.K = K;
+  a.ab2 = d.ab_order == 2;
+  a.ab_old = (R)(-(0.5 + d.ab_eps));
+  a.ab_new = (R)(1.5 + d.ab_eps);
   auto pick_w = [](int want, int a, int b, int c, int def) {
     return (want == a || want == b || want == c) ? want : def;
   };

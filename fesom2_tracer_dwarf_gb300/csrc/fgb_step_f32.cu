@@ -27,6 +27,7 @@ int launch_stages_f32(const DMesh& m, const fgb_step_desc& d, int mask, cudaStre
     return -1;
   }
   if (!d.T || !d.vel || !d.w || !d.we || !d.workspace) { *err = "null device pointer"; return -1; }
+  if (d.ab_order < 0 || d.ab_order > 2) { *err = "ab_order must be 0, 1 or 2"; return -1; }
   const WorkspaceLayout wl = workspace_layout<float>(m, K);
   if (d.workspace_bytes < wl.total) { *err = "workspace too small"; return -1; }
   if ((d.ver == FGB_VER_QR4C || d.ver == FGB_VER_PPM) && m.min_layers < 2) {
@@ -81,6 +82,9 @@ int launch_stages_f32(const DMesh& m, const fgb_step_desc& d, int mask, cudaStre
   a.dt = (float)d.dt;
   a.ph = (float)d.ph;
   a.pv = (float)d.pv;
+  a.ab2 = d.ab_order == 2;
+  a.ab_old = (float)(-(0.5 + d.ab_eps));
+  a.ab_new = (float)(1.5 + d.ab_eps);
   auto pick = [](int want, int x, int y, int z, int def) { return (want == x || want == y || want == z) ? want : def; };
   LaunchArgs L;
   L.mask = mask;

@@ -11,7 +11,10 @@ form; the FP32 form groups V = 4 (or 2) tracers per node-layer, a
 
 valuesAB (the field the high-order fluxes read) is either frozen at the
 values given to ``set_tracers`` -- the analytic dwarf, src/fesom_analytic.F90:335
--- or follows the values (``copy_ab=True``).
+-- or follows the values (``copy_ab=True``), or (``ab2_eps=eps``) is the
+second-order Adams-Bashforth level -(0.5+eps) T_old + (1.5+eps) T_new that the
+update stage writes for the next step (FESOM2's tracer AB2 with offset
+epsilon; the reference declares epsilon = 0.1 at lib/oce_modules.F90:75).
 """
 from __future__ import annotations
 
@@ -35,8 +38,11 @@ def _require_cuda():
 class TracerAdvection:
     def __init__(self, mesh: Mesh, ntracers: int, precision: str = "fp64", hor: str = "UPW1",
                  ver: str = "UPW1", lim: str = "NONE", ph: float = 1.0, pv: float = 1.0,
-                 copy_ab: bool = False, device: str = "cuda", tracer_vec: int | None = None):
+                 copy_ab: bool = False, device: str = "cuda", tracer_vec: int | None = None,
+                 ab2_eps: float | None = None):
         _require_cuda()
+        if ab2_eps is not None and copy_ab:
+            raise ValueError("copy_ab and ab2_eps are two choices of the valuesAB time level; give one")
         if precision not in _DT:
             raise ValueError(f"precision must be one of {list(_DT)}")
         self.mesh, self.K, self.precision = mesh, int(ntracers), precision
@@ -50,6 +56,7 @@ class TracerAdvection:
         self.device = torch.device(device)
         self.set_schemes(hor, ver, lim, ph, pv)
         self.copy_ab = copy_ab
+        self.ab2_eps = None if ab2_eps is None else float(ab2_eps)
         m = mesh
         m.upload()
         z = lambda *s: torch.zeros(*s, dtype=self.dtype, device=self.device)
@@ -174,6 +181,10 @@ class TracerAdvection:
         d.strideTA = m.N * m.LZ * self.V
         d.tracer_vec = self.V
         d.TAout = None
+        if self.ab2_eps is not None:
+            # the update stage writes the next step's AB2 level into TA
+            d.TAout = self.TA.data_ptr()
+            d.ab_order, d.ab_eps = 2, self.ab2_eps
         d.vel, d.w, d.we = self.vel.data_ptr(), self.w.data_ptr(), self.we.data_ptr()
         d.wi = None if self.wi is None else self.wi.data_ptr()
         d.del_ = None

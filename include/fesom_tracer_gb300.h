@@ -217,6 +217,15 @@ typedef struct {
    * two layers) and the antidiffusive vertical flux takes the upwind flux of
    * w instead of we. Without FCT it has no effect, as in the reference. */
   const void* wi;
+  /* What TAout receives: ab_order 0 or 1 the new values; 2 the second-order
+   * Adams-Bashforth time level of the next step's high-order fluxes,
+   * -(0.5 + ab_eps) * T_old + (1.5 + ab_eps) * T_new, on every stored layer
+   * (FESOM2's tracer AB2 with offset epsilon; the reference declares
+   * epsilon = 0.1, lib/oce_modules.F90:75, and allocates valuesold,
+   * lib/tracer_c_interface.F90:561). TAout may alias TA: the update stage
+   * runs after every stage that reads TA. */
+  int ab_order;
+  double ab_eps;
 } fgb_step_desc;
 
 /* Full step: vflux, hflux, and the FCT (lo, ratio, update) or plain update. */

@@ -1427,17 +1427,18 @@ int om_analytic_step(const omesh* m, omwork* wk, int ntr, double dt, const doubl
                      double* values, double* valuesAB, const int* hor, const int* ver, const int* lim,
                      const double* ph, const double* pv, int copy_ab, double* del_ttf) {
   return om_analytic_step_split(m, wk, ntr, dt, vel, w, w, w, 0, values, valuesAB, hor, ver, lim, ph, pv, copy_ab,
-                                del_ttf);
+                                0.0, del_ttf);
 }
 
 int om_analytic_step_split(const omesh* m, omwork* wk, int ntr, double dt, const double* vel, const double* w,
                            const double* wi, const double* we, int use_wsplit, double* values, double* valuesAB,
                            const int* hor, const int* ver, const int* lim, const double* ph, const double* pv,
-                           int copy_ab, double* del_ttf) {
+                           int copy_ab, double ab_eps, double* del_ttf) {
   const int nzl = m->nl - 1, N = m->nod2D;
   const size_t blk = (size_t)nzl * N;
   double* dh = (double*)xcalloc(blk, sizeof(double));
   double* dv = (double*)xcalloc(blk, sizeof(double));
+  double* old = copy_ab == 2 ? (double*)xcalloc(blk, sizeof(double)) : NULL;
   int rc = 0;
   for (int t = 0; t < ntr && rc == 0; ++t) {
     memset(dh, 0, blk * sizeof(double));
@@ -1447,16 +1448,26 @@ int om_analytic_step_split(const omesh* m, omwork* wk, int ntr, double dt, const
     double* vab = valuesAB + t * blk;
     rc = om_do_oce_adv_tra(m, wk, dt, vel, w, wi, we, val, vab, hor[t], ver[t], lim[t], ph[t], pv[t], use_wsplit, dh,
                            dv);
+    if (old) memcpy(old, val, blk * sizeof(double));
     for (int k = 1; k <= N; ++k)
       for (int kz = m->ulevels_nod2D[k - 1]; kz <= m->nlevels_nod2D[k - 1] - 1; ++kz)
         A2(del_ttf, nzl, kz, k) = A2(del_ttf, nzl, kz, k) + A2(dh, nzl, kz, k) + A2(dv, nzl, kz, k);
     for (int k = 1; k <= N; ++k)
       for (int kz = m->ulevels_nod2D[k - 1]; kz <= m->nlevels_nod2D[k - 1] - 1; ++kz)
         A2(val, nzl, kz, k) = A2(val, nzl, kz, k) + A2(del_ttf, nzl, kz, k) / A2(m->hnode_new, nzl, kz, k);
-    if (copy_ab) memcpy(vab, val, blk * sizeof(double));
+    if (copy_ab == 2) {
+      /* second-order Adams-Bashforth time level of the next step's high-order
+       * fluxes with offset epsilon (FESOM2's tracer AB2; the reference
+       * declares epsilon = 0.1 at lib/oce_modules.F90:75 and allocates
+       * valuesold, lib/tracer_c_interface.F90:561) */
+      for (size_t i = 0; i < blk; ++i) vab[i] = -(0.5 + ab_eps) * old[i] + (1.5 + ab_eps) * val[i];
+    } else if (copy_ab) {
+      memcpy(vab, val, blk * sizeof(double));
+    }
   }
   free(dh);
   free(dv);
+  free(old);
   return rc;
 }
 

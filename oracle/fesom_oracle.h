@@ -75,12 +75,14 @@ int om_analytic_step(const omesh* m, omwork* wk, int ntr, double dt, const doubl
                      int copy_ab, double* del_ttf);
 /* The same with separate implicit / explicit vertical velocities: use_wsplit
  * applies adv_tra_vert_impl with wi to the FCT low-order solution
- * (lib/oce_adv_tra_driver.F90:221-231); we feeds the LO vertical flux. */
+ * (lib/oce_adv_tra_driver.F90:221-231); we feeds the LO vertical flux.
+ * copy_ab: 0 valuesAB frozen, 1 valuesAB = new values, 2 valuesAB =
+ * -(0.5+ab_eps) old + (1.5+ab_eps) new (second-order Adams-Bashforth). */
 int om_analytic_step_split(const omesh* m, omwork* wk, int ntr, double dt, const double* vel,
                            const double* w, const double* wi, const double* we, int use_wsplit,
                            double* values, double* valuesAB, const int* hor, const int* ver,
                            const int* lim, const double* ph, const double* pv, int copy_ab,
-                           double* del_ttf);
+                           double ab_eps, double* del_ttf);
 
 /* tracer_advect_step semantics (lib/tracer_c_interface.F90:163-220): tracer 1 only,
  * del_ttf accumulates across calls. */

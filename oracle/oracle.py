@@ -70,7 +70,7 @@ def lib():
         L.om_analytic_step_split.restype = ctypes.c_int
         L.om_analytic_step_split.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_double,
                                              _dp, _dp, _dp, _dp, ctypes.c_int, _dp, _dp, _ip, _ip, _ip, _dp, _dp,
-                                             ctypes.c_int, _dp]
+                                             ctypes.c_int, ctypes.c_double, _dp]
         L.om_cabi_step.restype = ctypes.c_int
         L.om_cabi_step.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, _dp, _dp, _dp, _dp,
                                    _dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
@@ -207,9 +207,12 @@ def do_oce_adv_tra(mesh, work, dt, vel, w, ttf, ttfAB, hor="UPW1", ver="UPW1", l
     return dh, dv
 
 
-def analytic_step(mesh, work, dt, vel, w, values, valuesAB, schemes, copy_ab=False, wi=None, we=None):
+def analytic_step(mesh, work, dt, vel, w, values, valuesAB, schemes, copy_ab=False, wi=None, we=None,
+                  ab2_eps=None):
     """One driver step for all tracers, in place. schemes: list of (hor, ver, lim[, ph, pv]).
-    wi / we as for do_oce_adv_tra."""
+    wi / we as for do_oce_adv_tra. valuesAB afterwards: unchanged (copy_ab
+    False), the new values (copy_ab True), or with ab2_eps given the
+    second-order Adams-Bashforth level -(0.5+eps) old + (1.5+eps) new."""
     ntr = len(schemes)
     assert values.flags.c_contiguous and values.dtype == np.float64
     assert valuesAB.flags.c_contiguous and valuesAB.dtype == np.float64
@@ -225,7 +228,8 @@ def analytic_step(mesh, work, dt, vel, w, values, valuesAB, schemes, copy_ab=Fal
     we = w if we is None else _f64(we)
     rc = lib().om_analytic_step_split(mesh.h, work.h, ntr, dt, _p(vel), _p(w), _p(wi), _p(we), int(split),
                                       _p(values), _p(valuesAB), _p(hor, _ip), _p(ver, _ip), _p(lim, _ip),
-                                      _p(ph), _p(pv), int(copy_ab), _p(del_ttf))
+                                      _p(ph), _p(pv), 2 if ab2_eps is not None else int(copy_ab),
+                                      0.0 if ab2_eps is None else float(ab2_eps), _p(del_ttf))
     if rc != 0:
         raise RuntimeError(f"om_analytic_step failed: {rc}")
 
