@@ -470,11 +470,50 @@ __device__ __forceinline__ V<KV> ppm_edge(const V<KV>* T, const V<KV>* D, const 
 
 // PPM flux of layer L (1-based) through its upper (W > 0) or lower (W < 0)
 // interface, lib/oce_adv_tra_ver.F90:598-632; x = min(|W| dt / h, 1).
+// Two tracers at once: the arithmetic in packed FP32x2 instructions, the
+// limiter's tests and selects per tracer.
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 sel2(bool cx, bool cy, float2 a, float2 b) {
+  return make_float2(cx ? a.x : b.x, cy ? a.y : b.y);
+}
+__device__ __forceinline__ float2 ppm_flux2(float2 aL, float2 aR, const float2 t0, float hx, float cx, bool upper,
+                                            float aw) {
+  const float2 pr = __fmul2_rn(__fadd2_rn(aR, neg2(t0)), __fadd2_rn(t0, neg2(aL)));
+  aL = sel2(pr.x <= 0.f, pr.y <= 0.f, t0, aL);
+  aR = sel2(pr.x <= 0.f, pr.y <= 0.f, t0, aR);
+  const float2 t3 = __fmul2_rn(t0, make_float2(3.f, 3.f));
+  const float2 sixth = make_float2(1.f / 6.f, 1.f / 6.f), mhalf = make_float2(-0.5f, -0.5f);
+  float2 d = __fadd2_rn(aR, neg2(aL));
+  float2 dm = __fmul2_rn(d, __ffma2_rn(__fadd2_rn(aL, aR), mhalf, t0));
+  float2 dd = __fmul2_rn(__fmul2_rn(d, d), sixth);
+  aL = sel2(dm.x > dd.x, dm.y > dd.y, __ffma2_rn(aR, make_float2(-2.f, -2.f), t3), aL);
+  d = __fadd2_rn(aR, neg2(aL));
+  dm = __fmul2_rn(d, __ffma2_rn(__fadd2_rn(aR, aL), mhalf, t0));
+  dd = __fmul2_rn(__fmul2_rn(d, d), sixth);
+  aR = sel2(dm.x < -dd.x, dm.y < -dd.y, __ffma2_rn(aL, make_float2(-2.f, -2.f), t3), aR);
+  const float2 aj = __fmul2_rn(__ffma2_rn(__fadd2_rn(aL, aR), mhalf, t0), make_float2(6.f, 6.f));
+  // upper: -aL - hx ((aR - aL) + cx aj); lower: -aR + hx ((aR - aL) - cx aj)
+  const float p = upper ? cx : -cx, h = upper ? -hx : hx;
+  const float2 q = __ffma2_rn(aj, make_float2(p, p), __fadd2_rn(aR, neg2(aL)));
+  const float2 tv = __ffma2_rn(q, make_float2(h, h), neg2(upper ? aL : aR));
+  return __fmul2_rn(tv, make_float2(aw, aw));
+}
+
 template <int KV>
 __device__ __forceinline__ V<KV> ppm_flux(const V<KV>& aL0, const V<KV>& aR0, const V<KV>& T0, float x, bool upper,
                                           float aw) {
   const float hx = 0.5f * x, cx = 1.f - (2.f / 3.f) * x;
   V<KV> r;
+  if constexpr (KV % 2 == 0) {
+#pragma unroll
+    for (int t = 0; t < KV; t += 2) {
+      const float2 f = ppm_flux2(make_float2(aL0.v[t], aL0.v[t + 1]), make_float2(aR0.v[t], aR0.v[t + 1]),
+                                 make_float2(T0.v[t], T0.v[t + 1]), hx, cx, upper, aw);
+      r.v[t] = f.x;
+      r.v[t + 1] = f.y;
+    }
+    return r;
+  } else {
 #pragma unroll
   for (int t = 0; t < KV; ++t) {
     float aL = aL0.v[t], aR = aR0.v[t];
@@ -491,6 +530,7 @@ __device__ __forceinline__ V<KV> ppm_flux(const V<KV>& aL0, const V<KV>& aR0, co
     r.v[t] = tv * aw;
   }
   return r;
+  }
 }
 
 // Vertical flux of the column at every interface into out[iz], minus fold[iz]
@@ -560,14 +600,12 @@ __device__ void vert_flux(const ColF& c, const V<KV>* T, V<KV>* D, V<KV>* TV, co
         V<KV> tvert = splat<KV>(0.f);
         if (z == nzmin) {
           tvert = muls(TV[nzmin - 1], -(W * ar));
-        } else if (z < nzmax) {
-          if (W > 0.f) {
-            const float x = fminf(fdv(W * dt, c.hn[z - 1]), 1.f);
-            tvert = ppm_flux<KV>(TV[z - 1], TV[z], T[z - 1], x, true, ar * W);
-          } else if (W < 0.f) {
-            const float x = fminf(-fdv(W * dt, c.hn[z - 2]), 1.f);
-            tvert = ppm_flux<KV>(TV[z - 2], TV[z - 1], T[z - 2], x, false, ar * W);
-          }
+        } else if (z < nzmax && W != 0.f) {
+          // the upwind layer's parabola: layer z (1-based) for W > 0, z - 1 for W < 0
+          const bool up = W > 0.f;
+          const int zl = up ? z - 1 : z - 2;
+          const float x = fminf(fdv(fabsf(W) * dt, c.hn[zl]), 1.f);
+          tvert = ppm_flux<KV>(TV[zl], TV[zl + 1], T[zl], x, up, ar * W);
         }
         r = sub(tvert, f0);
       }
