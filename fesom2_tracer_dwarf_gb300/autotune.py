@@ -2,9 +2,9 @@
 
 The step is five kernels (vertical fluxes, edge fluxes, FCT low-order
 solution, FCT ratios, update); four of them have launch knobs that do not
-change results (fgb_step_desc.cfg): edges per block of the edge-flux kernel,
-node columns per block of the three node kernels, and tracers per chunk
-(FP64) or layers per lane per pass (FP32). The
+change results (fgb_step_desc.cfg): edges per block of the edge-flux kernel
+(FP32: or the tiled edge kernel), node columns per block of the three node
+kernels, and tracers per chunk (FP64) or layers per lane per pass (FP32). The
 best choice depends on the mesh size, the number of layers, the tracer count
 and the precision, so this module times the candidates of each kernel on the
 caller's own engine (its mesh, fields and schemes) and keeps the fastest.
@@ -46,7 +46,8 @@ def stage_candidates(stage: str, K: int, precision: str = "fp64", wsplit: bool =
     the implicit vertical step (part of the LO stage)."""
     if stage == "hflux":
         if precision == "fp32":
-            return [{0: w, 7: ns} for w, ns in product(EDGE_WARPS, SLICES)]
+            # + the tiled kernel (node rows staged once per tile; its own launch shape)
+            return [{0: w, 7: ns} for w, ns in product(EDGE_WARPS, SLICES)] + [{9: 1}]
         return [{0: w} for w in EDGE_WARPS]
     slot = {"lo": 0, "ratio": 1, "update": 2}[stage]
     if precision == "fp32":

@@ -267,7 +267,52 @@ int fgb_mesh_create(const fgb_hmesh* hm, fgb_mesh** out) {
     };
     if (!fill(tu, n1, o, &fwu[(size_t)4 * e]) || !fill(td, n2, o + 2, &fwd[(size_t)4 * e])) d.fast_tri_ok = 0;
   }
-  bool ok = !upload(mm, ftri.data(), ftri.size(), &d.f_tri) && !upload(mm, fwu.data(), fwu.size(), &d.f_wu) &&
+  // Tiles of the visit order for the tiled FP32 edge kernel: consecutive
+  // positions while the tile has at most kTileEdges edges and kTileNodes
+  // distinct nodes among their n1, n2 and f_tri vertices.
+  std::vector<int> tile_ptr(1, 0), tile_nptr(1, 0), tile_nodes;
+  std::vector<unsigned char> tile_slots((size_t)8 * h.E, 0);
+  {
+    std::vector<int> stamp(h.N, -1), slot(h.N, 0);
+    int tile = 0, tn = 0, te = 0;
+    for (int p = 0; p < h.E; ++p) {
+      const int e = h.edge_order[p];
+      const int v6[6] = {h.edges[2 * e], h.edges[2 * e + 1], ftri[4 * (size_t)e], ftri[4 * (size_t)e + 1],
+                         ftri[4 * (size_t)e + 2], ftri[4 * (size_t)e + 3]};
+      int fresh = 0;
+      for (int j = 0; j < 6; ++j) {
+        bool seen = stamp[v6[j]] == tile;
+        for (int i = 0; i < j && !seen; ++i) seen = v6[i] == v6[j];
+        fresh += seen ? 0 : 1;
+      }
+      if (te == fgb::fast::kTileEdges || tn + fresh > fgb::fast::kTileNodes) {
+        tile_ptr.push_back(p);
+        tile_nptr.push_back((int)tile_nodes.size());
+        ++tile;
+        tn = te = 0;
+      }
+      for (int j = 0; j < 6; ++j) {
+        const int v = v6[j];
+        if (stamp[v] != tile) {
+          stamp[v] = tile;
+          slot[v] = tn++;
+          tile_nodes.push_back(v);
+        }
+        tile_slots[8 * (size_t)p + j] = (unsigned char)slot[v];
+      }
+      ++te;
+    }
+    tile_ptr.push_back(h.E);
+    tile_nptr.push_back((int)tile_nodes.size());
+    d.ntiles = (int)tile_ptr.size() - 1;
+    d.tile_max_nodes = 1;
+    for (int t = 0; t < d.ntiles; ++t) d.tile_max_nodes = std::max(d.tile_max_nodes, tile_nptr[t + 1] - tile_nptr[t]);
+  }
+  bool ok = !upload(mm, tile_ptr.data(), tile_ptr.size(), &d.tile_ptr) &&
+            !upload(mm, tile_nptr.data(), tile_nptr.size(), &d.tile_nptr) &&
+            !upload(mm, tile_nodes.data(), tile_nodes.size(), &d.tile_nodes) &&
+            !upload(mm, tile_slots.data(), tile_slots.size(), &d.tile_slots) &&
+            !upload(mm, ftri.data(), ftri.size(), &d.f_tri) && !upload(mm, fwu.data(), fwu.size(), &d.f_wu) &&
             !upload(mm, fwd.data(), fwd.size(), &d.f_wd) &&!upload(mm, h.nlev_nod.data(), h.nlev_nod.size(), &d.nlev) &&
             !upload(mm, h.ulev_nod.data(), h.ulev_nod.size(), &d.ulev) &&
             !upload(mm, h.nboundary_lay.data(), h.nboundary_lay.size(), &d.nbl) &&

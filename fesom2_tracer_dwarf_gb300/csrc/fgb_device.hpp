@@ -54,6 +54,17 @@ struct DMesh {
   const float* f_wu;
   const float* f_wd;
   int fast_tri_ok;
+  // FP32 form, tiled edge kernel: the visit order cut into tiles of at most
+  // kTileEdges edges touching at most kTileNodes distinct nodes (the edges'
+  // nodes and the f_tri vertices). Tile t holds visit positions
+  // tile_ptr[t] .. tile_ptr[t+1]-1 and nodes tile_nodes[tile_nptr[t] ..]; the
+  // 8 bytes of tile_slots[p] give the tile slots of position p's n1, n2 and
+  // four f_tri vertices.
+  int ntiles, tile_max_nodes;
+  const int* tile_ptr;
+  const int* tile_nptr;
+  const int* tile_nodes;
+  const unsigned char* tile_slots;
   GeoPtrs<double> g64;
   GeoPtrs<float> g32;
 };
@@ -82,6 +93,9 @@ struct StepPtrs {
 };
 
 namespace fast {
+constexpr int kTileEdges = 64;  // edges per tile of the tiled edge kernel
+constexpr int kTileNodes = 96;  // distinct nodes per tile
+
 // Pointers of one launch. Group g of a per-tracer array starts at
 // base + g * stride (floats); offsets inside a group are in units of KV floats.
 struct FastPtrs {
@@ -127,6 +141,7 @@ struct LaunchArgs {
   int mask, edge_warps, nw_lo, nw_ratio, nw_upd, hor, ver, fct;
   int ns_h, ns_lo, ns_ratio, ns_upd;  // layers per lane per pass (1 or 2)
   int vimpl_thomas;  // w_split: lane-per-column Thomas sweeps also for columns of <= 64 layers
+  int hflux_tile;    // edge fluxes by the tiled kernel (node rows staged once per tile)
 };
 }  // namespace fast
 

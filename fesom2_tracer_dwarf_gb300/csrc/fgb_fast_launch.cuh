@@ -5,6 +5,7 @@
 
 #include "fesom_tracer_gb300.h"
 #include "fgb_fast.cuh"
+#include "fgb_fast_tile.cuh"
 
 namespace fgb {
 namespace fast {
@@ -23,10 +24,23 @@ void launch_hflux_f(const DMesh& m, const FastPtrs& a, bool fct, int ew, cudaStr
   else kf_hflux<HOR, false, KV, NS><<<grid, block, sm, s>>>(m, a);
 }
 
+template <int KV, int HOR, bool FCT>
+void launch_hflux_tile(const DMesh& m, const FastPtrs& a, cudaStream_t s) {
+  const size_t sm = tile_smem_bytes(KV, FCT && a.TA != a.T, m.tile_max_nodes);
+  allow_smem_f(kf_hflux_tile<HOR, FCT, KV>, sm);
+  kf_hflux_tile<HOR, FCT, KV><<<m.ntiles, kTileThreads, sm, s>>>(m, a);
+}
+
 template <int KV, int HOR>
 void launch_hflux_ns(const DMesh& m, const FastPtrs& a, const LaunchArgs& L, cudaStream_t s) {
-  if (L.ns_h == 1) launch_hflux_f<KV, HOR, 1>(m, a, L.fct, L.edge_warps, s);
-  else launch_hflux_f<KV, HOR, 2>(m, a, L.fct, L.edge_warps, s);
+  if (L.hflux_tile && m.ntiles > 0) {
+    if (L.fct) launch_hflux_tile<KV, HOR, true>(m, a, s);
+    else launch_hflux_tile<KV, HOR, false>(m, a, s);
+  } else if (L.ns_h == 1) {
+    launch_hflux_f<KV, HOR, 1>(m, a, L.fct, L.edge_warps, s);
+  } else {
+    launch_hflux_f<KV, HOR, 2>(m, a, L.fct, L.edge_warps, s);
+  }
 }
 
 template <int KV, int VER, int NS>

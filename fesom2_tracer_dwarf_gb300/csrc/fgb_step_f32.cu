@@ -100,6 +100,10 @@ int launch_stages_f32(const DMesh& m, const fgb_step_desc& d, int mask, cudaStre
   L.ns_ratio = (d.cfg[5] >= 1 && d.cfg[5] <= 4) ? d.cfg[5] : 0;
   L.ns_upd = ns(d.cfg[6], 1);
   L.vimpl_thomas = d.cfg[8] == 1;
+  // the tiled edge kernel stages rows with 16-byte asynchronous copies
+  auto al16 = [](const void* p) { return p == nullptr || reinterpret_cast<uintptr_t>(p) % 16 == 0; };
+  L.hflux_tile = d.cfg[9] == 1 && al16(d.T) && al16(d.TA) && al16(d.workspace) && (d.strideT * 4) % 16 == 0 &&
+                 (!d.TA || (d.strideTA * 4) % 16 == 0);
   L.hor = d.hor;
   L.ver = d.ver;
   L.fct = d.lim == FGB_LIM_FCT;

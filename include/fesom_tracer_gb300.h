@@ -208,7 +208,9 @@ typedef struct {
    * cfg[8]     FP32 form, w_split: 0 parallel cyclic reduction, one warp per
    *            column (columns of at most 64 layers; deeper ones always use
    *            the other solver), 1 Thomas sweeps, one lane per column
-   * cfg[9..11] unused, 0 */
+   * cfg[9]     FP32 form: 1 edge fluxes by the tiled kernel (each tile's node
+   *            rows staged once in shared memory)
+   * cfg[10..11] unused, 0 */
   int cfg[12];
   /* w_split (dynamics%use_wsplit, lib/oce_adv_tra_driver.F90:221-231): NULL
    * for off, else the implicit vertical velocity wi (N,LW). Under FCT the

@@ -20,7 +20,8 @@ def test_candidates_cover_allowed_values():
     assert all(set(c) == {3, 6} for c in up)
     r32 = autotune.stage_candidates("ratio", 4, "fp32")
     assert len(r32) == 12 and {2: 4, 5: 1} in r32 and {2: 2, 5: 3} in r32 and {2: 1, 5: 4} in r32
-    assert {0: 2, 7: 1} in autotune.stage_candidates("hflux", 4, "fp32")
+    assert {0: 2, 7: 1} in autotune.stage_candidates("hflux", 4, "fp32") and {9: 1} in autotune.stage_candidates(
+        "hflux", 4, "fp32")
     lo32 = autotune.stage_candidates("lo", 4, "fp32")
     lo32s = autotune.stage_candidates("lo", 4, "fp32", wsplit=True)
     assert len(lo32s) == 2 * len(lo32) and {1: 2, 4: 1, 8: 1} in lo32s and {1: 2, 4: 1, 8: 0} in lo32s

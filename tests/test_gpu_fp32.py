@@ -163,3 +163,39 @@ def test_fp32_workspace_views_follow_groups(pkg, oracle_mod):
         W = O.Work(om)
         O.do_oce_adv_tra(om, W, 300.0, vel, w, T[t], T[t], "MUSCL", "QR4C", "FCT")
         assert _rel(lo[t], W.get("fct_LO")) <= REL_TOL
+
+
+@pytest.mark.parametrize("meshname", ["periodic", "closed_left", "ragged"])
+@pytest.mark.parametrize("hor,lim", [("UPW1", "FCT"), ("MUSCL", "FCT"), ("MFCT", "FCT"), ("MUSCL", "NONE")])
+@pytest.mark.parametrize("K,V,frozen", [(4, 4, False), (4, 4, True), (6, 2, False), (3, 1, True)])
+def test_fp32_tiled_edge_kernel(pkg, oracle_mod, meshname, hor, lim, K, V, frozen):
+    """The tiled edge-flux kernel (cfg[9] = 1: node rows staged once per tile)
+    gives the default kernel's fluxes and the oracle's step, with T_AB shared
+    or separate, for every group width."""
+    mesh_mod, engine, synthetic = pkg
+    O = oracle_mod
+    kw = _ragged() if meshname == "ragged" else MESHES[meshname]
+    om, m = _pair(O, mesh_mod, **kw)
+    rng = np.random.default_rng(zlib.crc32(f"tile/{meshname}/{hor}/{lim}/{K}/{frozen}".encode()))
+    vel, w = synthetic.random_flow(m, rng)
+    T = synthetic.random_field(m, rng, K)
+    TA = T + rng.normal(0, 0.05, size=T.shape) if frozen else T
+    dt = 300.0
+    sch = (hor, "PPM", lim, 0.7, 0.6)
+    vals, vab = np.ascontiguousarray(T.copy()), np.ascontiguousarray(TA.copy())
+    O.analytic_step(om, O.Work(om), dt, vel, w, vals, vab, [sch] * K, copy_ab=not frozen)
+    out = {}
+    from fesom2_tracer_dwarf_gb300 import _lib
+
+    for tiled in (0, 1):
+        eng = engine.TracerAdvection(m, K, "fp32", *sch[:3], ph=0.7, pv=0.6, copy_ab=not frozen, tracer_vec=V)
+        eng.set_launch([0] * 9 + [tiled])
+        eng.set_tracers(T, TA if frozen else None)
+        eng.set_velocity(vel, w)
+        eng.step(dt, stages=_lib.STAGE_VFLUX | _lib.STAGE_HFLUX)
+        torch.cuda.synchronize()
+        out[tiled] = eng.workspace_view("adfh").cpu().numpy()
+        eng.step(dt, stages=_lib.STAGE_ALL & ~(_lib.STAGE_VFLUX | _lib.STAGE_HFLUX))
+        torch.cuda.synchronize()
+        assert _rel(eng.values(), vals) <= REL_TOL
+    assert np.allclose(out[1], out[0], rtol=1e-6, atol=1e-6 * np.abs(out[0]).max())
