@@ -64,6 +64,22 @@ def _env_rank():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def job_rate(ms_local, cells_local, dist=None, device="cpu"):
+    """Whole-job figures of a replicas run: each rank advanced its own copy
+    (cells_local tracer-cell updates per step) in ms_local per step. The job's
+    time per step is the slowest rank's, its work the sum over ranks. Returns
+    (ms per step, tracer-cell updates/s)."""
+    import torch
+
+    tm = torch.tensor([float(ms_local)], dtype=torch.float64, device=device)
+    tc = torch.tensor([float(cells_local)], dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(tm, op=dist.ReduceOp.MAX)
+        dist.all_reduce(tc, op=dist.ReduceOp.SUM)
+    t_max = float(tm.item())
+    return t_max, float(tc.item()) / (t_max / 1e3)
+
+
 # ---------------------------------------------------------------------------
 # Clocks during the timed region
 # ---------------------------------------------------------------------------
@@ -469,12 +485,7 @@ def run_gpu(args):
             total_ms, per, launches = time_engine(eng, T0, cfg["dt"], args.steps, args.warmup, barrier)
     clocks = clk.summary()
     ms = total_ms / nsteps
-    t_max = ms
-    if dist is not None:
-        tt = torch.tensor([ms], device=device)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
-    value = cells * world / (t_max / 1e3)
+    t_max, value = job_rate(ms, cells, dist, device)
     s = 4 if cfg["precision"] == "fp32" else 8
     wet_frac = m.wet_cells() / (m.N * m.nz)
     sb = {k: v * wet_frac for k, v in stage_bytes(m, K, s, cfg["ver"], fct=cfg["lim"] == "FCT",
@@ -488,7 +499,7 @@ def run_gpu(args):
     traffic = load_traffic(args.workload).get(dom)
     e2e_steps = max(2, min(nsteps, 10))
     e2e_ms, h2d, d2h = time_e2e(eng, T0, cfg["dt"], e2e_steps, barrier)
-    e2e_value = cells * world / (e2e_ms / e2e_steps / 1e3)
+    _, e2e_value = job_rate(e2e_ms / e2e_steps, cells, dist, device)
     if cfg["kind"] == "flat":
         mesh_desc = f"{cfg['nx'] - 1}x{cfg['nx'] - 1} doubly periodic analytic grid, dx=1 km, {cfg['nz']} layers 5->250 m"
     elif cfg["kind"] == "closed":
@@ -529,7 +540,7 @@ def run_gpu(args):
         n64 = max(2, min(args.steps, args.fp64_steps))
         tot64, per64, l64 = time_engine(e64, T64, cfg["dt"], n64, min(args.warmup, 2), barrier)
         ms64 = tot64 / n64
-        result["fp64"] = {"value": cells * world / (ms64 / 1e3), "ms_per_step": ms64, "steps": n64,
+        result["fp64"] = {"value": job_rate(ms64, cells, dist, device)[1], "ms_per_step": ms64, "steps": n64,
                           "stage_ms": {k: round(v, 3) for k, v in per64.items()}}
         result["fp32_over_fp64"] = value / result["fp64"]["value"]
         result["gpu_launches"] += l64
@@ -558,7 +569,7 @@ def run_gpu(args):
             result["gpu_launches"] += e.launches
             del e, p, v, w, T
         ms64 = tot64 / n64
-        result["fp64"] = {"value": cells * world / (ms64 / 1e3), "ms_per_step": ms64, "steps": n64,
+        result["fp64"] = {"value": job_rate(ms64, cells, dist, device)[1], "ms_per_step": ms64, "steps": n64,
                           "mode": "per-mesh sequential eager launches"}
         result["fp32_over_fp64"] = value / result["fp64"]["value"]
     if rank == 0 and not args.no_cpu:
