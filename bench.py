@@ -308,6 +308,8 @@ def precision_report(m, e32, T32, e64, T64, dt, steps):
     vol = torch.as_tensor(m.get("areasvol")[:, :nz] * m.get("hnode_new"), device=dev) * wet
     init = e64.from_layout(T64)[:, :, :nz]
     a = e32.from_layout(e32.T)[:, :, :nz].double()
+    if e32.offsets is not None:  # anomaly storage
+        a = a + torch.as_tensor(e32.offsets, device=a.device)[:, None, None]
     b = e64.from_layout(e64.T)[:, :, :nz]
     out = {"steps": steps, "max_rel_err": [], "sum_rel_err_fp32": [], "sum_rel_err_fp64": [],
            "violations_fp32": [], "violations_fp64": [], "max_excursion_fp32": [], "max_excursion_fp64": []}
@@ -546,6 +548,12 @@ def run_gpu(args):
         result["gpu_launches"] += l64
         if cfg.get("report_steps"):
             result["precision_report"] = precision_report(m, eng, T0, e64, T64, cfg["dt"], cfg["report_steps"])
+            # the same with the FP32 form storing anomalies about each tracer's initial mean
+            eng._offsets_req = "mean"
+            eng.load_padded(T=e64.from_layout(T64).clone())
+            result["precision_report_anomaly"] = precision_report(m, eng, eng.T.clone(), e64, T64, cfg["dt"],
+                                                                  cfg["report_steps"])
+            result["precision_report_anomaly"]["offsets"] = [float(c) for c in eng.offsets]
         del e64
     elif cfg.get("compare_fp64") == "sequential" and not args.no_fp64:
         # per-mesh sequential plain FP64 steps (eager launches, one mesh after another)

@@ -15,6 +15,19 @@ values given to ``set_tracers`` -- the analytic dwarf, src/fesom_analytic.F90:33
 second-order Adams-Bashforth level -(0.5+eps) T_old + (1.5+eps) T_new that the
 update stage writes for the next step (FESOM2's tracer AB2 with offset
 epsilon; the reference declares epsilon = 0.1 at lib/oce_modules.F90:75).
+
+Anomaly storage (``offsets``, opt-in, meant for the FP32 form): each tracer is
+stored as T - c_t for a per-tracer reference value c_t (given, or the mean of
+the initial values), and c_t is added back by ``values`` and ``stats``. Every
+scheme of the step maps T + c to T' + c when a uniform field stays uniform,
+i.e. when the velocities satisfy the discrete continuity of the step (as the
+flows of the benchmark configurations do); then the stored anomalies advance
+exactly as the full values would, and FP32 rounds them at their own, much
+smaller magnitude (S ~ 35 +- 0.3 keeps ~2 more digits). For flows that do not
+keep a uniform field uniform the offsets change the answer: leave them off.
+The FCT limiter is shift-invariant only while values and anomalies stay
+within +-1000: the reference bounds elements that are dry at a layer by
++-1e3 (bignumber, lib/oce_adv_tra_fct.F90:81,142-143).
 """
 from __future__ import annotations
 
@@ -39,7 +52,7 @@ class TracerAdvection:
     def __init__(self, mesh: Mesh, ntracers: int, precision: str = "fp64", hor: str = "UPW1",
                  ver: str = "UPW1", lim: str = "NONE", ph: float = 1.0, pv: float = 1.0,
                  copy_ab: bool = False, device: str = "cuda", tracer_vec: int | None = None,
-                 ab2_eps: float | None = None):
+                 ab2_eps: float | None = None, offsets=None):
         _require_cuda()
         if ab2_eps is not None and copy_ab:
             raise ValueError("copy_ab and ab2_eps are two choices of the valuesAB time level; give one")
@@ -57,6 +70,10 @@ class TracerAdvection:
         self.set_schemes(hor, ver, lim, ph, pv)
         self.copy_ab = copy_ab
         self.ab2_eps = None if ab2_eps is None else float(ab2_eps)
+        if offsets is not None and not (isinstance(offsets, str) and offsets == "mean"):
+            offsets = np.asarray(offsets, dtype=np.float64).reshape(self.K)
+        self._offsets_req = offsets
+        self.offsets = None  # per-tracer reference values of the stored anomalies (resolved at set_tracers)
         m = mesh
         m.upload()
         z = lambda *s: torch.zeros(*s, dtype=self.dtype, device=self.device)
@@ -123,14 +140,36 @@ class TracerAdvection:
         out[..., :width] = t.cpu()
         return out.to(self.device)
 
+    def _resolve_offsets(self, vals64):
+        """vals64: (K, N, nz) float64 tensor or array of the initial values."""
+        req = self._offsets_req
+        if req is None:
+            self.offsets = None
+        elif isinstance(req, str):
+            t = torch.as_tensor(vals64, dtype=torch.float64)
+            self.offsets = t.reshape(self.K, -1).mean(dim=1).cpu().numpy()
+        else:
+            self.offsets = req
+
+    def _shifted(self, vals, ld):
+        """(K, N, nz) float64 values -> (K, N, ld) engine dtype on the host, minus the offsets."""
+        m = self.mesh
+        t = torch.as_tensor(np.asarray(vals) if not torch.is_tensor(vals) else vals.cpu(), dtype=torch.float64)
+        t = t.reshape(self.K, m.N, -1)
+        if self.offsets is not None:
+            t = t - torch.as_tensor(self.offsets, dtype=torch.float64)[:, None, None]
+        out = torch.zeros(self.K, m.N, ld, dtype=self.dtype)
+        out[..., : t.shape[-1]] = t.to(self.dtype)
+        return out.to(self.device)
+
     def set_tracers(self, values, values_ab=None):
         """values: (K, N, nz) array. values_ab defaults to values."""
         m = self.mesh
-        v = self.to_layout(self._pad_nodes(values, m.nz, m.LZ).reshape(self.K, m.N, m.LZ))
+        self._resolve_offsets(values if torch.is_tensor(values) else np.asarray(values, dtype=np.float64))
+        v = self.to_layout(self._shifted(values, m.LZ))
         self.T.copy_(v)
         if self.TA is not None:
-            vab = v if values_ab is None else self._pad_nodes(values_ab, m.nz, m.LZ).reshape(self.K, m.N, m.LZ)
-            self.TA.copy_(self.to_layout(vab) if values_ab is not None else v)
+            self.TA.copy_(self.to_layout(self._shifted(values_ab, m.LZ)) if values_ab is not None else v)
 
     def set_velocity(self, vel, w, we=None, wi=None):
         """vel: (M, nz, 2) on elements; w, we, wi: (N, nl) at node interfaces.
@@ -153,10 +192,16 @@ class TracerAdvection:
     def load_padded(self, T=None, TA=None, vel=None, w=None, we=None, wi=None):
         """Copy device tensors that already have the padded layouts
         (K,N,LZ), (M,LZ,2), (N,LW). wi (w_split) is kept until replaced."""
+        m = self.mesh
         if T is not None:
-            self.T.copy_(self.to_layout(T))
+            self._resolve_offsets(T[:, :, : m.nz].double())
+            if self.offsets is not None:
+                T = T.double() - torch.as_tensor(self.offsets, device=T.device)[:, None, None]
+            self.T.copy_(self.to_layout(T.to(self.dtype)))
         if TA is not None and self.TA is not None:
-            self.TA.copy_(self.to_layout(TA))
+            if self.offsets is not None:
+                TA = TA.double() - torch.as_tensor(self.offsets, device=TA.device)[:, None, None]
+            self.TA.copy_(self.to_layout(TA.to(self.dtype)))
         if vel is not None:
             self.vel.copy_(vel)
         if w is not None:
@@ -220,7 +265,10 @@ class TracerAdvection:
     def values(self) -> np.ndarray:
         """(K, N, nz) tracer values as float64."""
         m = self.mesh
-        return self.from_layout(self.T)[:, :, : m.nz].double().cpu().numpy()
+        v = self.from_layout(self.T)[:, :, : m.nz].double().cpu().numpy()
+        if self.offsets is not None:
+            v += self.offsets[:, None, None]
+        return v
 
     def workspace_view(self, name: str):
         """One workspace array per tracer: vf (E,LZ), adfh (K,E,LZ), lo (K,N,LZ),
@@ -262,4 +310,10 @@ class TracerAdvection:
                                                   self.K, self.V, ctypes.c_void_p(self._stats_scratch.data_ptr()),
                                                   ctypes.c_void_p(self._stats_out.data_ptr()), stream),
                        "fgb_tracer_stats_grouped")
-        return self._stats_out.cpu().numpy()
+        out = self._stats_out.cpu().numpy()
+        if self.offsets is not None:
+            out = out.copy()
+            out[:, 0] += self.offsets
+            out[:, 1] += self.offsets
+            out[:, 2] += self.offsets * float(m.N * m.nz)
+        return out

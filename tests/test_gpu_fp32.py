@@ -199,3 +199,43 @@ def test_fp32_tiled_edge_kernel(pkg, oracle_mod, meshname, hor, lim, K, V, froze
         torch.cuda.synchronize()
         assert _rel(eng.values(), vals) <= REL_TOL
     assert np.allclose(out[1], out[0], rtol=1e-6, atol=1e-6 * np.abs(out[0]).max())
+
+
+def test_fp32_anomaly_storage(pkg, oracle_mod):
+    """Anomaly storage (offsets): with a continuity-consistent flow the stored
+    anomalies advance like the full values, and FP32 error against the FP64
+    oracle drops; zero offsets change nothing; stats add the offsets back."""
+    mesh_mod, engine, synthetic = pkg
+    O = oracle_mod
+    om, m = _pair(O, mesh_mod, **_ragged(14, 12, 14, seed=8))
+    rng = np.random.default_rng(70)
+    dt = 300.0
+    vel, w = synthetic.streamfunction_flow(m, rng, dt, cfl=0.4, psi_wall_zero=True)
+    K = 4
+    # (values stay below 1000: the FCT bound of dry elements is +-1e3, lib/oce_adv_tra_fct.F90:81,142-143)
+    T = synthetic.random_field(m, rng, K) * 0.03 + np.array([35.0, 20.0, 500.0, 0.5])[:, None, None]
+    sch = ("MUSCL", "PPM", "FCT")
+    vals = np.ascontiguousarray(T.copy())
+    vab = vals.copy()
+    W = O.Work(om)
+    for _ in range(20):
+        O.analytic_step(om, W, dt, vel, w, vals, vab, [sch] * K, copy_ab=True)
+    errs = {}
+    for off in (None, "mean", np.zeros(K)):
+        eng = engine.TracerAdvection(m, K, "fp32", *sch, copy_ab=True, offsets=off)
+        eng.set_tracers(T)
+        eng.set_velocity(vel, w)
+        eng.step(dt, 20)
+        torch.cuda.synchronize()
+        got = eng.values()
+        key = "zero" if isinstance(off, np.ndarray) else str(off)
+        errs[key] = np.abs(got - vals).reshape(K, -1).max(axis=1) / np.abs(vals).reshape(K, -1).max(axis=1)
+        if key == "zero":
+            assert np.array_equal(got, plain)
+        if key == "None":
+            plain = got
+        st = eng.stats()
+        assert np.allclose(st[:, 0], got.reshape(K, -1).min(axis=1)) and np.allclose(st[:, 1], got.reshape(K, -1).max(axis=1))
+        assert np.allclose(st[:, 2], got.reshape(K, -1).sum(axis=1), rtol=1e-10)
+    assert np.all(errs["mean"] <= 1e-6), errs
+    assert np.all(errs["mean"][:3] < 0.2 * errs["None"][:3]), errs
