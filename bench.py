@@ -371,24 +371,25 @@ def time_engine(eng, T0, dt, steps, warmup, dist_barrier, stage_steps=5):
 
 
 def time_e2e(eng, T0, dt, steps, dist_barrier):
-    """Same step through the public API with host buffers: H2D of the tracer
-    fields from pinned memory, the step, D2H of the result, every step."""
+    """Same steps through the public API with host buffers
+    (TracerAdvection.run_host): every step is one batch whose tracer fields
+    are copied host-to-device from pinned memory, stepped, and copied back
+    device-to-host; the copies of neighbouring batches overlap the steps."""
     import torch
 
     host_in = torch.empty(T0.shape, dtype=T0.dtype, pin_memory=True)
     host_in.copy_(T0.cpu())
     host_out = torch.empty_like(host_in).pin_memory()
+    eng.run_host([host_in], [host_out], dt)  # warm-up: streams and buffers
     torch.cuda.synchronize()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     dist_barrier()
     start.record()
-    for _ in range(steps):
-        eng.T.copy_(host_in, non_blocking=True)
-        eng.step(dt)
-        host_out.copy_(eng.T, non_blocking=True)
+    eng.run_host([host_in] * steps, [host_out] * steps, dt)
     end.record()
     torch.cuda.synchronize()
     dist_barrier()
+    eng.T.copy_(T0)
     nbytes = host_in.numel() * host_in.element_size()
     return start.elapsed_time(end), nbytes, nbytes
 

@@ -247,6 +247,62 @@ class TracerAdvection:
             _lib.check(L.fgb_adv_stages(self.mesh.handle, ctypes.byref(d), stages, stream), "fgb_adv_stages")
             self.launches += L.fgb_last_launch_count()
 
+    def run_host(self, host_in, host_out, dt: float, nsteps: int = 1):
+        """Advance independent batches of tracer fields that live in host
+        memory: batch i is copied to the device from ``host_in[i]``, advanced
+        ``nsteps`` steps, and copied back into ``host_out[i]`` (tensors of
+        ``layout_shape`` and the engine's dtype, pinned for asynchronous
+        copies; one tensor may serve several batches).
+
+        Three device buffers take turns as the field being stepped, the next
+        batch arriving and the previous batch leaving, so the host-to-device
+        copy of batch i+1 and the device-to-host copy of batch i-1 run on two
+        copy streams while batch i steps on the current stream. Needs a
+        copy-AB engine (valuesAB follows the values). Returns on the host
+        when every copy of every batch has been issued; synchronise the device
+        before reading ``host_out``."""
+        if self.TA is not None:
+            raise ValueError("run_host needs copy_ab=True (valuesAB follows the values)")
+        nb = len(host_in)
+        if len(host_out) != nb:
+            raise ValueError("host_in and host_out need one tensor per batch")
+        main = torch.cuda.current_stream(self.device)
+        if not hasattr(self, "_host_bufs"):
+            self._host_bufs = [self.T] + [torch.empty_like(self.T) for _ in range(2)]
+            self._h2d = torch.cuda.Stream(self.device)
+            self._d2h = torch.cuda.Stream(self.device)
+        bufs = self._host_bufs
+        free = [torch.cuda.Event() for _ in range(3)]     # buffer no longer read by a D2H copy
+        arrived = [torch.cuda.Event() for _ in range(3)]  # H2D copy into the buffer done
+        stepped = [torch.cuda.Event() for _ in range(3)]  # steps on the buffer done
+        for b in range(3):
+            free[b].record(main)
+
+        def load(i):
+            b = i % 3
+            with torch.cuda.stream(self._h2d):
+                self._h2d.wait_event(free[b])
+                bufs[b].copy_(host_in[i], non_blocking=True)
+                arrived[b].record(self._h2d)
+
+        if nb:
+            load(0)
+        for i in range(nb):
+            b = i % 3
+            if i + 1 < nb:
+                load(i + 1)
+            main.wait_event(arrived[b])
+            self.T = bufs[b]
+            self.step(dt, nsteps)
+            stepped[b].record(main)
+            with torch.cuda.stream(self._d2h):
+                self._d2h.wait_event(stepped[b])
+                host_out[i].copy_(bufs[b], non_blocking=True)
+                free[b].record(self._d2h)
+        for b in range(3):
+            main.wait_event(free[b])
+        return host_out
+
     def capture(self, dt: float, nsteps: int = 1):
         """Record ``nsteps`` steps as one CUDA graph (torch.cuda.CUDAGraph);
         ``graph.replay()`` then advances the tracers by nsteps steps with one

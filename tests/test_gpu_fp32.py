@@ -239,3 +239,29 @@ def test_fp32_anomaly_storage(pkg, oracle_mod):
         assert np.allclose(st[:, 2], got.reshape(K, -1).sum(axis=1), rtol=1e-10)
     assert np.all(errs["mean"] <= 1e-6), errs
     assert np.all(errs["mean"][:3] < 0.2 * errs["None"][:3]), errs
+
+
+def test_run_host_batches(pkg, oracle_mod):
+    """run_host: independent batches from host memory, copies overlapped with
+    the steps, give what stepping each batch on its own gives."""
+    mesh_mod, engine, synthetic = pkg
+    m = mesh_mod.Mesh(**MESHES["periodic"])
+    rng = np.random.default_rng(80)
+    vel, w = synthetic.random_flow(m, rng)
+    eng = engine.TracerAdvection(m, 4, "fp32", "MUSCL", "PPM", "FCT", copy_ab=True)
+    eng.set_velocity(vel, w)
+    fields = [synthetic.random_field(m, rng, 4) for _ in range(5)]
+    expect = []
+    for f in fields:
+        eng.set_tracers(f)
+        eng.step(300.0, 2)
+        expect.append(eng.T.cpu().clone())
+    host_in = []
+    for f in fields:
+        eng.set_tracers(f)
+        host_in.append(eng.T.cpu().pin_memory())
+    host_out = [torch.empty_like(h).pin_memory() for h in host_in]
+    eng.run_host(host_in, host_out, 300.0, nsteps=2)
+    torch.cuda.synchronize()
+    for got, exp in zip(host_out, expect):
+        assert torch.equal(got, exp)
