@@ -500,7 +500,7 @@ def run_gpu(args):
     dom = max(per, key=per.get)
     achieved = sb[dom] / (per[dom] / 1e3) / 1e9
     traffic = load_traffic(args.workload).get(dom)
-    e2e_steps = max(2, min(nsteps, 10))
+    e2e_steps = max(2, min(nsteps, 20))
     e2e_ms, h2d, d2h = time_e2e(eng, T0, cfg["dt"], e2e_steps, barrier)
     _, e2e_value = job_rate(e2e_ms / e2e_steps, cells, dist, device)
     if cfg["kind"] == "flat":
