@@ -117,6 +117,7 @@ struct FastPtrs {
   float dt, ph, pv;
   int ab2;  // TAout = ab_old * T_old + ab_new * T_new (else T_new)
   float ab_old, ab_new;
+  int wsplit_fused;  // w_split: the LO kernel also solves the implicit vertical step
 };
 
 // Shared-memory shape of the w_split kernel (kf_vert_impl): a warp holds

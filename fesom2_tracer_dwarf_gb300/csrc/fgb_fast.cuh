@@ -671,6 +671,94 @@ struct WarpMem {
   }
 };
 
+template <int KV>
+__device__ __forceinline__ V<KV> shfl_v(const V<KV>& x, int src) {
+  V<KV> r;
+#pragma unroll
+  for (int t = 0; t < KV; ++t) r.v[t] = __shfl_sync(0xffffffffu, x.v[t], src);
+  return r;
+}
+
+template <int KV>
+struct PcrRow {
+  float A, C;
+  V<KV> D;
+};
+
+template <int KV>
+__device__ __forceinline__ PcrRow<KV> pcr_shfl(const PcrRow<KV>& r, int src) {
+  return PcrRow<KV>{__shfl_sync(0xffffffffu, r.A, src), __shfl_sync(0xffffffffu, r.C, src), shfl_v<KV>(r.D, src)};
+}
+
+template <int KV>
+__device__ __forceinline__ void pcr_update(float& a, float& b, float& c, V<KV>& d, PcrRow<KV>& row, bool hm,
+                                           const PcrRow<KV>& m, bool hp, const PcrRow<KV>& p) {
+  const float Am = hm ? m.A : 0.f, Cm = hm ? m.C : 0.f, Ap = hp ? p.A : 0.f, Cp = hp ? p.C : 0.f;
+  const float na = -a, nc = -c;
+  b = fmaf(nc, Ap, fmaf(na, Cm, b));
+  V<KV> dd = d;
+  if (hm) dd = fmas(m.D, na, dd);
+  if (hp) dd = fmas(p.D, nc, dd);
+  d = dd;
+  a = na * Am;
+  c = nc * Cp;
+  const float rb = fdv(1.f, b);
+  row.A = a * rb;
+  row.C = c * rb;
+  row.D = muls(d, rb);
+}
+
+// Parallel cyclic reduction of one column held by a warp, rows lane and
+// lane + 32 (a: coupling to the row above, b: diagonal, c: coupling to the row
+// below, d: right-hand sides); rows outside the column are identity rows
+// (a = c = d = 0, b = 1). Six steps couple rows 1, 2, 4, ..., 32 apart; d
+// returns the solution.
+template <int KV>
+__device__ __forceinline__ void pcr_solve2(float av[2], float bv[2], float cv[2], V<KV> dv[2], int lane) {
+  PcrRow<KV> row[2];
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const float rb = fdv(1.f, bv[r]);
+    row[r] = PcrRow<KV>{av[r] * rb, cv[r] * rb, muls(dv[r], rb)};
+  }
+#pragma unroll
+  for (int h = 1; h < kW; h *= 2) {
+    const int sm = (lane - h) & (kW - 1), sp = (lane + h) & (kW - 1);
+    const PcrRow<KV> m0 = pcr_shfl(row[0], sm), m1 = pcr_shfl(row[1], sm);
+    const PcrRow<KV> p0 = pcr_shfl(row[0], sp), p1 = pcr_shfl(row[1], sp);
+    const bool lo_in = lane >= h, hi_in = lane + h < kW;
+    // row lane: k - h from lane - h (row 0) if lane >= h; k + h from lane + h
+    // (row 0) or, past 31, from lane + h - 32 (row 1)
+    pcr_update(av[0], bv[0], cv[0], dv[0], row[0], lo_in, m0, true, hi_in ? p0 : p1);
+    // row lane + 32: k - h from lane - h (row 1) or lane - h + 32 (row 0);
+    // k + h from lane + h (row 1) while below 64
+    pcr_update(av[1], bv[1], cv[1], dv[1], row[1], true, lo_in ? m1 : m0, hi_in, p1);
+  }
+  {  // h = 32: the two rows of a lane couple to each other
+    const PcrRow<KV> r0 = row[0], r1 = row[1];
+    pcr_update(av[0], bv[0], cv[0], dv[0], row[0], false, r0, true, r1);
+    pcr_update(av[1], bv[1], cv[1], dv[1], row[1], true, r0, false, r1);
+  }
+  dv[0] = row[0].D;
+  dv[1] = row[1].D;
+}
+
+// Row k of the implicit upwind system of w_split (lib/oce_adv_tra_ver.F90:
+// 158-190) for a column with layers k0..k1 (0-based): a, b, c from wi at the
+// row's two interfaces, the interface areas, areasvol and hnode_new.
+__device__ __forceinline__ void vimpl_row(int k, int k0, int k1, float W0, float W1, float ar0, float ar1, float av,
+                                          float hnn, float dt, float& a, float& b, float& c) {
+  const float rav = fdv(dt, av);
+  const float v0 = ar0 * rav, v1 = ar1 * rav;
+  a = k == k0 ? 0.f : fminf(W0, 0.f) * v0;
+  b = hnn + (k == k0 ? W0 : fmaxf(W0, 0.f)) * v0;
+  c = 0.f;
+  if (k != k1) {
+    b -= fminf(W1, 0.f) * v1;
+    c = -fmaxf(W1, 0.f) * v1;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // FCT stage 1: low-order solution and vertical antidiffusive flux
 // (lib/oce_adv_tra_driver.F90:91-235). Low-order edge flux of edge j at this
@@ -803,7 +891,9 @@ __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
         }
       }
 #pragma unroll
+      V<KV> lk[NS];
       for (int i = 0; i < NS; ++i) {
+        lk[i] = splat<KV>(0.f);
         if (!in[i]) continue;
         const unsigned k = kk[i];
         const int z = (int)k + 1;
@@ -814,7 +904,37 @@ __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
           const float ra = hn / hnn, rb = fdv(dt, av * hnn);  // ra IEEE: exactly 1 for an unchanged layer
           l = fmas(add(l, sub(sFlo[k], sFlo[k + 1])), rb, muls(tn, ra));
         }
-        st<KV>(lo, n * LZ + k, l);
+        if (WSPLIT && NS == 2 && a.wsplit_fused) lk[i] = l;
+        else st<KV>(lo, n * LZ + k, l);
+      }
+      if constexpr (WSPLIT && NS == 2) {
+        if (a.wsplit_fused) {
+          // w_split: the implicit vertical step on the column just formed (one
+          // pass holds all of it: at most 64 layers), by cyclic reduction
+          const int k0 = nzmin - 1, k1 = nzmax - 2;
+          float ac[2], bc[2], cc[2];
+          V<KV> dv[2];
+          bool act[2];
+#pragma unroll
+          for (int r = 0; r < 2; ++r) {
+            const int k = (int)base + lane + kW * r;
+            act[r] = k >= k0 && k <= k1;
+            const int kq = act[r] ? k : k0, kq1 = kq < k1 ? kq + 1 : kq;
+            float A_, B_, C_;
+            vimpl_row(kq, k0, k1, a.wi[n * LW + kq], a.wi[n * LW + kq1], sA[kq], sA[kq1], avv[r], hnnv[r], dt, A_,
+                      B_, C_);
+            ac[r] = act[r] ? A_ : 0.f;
+            bc[r] = act[r] ? B_ : 1.f;
+            cc[r] = act[r] ? C_ : 0.f;
+            dv[r] = act[r] ? muls(lk[r], hnnv[r]) : splat<KV>(0.f);
+          }
+          pcr_solve2<KV>(ac, bc, cc, dv, lane);
+#pragma unroll
+          for (int r = 0; r < 2; ++r) {
+            const unsigned k = base + lane + kW * r;
+            if (k < LZ) st<KV>(lo, n * LZ + k, act[r] ? dv[r] : lk[r]);
+          }
+        }
       }
     }
     __syncwarp();
@@ -957,13 +1077,6 @@ __global__ void __launch_bounds__(128, (NS == 1 ? 10 : 7)) kf_ratio(DMesh m, Fas
 // from neighbouring lanes by shuffles and the kernel needs no shared memory;
 // the edge and cluster lists are read through L1. Fewer resources per warp,
 // more resident warps.
-template <int KV>
-__device__ __forceinline__ V<KV> shfl_v(const V<KV>& x, int src) {
-  V<KV> r;
-#pragma unroll
-  for (int t = 0; t < KV; ++t) r.v[t] = __shfl_sync(0xffffffffu, x.v[t], src);
-  return r;
-}
 
 // LEAN: fewer registers (64, one cluster node in flight) for more resident warps.
 template <int KV, bool LEAN>
@@ -1455,35 +1568,6 @@ __global__ void __launch_bounds__(kVimplWarpsF * kW) kf_vert_impl(DMesh m, FastP
 // rows outside the column being identity rows (a = c = d = 0, b = 1); after
 // the last step D is the solution.
 template <int KV>
-struct PcrRow {
-  float A, C;
-  V<KV> D;
-};
-
-template <int KV>
-__device__ __forceinline__ PcrRow<KV> pcr_shfl(const PcrRow<KV>& r, int src) {
-  return PcrRow<KV>{__shfl_sync(0xffffffffu, r.A, src), __shfl_sync(0xffffffffu, r.C, src), shfl_v<KV>(r.D, src)};
-}
-
-template <int KV>
-__device__ __forceinline__ void pcr_update(float& a, float& b, float& c, V<KV>& d, PcrRow<KV>& row, bool hm,
-                                           const PcrRow<KV>& m, bool hp, const PcrRow<KV>& p) {
-  const float Am = hm ? m.A : 0.f, Cm = hm ? m.C : 0.f, Ap = hp ? p.A : 0.f, Cp = hp ? p.C : 0.f;
-  const float na = -a, nc = -c;
-  b = fmaf(nc, Ap, fmaf(na, Cm, b));
-  V<KV> dd = d;
-  if (hm) dd = fmas(m.D, na, dd);
-  if (hp) dd = fmas(p.D, nc, dd);
-  d = dd;
-  a = na * Am;
-  c = nc * Cp;
-  const float rb = fdv(1.f, b);
-  row.A = a * rb;
-  row.C = c * rb;
-  row.D = muls(d, rb);
-}
-
-template <int KV>
 __global__ void __launch_bounds__(256) kf_vert_pcr(DMesh m, FastPtrs a) {
   const int lane = threadIdx.x & (kW - 1);
   const int n = blockIdx.x * (blockDim.x / kW) + threadIdx.x / kW;
@@ -1491,8 +1575,7 @@ __global__ void __launch_bounds__(256) kf_vert_pcr(DMesh m, FastPtrs a) {
   const unsigned LZ = m.LZ, LW = m.LW;
   const int k0 = m.ulev[n] - 1, k1 = m.nlev[n] - 2;
   const GeoPtrs<float>& g = m.g32;
-  const float dt = a.dt;
-  // coefficients of rows lane and lane + 32 (lib/oce_adv_tra_ver.F90:158-190)
+  // coefficients of rows lane and lane + 32 (rows outside the column: identity)
   float a0[2], b0[2], c0[2], hn[2];
   bool act[2];
 #pragma unroll
@@ -1502,56 +1585,25 @@ __global__ void __launch_bounds__(256) kf_vert_pcr(DMesh m, FastPtrs a) {
     const int kk = act[r] ? k : k0;
     const unsigned iw = (unsigned)n * LW + kk, iz = (unsigned)n * LZ + kk;
     const unsigned iw1 = iw + (kk < k1 ? 1u : 0u);
-    const float W0 = a.wi[iw], W1 = a.wi[iw1], ar0 = g.area[iw], ar1 = g.area[iw1];
-    const float rav = fdv(dt, g.areasvol[iz]), hnn = g.hnode_new[iz];
-    const float v0 = ar0 * rav, v1 = ar1 * rav;
-    float ak = kk == k0 ? 0.f : fminf(W0, 0.f) * v0;
-    float bk = hnn + (kk == k0 ? W0 : fmaxf(W0, 0.f)) * v0, ck = 0.f;
-    if (kk != k1) {
-      bk -= fminf(W1, 0.f) * v1;
-      ck = -fmaxf(W1, 0.f) * v1;
-    }
+    float ak, bk, ck;
+    vimpl_row(kk, k0, k1, a.wi[iw], a.wi[iw1], g.area[iw], g.area[iw1], g.areasvol[iz], g.hnode_new[iz], a.dt, ak,
+              bk, ck);
     a0[r] = act[r] ? ak : 0.f;
     b0[r] = act[r] ? bk : 1.f;
     c0[r] = act[r] ? ck : 0.f;
-    hn[r] = act[r] ? hnn : 0.f;
+    hn[r] = act[r] ? g.hnode_new[iz] : 0.f;
   }
   for (int gi = 0; gi < a.G; ++gi) {
     float* __restrict__ lo = a.lo + gi * a.gN;
-    float av[2], bv[2], cv[2];
+    float av[2] = {a0[0], a0[1]}, bv[2] = {b0[0], b0[1]}, cv[2] = {c0[0], c0[1]};
     V<KV> dv[2];
-    PcrRow<KV> row[2];
-#pragma unroll
-    for (int r = 0; r < 2; ++r) {
-      const unsigned k = lane + kW * r;
-      dv[r] = act[r] ? muls(ld<KV>(lo, (unsigned)n * LZ + k), hn[r]) : splat<KV>(0.f);
-      av[r] = a0[r];
-      bv[r] = b0[r];
-      cv[r] = c0[r];
-      const float rb = fdv(1.f, bv[r]);
-      row[r] = PcrRow<KV>{av[r] * rb, cv[r] * rb, muls(dv[r], rb)};
-    }
-#pragma unroll
-    for (int h = 1; h < kW; h *= 2) {
-      const int sm = (lane - h) & (kW - 1), sp = (lane + h) & (kW - 1);
-      const PcrRow<KV> m0 = pcr_shfl(row[0], sm), m1 = pcr_shfl(row[1], sm);
-      const PcrRow<KV> p0 = pcr_shfl(row[0], sp), p1 = pcr_shfl(row[1], sp);
-      const bool lo_in = lane >= h, hi_in = lane + h < kW;
-      // row lane: k - h from lane - h (row 0) if lane >= h; k + h from lane + h
-      // (row 0) or, past 31, from lane + h - 32 (row 1)
-      pcr_update(av[0], bv[0], cv[0], dv[0], row[0], lo_in, m0, true, hi_in ? p0 : p1);
-      // row lane + 32: k - h from lane - h (row 1) or lane - h + 32 (row 0);
-      // k + h from lane + h (row 1) while below 64
-      pcr_update(av[1], bv[1], cv[1], dv[1], row[1], true, lo_in ? m1 : m0, hi_in, p1);
-    }
-    {  // h = 32: the two rows of a lane couple to each other
-      const PcrRow<KV> r0 = row[0], r1 = row[1];
-      pcr_update(av[0], bv[0], cv[0], dv[0], row[0], false, r0, true, r1);
-      pcr_update(av[1], bv[1], cv[1], dv[1], row[1], true, r0, false, r1);
-    }
 #pragma unroll
     for (int r = 0; r < 2; ++r)
-      if (act[r]) st<KV>(lo, (unsigned)n * LZ + lane + kW * r, row[r].D);
+      dv[r] = act[r] ? muls(ld<KV>(lo, (unsigned)n * LZ + lane + kW * r), hn[r]) : splat<KV>(0.f);
+    pcr_solve2<KV>(av, bv, cv, dv, lane);
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+      if (act[r]) st<KV>(lo, (unsigned)n * LZ + lane + kW * r, dv[r]);
   }
 }
 

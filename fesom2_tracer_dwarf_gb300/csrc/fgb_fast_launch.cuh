@@ -110,15 +110,18 @@ int launch_fast(const DMesh& m, const FastPtrs& a, const LaunchArgs& L, cudaStre
   }
   if (L.fct) {
     if (L.mask & FGB_STAGE_LO) {
+      FastPtrs al = a;
+      al.wsplit_fused = a.wi && L.ns_lo == 2 && m.LZ <= 2 * kW && !L.vimpl_thomas;
       switch (L.ver) {
-        case FGB_VER_QR4C: launch_lo_ns<KV, 1>(m, a, L, s); break;
-        case FGB_VER_CDIFF: launch_lo_ns<KV, 2>(m, a, L, s); break;
-        case FGB_VER_PPM: launch_lo_ns<KV, 3>(m, a, L, s); break;
-        default: launch_lo_ns<KV, 0>(m, a, L, s); break;
+        case FGB_VER_QR4C: launch_lo_ns<KV, 1>(m, al, L, s); break;
+        case FGB_VER_CDIFF: launch_lo_ns<KV, 2>(m, al, L, s); break;
+        case FGB_VER_PPM: launch_lo_ns<KV, 3>(m, al, L, s); break;
+        default: launch_lo_ns<KV, 0>(m, al, L, s); break;
       }
       ++launches;
-      if (a.wi) {
-        // w_split: the implicit vertical step on the LO solution
+      if (a.wi && !(L.ns_lo == 2 && m.LZ <= 2 * kW && !L.vimpl_thomas)) {
+        // w_split: the implicit vertical step on the LO solution (unless the
+        // LO kernel solved it in the same pass)
         if (m.LZ <= 2 * kW && !L.vimpl_thomas) {
           kf_vert_pcr<KV><<<(m.N + 7) / 8, 8 * kW, 0, s>>>(m, a);
         } else {
