@@ -427,7 +427,11 @@ __global__ void k_stats_partial(const R* __restrict__ T, long long sT, int KV, i
   for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
     const long long n = i / nz, k = i - n * nz;
     const double v = (double)base[(n * LZ + k) * KV];
-    if (v != v) { nan += 1.0; continue; }
+    if (v != v) {  // counted; the sum turns NaN as the reference's sum(dble(values)) does
+      nan += 1.0;
+      sm += v;
+      continue;
+    }
     mn = fmin(mn, v);
     mx = fmax(mx, v);
     sm += v;

@@ -236,7 +236,8 @@ int fgb_adv_step(const fgb_mesh* m, const fgb_step_desc* d, void* stream);
 int fgb_adv_stages(const fgb_mesh* m, const fgb_step_desc* d, int stage_mask, void* stream);
 
 /* Min, max, plain sum (FP64) and NaN count of values (K,N,LZ) over the
- * first nz layers of every node (src/fesom_analytic.F90:441-445): out_dev
+ * first nz layers of every node (src/fesom_analytic.F90:441-445; min and max
+ * skip NaN, the sum is NaN when a value is): out_dev
  * receives 4 doubles per tracer; scratch of fgb_stats_scratch_bytes. */
 long long fgb_stats_scratch_bytes(const fgb_mesh* m, int ntracers);
 int fgb_tracer_stats(const fgb_mesh* m, int precision, const void* T, long long strideT, int ntracers,

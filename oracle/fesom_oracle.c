@@ -1511,7 +1511,7 @@ void om_stats(const omesh* m, const double* values, double* out) {
   long nan = 0;
   for (size_t i = 0; i < cnt; ++i) {
     double v = values[i];
-    if (v != v) { nan++; continue; }
+    if (v != v) { nan++; sm = sm + v; continue; } /* minval/maxval skip NaN; sum(dble()) turns NaN */
     if (v < mn) mn = v;
     if (v > mx) mx = v;
     sm = sm + v;

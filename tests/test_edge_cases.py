@@ -1,0 +1,115 @@
+"""Edge cases of the step: the smallest analytic meshes (boundary edges without
+triangles, every node on a wall), one-layer columns (UPW1 / CDIFF; QR4C and PPM
+are refused), a single tracer, and the statistics with NaN values (min and max
+skip NaN, the sum turns NaN, as src/fesom_analytic.F90:441-445 computes them).
+"""
+import itertools
+import zlib
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+SMALLEST = {
+    "closed_2x2": dict(nx=2, ny=2, nl=3, periodic=False),
+    "periodic_3x3": dict(nx=3, ny=3, nl=3, periodic=True),
+}
+
+
+def _one_layer_kw(nx=9, ny=8, nl=6):
+    from fesom2_tracer_dwarf_gb300 import synthetic
+
+    zb = synthetic.stretched_zbar(nl - 1, 5.0, 120.0)
+    en = np.full(2 * (nx - 1) * (ny - 1), nl, dtype=np.int32)
+    en[:20] = 2  # one-layer elements: their nodes' columns have one layer
+    return dict(nx=nx, ny=ny, nl=nl, periodic=False, zbar=zb, elem_nlev=en)
+
+
+def test_oracle_stats_with_nan(oracle_mod):
+    om = oracle_mod.Mesh(5, 5, 4, periodic=False)
+    v = np.arange(om.nod2D * (om.nl - 1), dtype=np.float64).reshape(om.nod2D, om.nl - 1) + 1.0
+    v[2, 1] = np.nan
+    mn, mx, sm, nan = om.stats(v)
+    assert mn == 1.0 and mx == v.size and np.isnan(sm) and nan == 1
+
+
+def _gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA GPU")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("meshname", ["closed_2x2", "periodic_3x3", "one_layer"])
+@pytest.mark.parametrize("hor,ver,lim", list(itertools.product(["UPW1", "MUSCL", "MFCT"], ["UPW1", "CDIFF"],
+                                                                ["NONE", "FCT"])))
+def test_small_and_one_layer_meshes(oracle_mod, meshname, hor, ver, lim):
+    _gpu()
+    from fesom2_tracer_dwarf_gb300 import engine, synthetic
+    from fesom2_tracer_dwarf_gb300.mesh import Mesh
+
+    O = oracle_mod
+    kw = _one_layer_kw() if meshname == "one_layer" else SMALLEST[meshname]
+    om, m = O.Mesh(**kw), Mesh(**kw)
+    rng = np.random.default_rng(zlib.crc32(f"edge/{meshname}/{hor}/{ver}/{lim}".encode()))
+    vel, w = synthetic.random_flow(m, rng)
+    T = synthetic.random_field(m, rng, 2)
+    dt = 300.0
+    sch = (hor, ver, lim, 0.7, 0.6)
+    vals, vab = np.ascontiguousarray(T.copy()), np.ascontiguousarray(T.copy())
+    W = O.Work(om)
+    for _ in range(3):
+        O.analytic_step(om, W, dt, vel, w, vals, vab, [sch] * 2, copy_ab=True)
+    for precision in ("fp64", "fp32"):
+        eng = engine.TracerAdvection(m, 2, precision, hor, ver, lim, ph=0.7, pv=0.6, copy_ab=True)
+        eng.set_tracers(T)
+        eng.set_velocity(vel, w)
+        eng.step(dt, 3)
+        torch.cuda.synchronize()
+        got = eng.values()
+        if precision == "fp64":
+            assert np.array_equal(got, vals), f"max |diff| {np.abs(got - vals).max()}"
+        else:
+            assert np.abs(got - vals).max() <= 1e-5 * max(1.0, np.abs(vals).max())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ver", ["QR4C", "PPM"])
+def test_one_layer_columns_refused_by_qr4c_ppm(ver):
+    _gpu()
+    from fesom2_tracer_dwarf_gb300 import engine, synthetic
+    from fesom2_tracer_dwarf_gb300.mesh import Mesh
+
+    m = Mesh(**_one_layer_kw())
+    rng = np.random.default_rng(3)
+    vel, w = synthetic.random_flow(m, rng)
+    for precision in ("fp64", "fp32"):
+        eng = engine.TracerAdvection(m, 1, precision, "UPW1", ver, "FCT")
+        eng.set_tracers(synthetic.random_field(m, rng, 1))
+        eng.set_velocity(vel, w)
+        with pytest.raises(RuntimeError, match="two layers"):
+            eng.step(300.0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,V", [("fp64", 1), ("fp32", 4), ("fp32", 1)])
+def test_stats_with_nan(oracle_mod, precision, V):
+    _gpu()
+    from fesom2_tracer_dwarf_gb300 import engine, synthetic
+    from fesom2_tracer_dwarf_gb300.mesh import Mesh
+
+    kw = dict(nx=9, ny=8, nl=6, periodic=True)
+    om, m = oracle_mod.Mesh(**kw), Mesh(**kw)
+    T = synthetic.random_field(m, np.random.default_rng(4), 4)
+    T[1, 3, 2] = np.nan
+    T[1, 7, 0] = np.nan
+    eng = engine.TracerAdvection(m, 4, precision, tracer_vec=V)
+    eng.set_tracers(T)
+    st = eng.stats()
+    for t in range(4):
+        ref = om.stats(np.ascontiguousarray(eng.values()[t]))
+        assert st[t, 0] == ref[0] and st[t, 1] == ref[1] and st[t, 3] == ref[3]
+        if t == 1:
+            assert np.isnan(st[t, 2]) and st[t, 3] == 2
+        else:
+            assert abs(st[t, 2] - ref[2]) <= 1e-12 * abs(ref[2])
