@@ -96,3 +96,18 @@ def test_dwarf_driver_golden_and_scalars(tmp_path):
     assert np.array_equal(raw[0], analytic.dwarf_fields(Mesh(20, 20, 10, periodic=True, upload=False))[0])
     assert abs(raw[-1].sum() - rows[-1][2]) <= 1e-9 * abs(rows[-1][2])
     assert os.path.exists(tmp_path / "coord_nod2D.bin")
+
+
+@pytest.mark.gpu
+def test_dwarf_driver_fp32_form():
+    """The dwarf in the FP32 form: per-step min and max within FP32 rounding of
+    the FP64 run, the sum within 1e-8 relative (it drifts by a few 1e-10 over
+    10 steps: every value is rounded to FP32 each step)."""
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA GPU")
+    buf = io.StringIO()
+    r64 = analytic.run(20, 20, 10, periodic=True, out=buf)
+    r32 = analytic.run(20, 20, 10, periodic=True, precision="fp32", out=buf)
+    for a, b in zip(r32, r64):
+        assert abs(a[0] - b[0]) <= 2e-6 * abs(b[1]) and abs(a[1] - b[1]) <= 2e-6 * abs(b[1])
+        assert abs(a[2] - b[2]) <= 1e-8 * abs(b[2]) and a[3] == 0
