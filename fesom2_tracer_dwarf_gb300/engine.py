@@ -247,7 +247,7 @@ class TracerAdvection:
             _lib.check(L.fgb_adv_stages(self.mesh.handle, ctypes.byref(d), stages, stream), "fgb_adv_stages")
             self.launches += L.fgb_last_launch_count()
 
-    def run_host(self, host_in, host_out, dt: float, nsteps: int = 1):
+    def run_host(self, host_in, host_out, dt: float, nsteps: int = 1, copy_streams: int = 4):
         """Advance independent batches of tracer fields that live in host
         memory: batch i is copied to the device from ``host_in[i]``, advanced
         ``nsteps`` steps, and copied back into ``host_out[i]`` (tensors of
@@ -256,34 +256,45 @@ class TracerAdvection:
 
         Three device buffers take turns as the field being stepped, the next
         batch arriving and the previous batch leaving, so the host-to-device
-        copy of batch i+1 and the device-to-host copy of batch i-1 run on two
-        copy streams while batch i steps on the current stream. Needs a
-        copy-AB engine (valuesAB follows the values). Returns on the host
-        when every copy of every batch has been issued; synchronise the device
+        copy of batch i+1 and the device-to-host copy of batch i-1 run during
+        the steps of batch i on the current stream. Each copy is split into
+        ``copy_streams`` chunks on as many streams per direction (host-device
+        transfers in both directions at once run faster spread over several
+        streams). Needs a copy-AB engine (valuesAB follows the values). Returns
+        on the host when every copy has been issued; synchronise the device
         before reading ``host_out``."""
         if self.TA is not None:
             raise ValueError("run_host needs copy_ab=True (valuesAB follows the values)")
         nb = len(host_in)
         if len(host_out) != nb:
             raise ValueError("host_in and host_out need one tensor per batch")
+        nc = max(1, int(copy_streams))
         main = torch.cuda.current_stream(self.device)
-        if not hasattr(self, "_host_bufs"):
-            self._host_bufs = [self.T] + [torch.empty_like(self.T) for _ in range(2)]
-            self._h2d = torch.cuda.Stream(self.device)
-            self._d2h = torch.cuda.Stream(self.device)
+        if getattr(self, "_host_nc", None) != nc:
+            if not hasattr(self, "_host_bufs"):
+                self._host_bufs = [self.T] + [torch.empty_like(self.T) for _ in range(2)]
+            self._h2d = [torch.cuda.Stream(self.device) for _ in range(nc)]
+            self._d2h = [torch.cuda.Stream(self.device) for _ in range(nc)]
+            self._host_nc = nc
         bufs = self._host_bufs
-        free = [torch.cuda.Event() for _ in range(3)]     # buffer no longer read by a D2H copy
-        arrived = [torch.cuda.Event() for _ in range(3)]  # H2D copy into the buffer done
-        stepped = [torch.cuda.Event() for _ in range(3)]  # steps on the buffer done
+        numel = bufs[0].numel()
+        bounds = [(c * numel) // nc for c in range(nc + 1)]
+        free = [[torch.cuda.Event() for _ in range(nc)] for _ in range(3)]     # chunk no longer read by D2H
+        arrived = [[torch.cuda.Event() for _ in range(nc)] for _ in range(3)]  # chunk copied in
+        stepped = [torch.cuda.Event() for _ in range(3)]                        # steps on the buffer done
         for b in range(3):
-            free[b].record(main)
+            for c in range(nc):
+                free[b][c].record(main)
 
         def load(i):
             b = i % 3
-            with torch.cuda.stream(self._h2d):
-                self._h2d.wait_event(free[b])
-                bufs[b].copy_(host_in[i], non_blocking=True)
-                arrived[b].record(self._h2d)
+            src, dst = host_in[i].view(-1), bufs[b].view(-1)
+            for c in range(nc):
+                st = self._h2d[c]
+                with torch.cuda.stream(st):
+                    st.wait_event(free[b][c])
+                    dst[bounds[c]:bounds[c + 1]].copy_(src[bounds[c]:bounds[c + 1]], non_blocking=True)
+                    arrived[b][c].record(st)
 
         if nb:
             load(0)
@@ -291,16 +302,21 @@ class TracerAdvection:
             b = i % 3
             if i + 1 < nb:
                 load(i + 1)
-            main.wait_event(arrived[b])
+            for c in range(nc):
+                main.wait_event(arrived[b][c])
             self.T = bufs[b]
             self.step(dt, nsteps)
             stepped[b].record(main)
-            with torch.cuda.stream(self._d2h):
-                self._d2h.wait_event(stepped[b])
-                host_out[i].copy_(bufs[b], non_blocking=True)
-                free[b].record(self._d2h)
+            src, dst = bufs[b].view(-1), host_out[i].view(-1)
+            for c in range(nc):
+                st = self._d2h[c]
+                with torch.cuda.stream(st):
+                    st.wait_event(stepped[b])
+                    dst[bounds[c]:bounds[c + 1]].copy_(src[bounds[c]:bounds[c + 1]], non_blocking=True)
+                    free[b][c].record(st)
         for b in range(3):
-            main.wait_event(free[b])
+            for c in range(nc):
+                main.wait_event(free[b][c])
         return host_out
 
     def capture(self, dt: float, nsteps: int = 1):
