@@ -551,8 +551,9 @@ def run_gpu(args):
         result["fp32_over_fp64"] = value / result["fp64"]["value"]
         if cfg.get("report_steps"):
             result["precision_report"] = precision_report(m, eng, T0, e64, T64, cfg["dt"], cfg["report_steps"])
-            # the same with the FP32 form storing anomalies about each tracer's initial mean
-            eng._offsets_req = "mean"
+            # the same with the FP32 form storing anomalies about each tracer's initial mean where that
+            # shrinks the stored values (offsets="auto"; the passive blobs touch zero and keep offset 0)
+            eng._offsets_req = "auto"
             eng.load_padded(T=e64.from_layout(T64).clone())
             result["precision_report_anomaly"] = precision_report(m, eng, eng.T.clone(), e64, T64, cfg["dt"],
                                                                   cfg["report_steps"])

@@ -890,8 +890,8 @@ __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
           acc[i] = fmas(to[i], coj, acc[i]);
         }
       }
-#pragma unroll
       V<KV> lk[NS];
+#pragma unroll
       for (int i = 0; i < NS; ++i) {
         lk[i] = splat<KV>(0.f);
         if (!in[i]) continue;

@@ -430,30 +430,41 @@ __device__ __forceinline__ R ppm_tv(const Col<R>& c, int z, int nzmin, int nzmax
   return T[nzmin - 1];
 }
 
-// PPM flux contribution of layer nz to its interface (upper: W(nz) > 0 side,
-// lower: W(nz+1) < 0 side), lib/oce_adv_tra_ver.F90:598-632.
+// The tracer part of ppm_layer for a given x = min(|W| dt / h, 1) of the layer.
 template <typename R>
-__device__ __forceinline__ R ppm_layer(const Col<R>& c, int nz, bool upper, R dt) {
-  R aL = c.tv[nz - 1], aR = c.tv[nz];
-  const R T0 = c.T[nz - 1];
+__device__ __forceinline__ R ppm_layer_x(R aL, R aR, R T0, R x, bool upper, R area, R W) {
   if ((aR - T0) * (T0 - aL) <= R(0)) {
     aL = T0;
     aR = T0;
   }
   if ((aR - aL) * (T0 - R(0.5) * (aL + aR)) > fdiv((aR - aL) * (aR - aL), R(6))) aL = R(3) * T0 - R(2) * aR;
   if ((aR - aL) * (T0 - R(0.5) * (aR + aL)) < -fdiv((aR - aL) * (aR - aL), R(6))) aR = R(3) * T0 - R(2) * aL;
-  const R dzj = c.hn[nz - 1];
   const R aj = R(6) * (T0 - R(0.5) * (aL + aR));
   if (upper) {
-    const R W = c.W[nz - 1];
-    const R x = rmin(fdiv(W * dt, dzj), R(1));
     R tv = -aL - (R(0.5) * x) * ((aR - aL) + (R(1) - fdiv(R(2), R(3)) * x) * aj);
-    return (tv * c.area[nz - 1]) * W;
+    return (tv * area) * W;
+  }
+  R tv = -aR + (R(0.5) * x) * ((aR - aL) - (R(1) - fdiv(R(2), R(3)) * x) * aj);
+  return (tv * area) * W;
+}
+
+// x of ppm_layer: upper side min(W dt / h, 1), lower side min(-(W dt / h), 1).
+template <typename R>
+__device__ __forceinline__ R ppm_x(R W, R dt, R dzj, bool upper) {
+  return upper ? rmin(fdiv(W * dt, dzj), R(1)) : rmin(-fdiv(W * dt, dzj), R(1));
+}
+
+// PPM flux contribution of layer nz to its interface (upper: W(nz) > 0 side,
+// lower: W(nz+1) < 0 side), lib/oce_adv_tra_ver.F90:598-632.
+template <typename R>
+__device__ __forceinline__ R ppm_layer(const Col<R>& c, int nz, bool upper, R dt) {
+  const R dzj = c.hn[nz - 1];
+  if (upper) {
+    const R W = c.W[nz - 1];
+    return ppm_layer_x(c.tv[nz - 1], c.tv[nz], c.T[nz - 1], ppm_x(W, dt, dzj, true), true, c.area[nz - 1], W);
   }
   const R W = c.W[nz];
-  const R x = rmin(-fdiv(W * dt, dzj), R(1));
-  R tv = -aR + (R(0.5) * x) * ((aR - aL) - (R(1) - fdiv(R(2), R(3)) * x) * aj);
-  return (tv * c.area[nz]) * W;
+  return ppm_layer_x(c.tv[nz - 1], c.tv[nz], c.T[nz - 1], ppm_x(W, dt, dzj, false), false, c.area[nz], W);
 }
 
 template <typename R>
@@ -507,6 +518,95 @@ __device__ __forceinline__ void column_ver_flux(Col<R>& c, R* tvbuf, const R* fo
     const int z = iz + 1;
     const R f0 = fold ? fold[iz] : R(0);
     out[iz] = (z >= nzmin && z <= nzmax) ? ver_flux<R, VER>(c, z, nzmin, nzmax, num_ord, dt, f0) : f0;
+  }
+  __syncwarp();
+}
+
+// PPM vertical HO fluxes of KC tracer columns of one node (column_ver_flux
+// with VER = 3 for each tracer), with the geometry-only divisions of the edge
+// values and of x done once per interface instead of once per tracer: the
+// same operations on the same operands, so the results are bit-identical.
+// T, tv, fold and out hold KC columns LW apart; fold == out is allowed.
+template <typename R, int KC>
+__device__ __forceinline__ void column_ppm_multi(const Col<R>& g, const R* T, R* tv, const R* fold, R* out, int LW,
+                                                 int nl, int nzmin, int nzmax, R dt, int lane) {
+  const R* hnn = g.hnn;
+  for (int iz = lane; iz < nl; iz += kWarp) {
+    const int z = iz + 1;
+    if (z < nzmin || z > nzmax) {
+#pragma unroll
+      for (int i = 0; i < KC; ++i) tv[i * LW + iz] = R(0);
+      continue;
+    }
+    if (z >= nzmin + 2 && z <= nzmax - 2) {
+      const int nz = z - 1;
+      const R dzjm1 = hnn[nz - 2], dzj = hnn[nz - 1], dzjp1 = hnn[nz], dzjp2 = hnn[nz + 1];
+      const R ga = fdiv(dzj, dzjm1 + dzj + dzjp1);
+      const R gb = fdiv(R(2) * dzjm1 + dzj, dzjp1 + dzj), gc = fdiv(dzj + R(2) * dzjp1, dzjm1 + dzj);
+      const R gd = fdiv(dzjp1, dzj + dzjp1 + dzjp2);
+      const R ge = fdiv(R(2) * dzj + dzjp1, dzjp2 + dzjp1), gf = fdiv(dzjp1 + R(2) * dzjp2, dzj + dzjp1);
+      const R gh = fdiv((R(2) * dzjp1) * dzj, dzj + dzjp1) *
+                   (fdiv(dzjm1 + dzj, R(2) * dzj + dzjp1) - fdiv(dzjp2 + dzjp1, R(2) * dzjp1 + dzj));
+      const R gi = fdiv(dzj * (dzjm1 + dzj), R(2) * dzj + dzjp1);
+      const R gj = fdiv(dzjp1 * (dzjp1 + dzjp2), dzj + R(2) * dzjp1);
+      const R gk = fdiv(dzj, dzj + dzjp1), gl = fdiv(R(1), dzjm1 + dzj + dzjp1 + dzjp2);
+#pragma unroll
+      for (int i = 0; i < KC; ++i) {
+        const R* Ti = T + i * LW;
+        const R Tm = Ti[nz - 2], T0 = Ti[nz - 1], Tp = Ti[nz], Tpp = Ti[nz + 1];
+        R deltaj = ga * (gb * (Tp - T0) + gc * (T0 - Tm));
+        R deltajp1 = gd * (ge * (Tpp - Tp) + gf * (Tp - T0));
+        if ((Tp - T0) * (T0 - Tm) > R(0))
+          deltaj = rmin(rmin(rabs(deltaj), R(2) * rabs(Tp - T0)), R(2) * rabs(T0 - Tm)) * copysign(R(1), deltaj);
+        else
+          deltaj = R(0);
+        if ((Tpp - Tp) * (Tp - T0) > R(0))
+          deltajp1 = rmin(rmin(rabs(deltajp1), R(2) * rabs(Tpp - Tp)), R(2) * rabs(Tp - T0)) * copysign(R(1), deltajp1);
+        else
+          deltajp1 = R(0);
+        const R inner1 = gh * (Tp - T0);
+        const R inner2 = gi * deltajp1;
+        const R inner3 = gj * deltaj;
+        tv[i * LW + iz] = (T0 + gk * (Tp - T0)) + gl * (inner1 - inner2 + inner3);
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < KC; ++i) {
+        const Col<R> ci{T + i * LW, g.W, g.area, g.hn, g.hnn, g.Z, g.zb, nullptr};
+        tv[i * LW + iz] = ppm_tv(ci, z, nzmin, nzmax);
+      }
+    }
+  }
+  __syncwarp();
+  for (int iz = lane; iz < nl; iz += kWarp) {
+    const int z = iz + 1;
+    R f0[KC];
+#pragma unroll
+    for (int i = 0; i < KC; ++i) f0[i] = fold ? fold[i * LW + iz] : R(0);
+    if (z < nzmin || z > nzmax) {
+#pragma unroll
+      for (int i = 0; i < KC; ++i) out[i * LW + iz] = f0[i];
+      continue;
+    }
+    if (z == nzmin) {
+#pragma unroll
+      for (int i = 0; i < KC; ++i)
+        out[i * LW + iz] = -((tv[i * LW + nzmin - 1] * g.W[nzmin - 1]) * g.area[nzmin - 1]) - f0[i];
+      continue;
+    }
+    const R W = g.W[z - 1];
+    if (z < nzmax && W != R(0)) {
+      const bool up = W > R(0);
+      const int L = up ? z : z - 1;  // the layer whose parabola crosses the interface
+      const R x = ppm_x(W, dt, g.hn[L - 1], up);
+#pragma unroll
+      for (int i = 0; i < KC; ++i)
+        out[i * LW + iz] =
+            ppm_layer_x(tv[i * LW + L - 1], tv[i * LW + L], T[i * LW + L - 1], x, up, g.area[z - 1], W) - f0[i];
+    } else {
+#pragma unroll
+      for (int i = 0; i < KC; ++i) out[i * LW + iz] = R(0) - f0[i];
+    }
   }
   __syncwarp();
 }
@@ -655,9 +755,15 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_fct_lo(DMesh 
       }
     }
     // HO vertical flux on T_AB with w; adf_v = HO - LO ("X - flux").
+    if constexpr (VER == 3) {
+      const Col<R> g{nullptr, sW, sA, sHn, sHnn, sZ, sX, nullptr};
+      column_ppm_multi<R, KC>(g, ta_sep ? sTA : sT, sTv, sFv, sFv, (int)LW, nl, nzmin, nzmax, dt, lane);
+    }
     for (int i = 0; i < KC; ++i) {
-      Col<R> cho{(ta_sep ? sTA : sT) + i * LW, sW, sA, sHn, sHnn, sZ, sX, nullptr};
-      column_ver_flux<R, VER>(cho, sTv + i * LW, sFv + i * LW, sFv + i * LW, nl, nzmin, nzmax, a.pv, dt, lane);
+      if constexpr (VER != 3) {
+        Col<R> cho{(ta_sep ? sTA : sT) + i * LW, sW, sA, sHn, sHnn, sZ, sX, nullptr};
+        column_ver_flux<R, VER>(cho, sTv + i * LW, sFv + i * LW, sFv + i * LW, nl, nzmin, nzmax, a.pv, dt, lane);
+      }
       R* __restrict__ adfv = a.adfv + (t0 + i) * a.sW + n * LW;
       for (int iz = lane; iz < (int)LW; iz += kWarp) adfv[iz] = iz < nl ? sFv[i * LW + iz] : R(0);
     }
@@ -965,9 +1071,14 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_nofct_update(
 #pragma unroll
     for (int i = 0; i < KC; ++i) stage(sTA + i * LW, a.TA + (t0 + i) * a.sTA + n * LZ, nz, lane);
     __syncwarp();
-    for (int i = 0; i < KC; ++i) {
-      Col<R> c{sTA + i * LW, sW, sA, sHn, sHnn, sZ, sX, nullptr};
-      column_ver_flux<R, VER>(c, sTv + i * LW, nullptr, sF + i * LW, nl, nzmin, nzmax, a.pv, dt, lane);
+    if constexpr (VER == 3) {
+      const Col<R> gc{nullptr, sW, sA, sHn, sHnn, sZ, sX, nullptr};
+      column_ppm_multi<R, KC>(gc, sTA, sTv, nullptr, sF, (int)LW, nl, nzmin, nzmax, dt, lane);
+    } else {
+      for (int i = 0; i < KC; ++i) {
+        Col<R> c{sTA + i * LW, sW, sA, sHn, sHnn, sZ, sX, nullptr};
+        column_ver_flux<R, VER>(c, sTv + i * LW, nullptr, sF + i * LW, nl, nzmin, nzmax, a.pv, dt, lane);
+      }
     }
     for (int p = lane; 2 * p < m.LZ; p += kWarp) {
       const int k0 = 2 * p, z0 = k0 + 1, z1 = k0 + 2;

@@ -17,8 +17,11 @@ update stage writes for the next step (FESOM2's tracer AB2 with offset
 epsilon; the reference declares epsilon = 0.1 at lib/oce_modules.F90:75).
 
 Anomaly storage (``offsets``, opt-in, meant for the FP32 form): each tracer is
-stored as T - c_t for a per-tracer reference value c_t (given, or the mean of
-the initial values), and c_t is added back by ``values`` and ``stats``. Every
+stored as T - c_t for a per-tracer reference value c_t (given; "mean": the
+mean of the initial values; "auto": that mean only where it shrinks the stored
+magnitude at least fourfold, else 0, so that fields touching zero such as
+passive-tracer blobs keep exact zeros and stay non-negative), and c_t is added
+back by ``values`` and ``stats``. Every
 scheme of the step maps T + c to T' + c when a uniform field stays uniform,
 i.e. when the velocities satisfy the discrete continuity of the step (as the
 flows of the benchmark configurations do); then the stored anomalies advance
@@ -48,6 +51,20 @@ def _require_cuda():
         raise RuntimeError("fesom2_tracer_dwarf_gb300 needs a CUDA GPU; there is no CPU path")
 
 
+def anomaly_offsets(vals64, K, mode="mean"):
+    """Per-tracer reference values of anomaly storage from (K, ...) values.
+
+    "mean": each tracer's mean. "auto": the mean where max |T - mean| is at
+    most a quarter of max |T| (the stored anomalies are then at least four
+    times smaller than the values), else 0."""
+    t = torch.as_tensor(vals64, dtype=torch.float64).reshape(K, -1)
+    mean = t.mean(dim=1)
+    if mode == "auto":
+        spread = (t - mean[:, None]).abs().amax(dim=1)
+        mean = torch.where(spread <= 0.25 * t.abs().amax(dim=1), mean, torch.zeros_like(mean))
+    return mean.cpu().numpy()
+
+
 class TracerAdvection:
     def __init__(self, mesh: Mesh, ntracers: int, precision: str = "fp64", hor: str = "UPW1",
                  ver: str = "UPW1", lim: str = "NONE", ph: float = 1.0, pv: float = 1.0,
@@ -70,7 +87,10 @@ class TracerAdvection:
         self.set_schemes(hor, ver, lim, ph, pv)
         self.copy_ab = copy_ab
         self.ab2_eps = None if ab2_eps is None else float(ab2_eps)
-        if offsets is not None and not (isinstance(offsets, str) and offsets == "mean"):
+        if isinstance(offsets, str):
+            if offsets not in ("mean", "auto"):
+                raise ValueError('offsets must be None, "mean", "auto" or one value per tracer')
+        elif offsets is not None:
             offsets = np.asarray(offsets, dtype=np.float64).reshape(self.K)
         self._offsets_req = offsets
         self.offsets = None  # per-tracer reference values of the stored anomalies (resolved at set_tracers)
@@ -146,8 +166,7 @@ class TracerAdvection:
         if req is None:
             self.offsets = None
         elif isinstance(req, str):
-            t = torch.as_tensor(vals64, dtype=torch.float64)
-            self.offsets = t.reshape(self.K, -1).mean(dim=1).cpu().numpy()
+            self.offsets = anomaly_offsets(vals64, self.K, req)
         else:
             self.offsets = req
 

@@ -34,6 +34,23 @@ def test_oracle_stats_with_nan(oracle_mod):
     assert mn == 1.0 and mx == v.size and np.isnan(sm) and nan == 1
 
 
+def test_anomaly_offsets_rule():
+    """offsets="auto": the mean only where it shrinks the stored magnitude at
+    least fourfold; fields touching zero keep offset 0 (exact zeros)."""
+    from fesom2_tracer_dwarf_gb300.engine import anomaly_offsets
+
+    rng = np.random.default_rng(5)
+    S = 35.0 + 0.3 * rng.standard_normal((6, 5))
+    blob = np.zeros((6, 5))
+    blob[2:4, 1:3] = 1.0
+    T = 10.0 + 8.0 * rng.standard_normal((6, 5))  # spread comparable to the values
+    v = np.stack([S, blob, T])
+    mean = anomaly_offsets(v, 3, "mean")
+    assert np.allclose(mean, v.reshape(3, -1).mean(axis=1))
+    auto = anomaly_offsets(v, 3, "auto")
+    assert auto[0] == mean[0] and auto[1] == 0.0 and auto[2] == 0.0
+
+
 def _gpu():
     if not torch.cuda.is_available():
         pytest.skip("needs a CUDA GPU")
