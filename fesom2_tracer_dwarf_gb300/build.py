@@ -29,6 +29,7 @@ CXX_COMMON = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-fno-fast-math
 
 SOURCES = [
     ("fgb_hmesh.cpp", "cxx", []),
+    ("fgb_hmesh_files.cpp", "cxx", []),
     ("fgb_capi.cpp", "cxx", []),
     ("fgb_api.cu", "nvcc", []),
     ("fgb_step_f64.cu", "nvcc", ["-fmad=false"]),

@@ -141,6 +141,16 @@ int fgb_hmesh_analytic(int nx, int ny, int nl, double Lx, double Ly, double dept
   return 0;
 }
 
+int fgb_hmesh_from_files(const char* dir, int flags, fgb_hmesh** out) {
+  if (!out || !dir) { set_error("null argument"); return -1; }
+  if (flags & ~7) { set_error("unknown mesh-file flags"); return -1; }
+  std::string err;
+  HostMesh* m = build_from_files(dir, flags, &err);
+  if (!m) { set_error(err); return -1; }
+  *out = new fgb_hmesh{m};
+  return 0;
+}
+
 int fgb_hmesh_union(const fgb_hmesh* const* parts, int count, fgb_hmesh** out) {
   if (!parts || !out || count < 1) { set_error("bad argument"); return -1; }
   std::vector<const HostMesh*> ps(count);

@@ -13,7 +13,11 @@
 //  - valuesAB is set by tracer_set_values only (frozen time level);
 //  - tracer_set_thickness sets hnode_new only; tracer_init_ale_arrays sets
 //    hnode, hnode_new and helem from zbar.
-// Restart files and FESOM ASCII meshes are not read: those calls return -1.
+//  - tracer_load_mesh_from_files reads the FESOM mesh files of the directory
+//    as one partition (the reference reads dist_<npes>/ partition lists with
+//    MPI; a single-GPU library owns every node), with the reference's
+//    geometry defaults; a missing '/' at the end of the path is added.
+// Restart files are not read: tracer_load_mesh_partition returns -1.
 #include <cuda_runtime.h>
 #include <sys/stat.h>
 
@@ -158,7 +162,7 @@ int sync_values_to_host() {
 // Applies the caller's level and thickness arrays to the host mesh and
 // (re)creates the device mesh and buffers when needed.
 int prepare_device() {
-  if (!g.hmesh) return fail("no mesh: call tracer_generate_analytic_mesh first");
+  if (!g.hmesh) return fail("no mesh: call tracer_load_mesh_from_files or tracer_generate_analytic_mesh first");
   fgb::HostMesh& h = *g.hmesh->m;
   if (g.tr.empty()) return fail("no tracers: call tracer_allocate_tracers first");
   if (node_size() != h.N) return fail("partition size (myDim+eDim) does not match the mesh nodes");
@@ -463,8 +467,39 @@ int tracer_load_mesh_partition(const char* restart_dir) {
 }
 
 int tracer_load_mesh_from_files(const char* mesh_path) {
-  (void)mesh_path;
-  return fail("FESOM ASCII mesh reader not available in this library; use tracer_generate_analytic_mesh");
+  const std::string path = c2s(mesh_path);
+  std::printf("Loading mesh from partition files: %s\n", path.c_str());  // lib/tracer_c_interface.F90:849-851
+  fgb_hmesh* h = nullptr;
+  if (fgb_hmesh_from_files(path.c_str(), 0, &h)) return fail(fgb_last_error());
+  if (sync_values_to_host()) {
+    fgb_hmesh_free(h);
+    return -1;
+  }
+  free_device();
+  if (g.dmesh) fgb_mesh_free(g.dmesh);
+  if (g.hmesh) fgb_hmesh_free(g.hmesh);
+  g.dmesh = nullptr;
+  g.hmesh = h;
+  const fgb::HostMesh& m = *g.hmesh->m;
+  g.nl = m.nl;
+  g.nod2D = m.N;
+  g.edge2D = m.E;
+  g.elem2D = m.M;
+  g.myDim = m.N;
+  g.eDim = 0;
+  g.hnode = m.hnode;
+  g.hnode_new = m.hnode_new;
+  g.helem = m.helem;
+  g.have_hnode = g.have_hnode_new = g.have_helem = false;
+  g.set_nlev.clear();
+  g.set_ulev.clear();
+  g.initialized = true;  // :856-857
+  g.mesh_dirty = g.inputs_dirty = true;
+  std::printf("Mesh loaded successfully from partition files\n");
+  std::printf("  Mesh: nl=%8d, nod2D=%8d, edge2D=%8d\n", m.nl, m.N, m.E);
+  std::printf("  Partition: myDim=%8d, eDim=%8d\n", m.N, 0);
+  std::fflush(stdout);
+  return 0;
 }
 
 int tracer_init_ale_arrays(void) {

@@ -46,6 +46,10 @@ struct Grid {
   }
 };
 
+}  // namespace
+
+namespace detail {
+
 // Lists of the elements around each node, in element order
 // (lib/analytic_mesh.F90:675-694); nodes >= nlimit are skipped.
 void node_elem_lists(const std::vector<int>& en, int M, int ntotal, int nlimit, std::vector<int>& num,
@@ -68,11 +72,17 @@ void node_elem_lists(const std::vector<int>& en, int M, int ntotal, int nlimit, 
 }
 
 // Up/downwind triangle search of lib/oce_muscl_adv.F90:245-337 for one node.
-// Vectors are wrapped to the minimum image on periodic meshes (the
-// reference's trim with cyclic_length=360 never fires on radian coordinates).
+// x components are trimmed by the mesh's cyclic_length as the reference does
+// (with 360 a no-op on radian coordinates); on periodic analytic meshes the
+// vectors are then wrapped to the minimum image.
 // The Fortran `cycle` keeps scanning, so the last matching element wins.
 int updn_search(const HostMesh& m, int node, const double* x) {
   const double px = m.Lx / kREarth, py = m.Ly / kREarth;
+  auto trim = [&](double v) {  // trim of b(1), c(1) by cyclic_length
+    if (v > m.cyclic / 2.0) v = v - m.cyclic;
+    if (v < -m.cyclic / 2.0) v = v + m.cyclic;
+    return v;
+  };
   auto wrap = [&](double* v) {
     if (!m.periodic) return;
     if (v[0] > 0.5 * px) v[0] = v[0] - px;
@@ -90,6 +100,8 @@ int updn_search(const HostMesh& m, int node, const double* x) {
     else { v1 = en[2]; v2 = en[0]; v3 = en[1]; }
     double b[2] = {m.coord[2 * v2] - m.coord[2 * v1], m.coord[2 * v2 + 1] - m.coord[2 * v1 + 1]};
     double c[2] = {m.coord[2 * v3] - m.coord[2 * v1], m.coord[2 * v3 + 1] - m.coord[2 * v1 + 1]};
+    b[0] = trim(b[0]);
+    c[0] = trim(c[0]);
     wrap(b);
     wrap(c);
     double cr = c[0] * c[0] + c[1] * c[1];
@@ -104,7 +116,7 @@ int updn_search(const HostMesh& m, int node, const double* x) {
   return found;
 }
 
-}  // namespace
+}  // namespace detail
 
 void ale_from_zbar(HostMesh& m) {
   const int N = m.N, M = m.M, nz = m.nz, nl = m.nl;
@@ -295,7 +307,7 @@ HostMesh* build_analytic(int nx, int ny, int nl, double Lx, double Ly, double de
   // nod_in_elem2D before the periodic remap (lib/analytic_mesh.F90:675-694).
   std::vector<int> num_t, lst_t;
   int maxn_t = 0;
-  node_elem_lists(en, M, NT, NT, num_t, lst_t, maxn_t);
+  detail::node_elem_lists(en, M, NT, NT, num_t, lst_t, maxn_t);
 
   // mesh_areas (lib/oce_mesh.F90:2043-2309), cartesian, no cavity.
   m.elem_area.assign(M, 0.0);
@@ -403,7 +415,7 @@ HostMesh* build_analytic(int nx, int ny, int nl, double Lx, double Ly, double de
   // Element lists around the real nodes: un-remapped (the reference's lists,
   // built before the remap) or full (every element around the folded node).
   if (periodic && cluster_full) {
-    node_elem_lists(en, M, N, N, m.nie_num, m.nie, m.max_nie);
+    detail::node_elem_lists(en, M, N, N, m.nie_num, m.nie, m.max_nie);
   } else {
     m.max_nie = maxn_t;
     m.nie_num.assign(num_t.begin(), num_t.begin() + N);
@@ -451,8 +463,8 @@ HostMesh* build_analytic(int nx, int ny, int nl, double Lx, double Ly, double de
       if (x[1] < -0.5 * py) x[1] = x[1] + py;
     }
     double mx[2] = {-x[0], -x[1]};
-    m.edge_updn[2 * n] = updn_search(m, e1, mx);
-    m.edge_updn[2 * n + 1] = updn_search(m, e2, x);
+    m.edge_updn[2 * n] = detail::updn_search(m, e1, mx);
+    m.edge_updn[2 * n + 1] = detail::updn_search(m, e2, x);
   }
   build_tables(m);
   return mp;

@@ -14,6 +14,7 @@ struct HostMesh {
   int N = 0, E = 0, M = 0, nl = 0, nz = 0, max_nie = 0, edge2D_in = 0;
   int periodic = 0, cluster_full = 0, orient_left = 0;
   double Lx = 0, Ly = 0;
+  double cyclic = 360.0;  // cyclic_length, lib/gen_modules_config.F90:83 (degrees, never converted)
 
   // connectivity (reference names, lib/MOD_MESH.F90:24-184)
   std::vector<double> coord;          // (N,2) radians
@@ -71,7 +72,17 @@ constexpr int kOrientLeft = 2;
 HostMesh* build_analytic(int nx, int ny, int nl, double Lx, double Ly, double depth, int periodic,
                          int flags, const double* zbar, const int* elem_nlev, std::string* err);
 
-// Derived tables (CSR, cluster, per-edge level windows). Called by build_analytic.
+// A FESOM mesh from its files (nod2d.out, elem2d.out, aux3d.out, edgenum.out,
+// edges.out, edge_tri.out, elvls.out, nlvls.out) as one partition, with the
+// geometry of lib/oce_mesh.F90 on the sphere. flags: kFileNoRotation,
+// kFileEulerDegrees, kFileCyclic2Pi (FESOM2's namelist handling instead of
+// the reference's defaults).
+constexpr int kFileNoRotation = 1;
+constexpr int kFileEulerDegrees = 2;
+constexpr int kFileCyclic2Pi = 4;
+HostMesh* build_from_files(const std::string& dir, int flags, std::string* err);
+
+// Derived tables (CSR, cluster, per-edge level windows). Called by the builders.
 void build_tables(HostMesh& m);
 
 // Recompute the vertical arrays from zbar (the analytic driver's ALE set-up).
@@ -83,6 +94,14 @@ void ale_from_zbar(HostMesh& m);
 // nl, whose extra layers lie below every column of the shallower parts.
 // Derived tables are rebuilt, so each part's gathers keep their order.
 HostMesh* union_meshes(const HostMesh* const* parts, int count, std::string* err);
+
+namespace detail {
+// nod_in_elem2D in element order for nodes < nlimit (lib/oce_mesh.F90:1850-1999).
+void node_elem_lists(const std::vector<int>& en, int M, int ntotal, int nlimit, std::vector<int>& num,
+                     std::vector<int>& lst, int& maxn);
+// Up/downwind triangle at `node` for the edge vector x (lib/oce_muscl_adv.F90:245-337).
+int updn_search(const HostMesh& m, int node, const double* x);
+}  // namespace detail
 
 constexpr double kREarth = 6367500.0;   // lib/oce_modules.F90:24
 constexpr double kPiRef = 3.14159265358979;  // lib/oce_modules.F90:19

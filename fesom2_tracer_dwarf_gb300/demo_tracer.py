@@ -119,6 +119,15 @@ class FESOMTracerAdvection:
             self.nl = nl
         return rc
 
+    def load_mesh_from_files(self, mesh_path):
+        """tracer_load_mesh_from_files: a FESOM mesh directory as one partition."""
+        rc = self.lib.tracer_load_mesh_from_files(str(mesh_path).encode())
+        if rc == 0:
+            nz, nn = ctypes.c_int(), ctypes.c_int()
+            self.lib.tracer_get_size(ctypes.byref(nz), ctypes.byref(nn))
+            self.nl, self.nod2D = nz.value + 1, nn.value
+        return rc
+
     def set_mesh_dims(self, nl, nod2D, edge2D, elem2D):
         return self.lib.tracer_set_mesh_dims(nl, nod2D, edge2D, elem2D)
 

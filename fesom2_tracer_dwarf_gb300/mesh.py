@@ -2,7 +2,8 @@
 
 ``Mesh`` builds the analytic mesh of the reference dwarf
 (lib/analytic_mesh.F90:114-829 with the geometry of lib/oce_mesh.F90) through
-``fgb_hmesh_analytic`` and uploads it with ``fgb_mesh_create``. Arrays are
+``fgb_hmesh_analytic``, or reads a FESOM mesh directory (``Mesh.from_files``,
+``fgb_hmesh_from_files``), and uploads it with ``fgb_mesh_create``. Arrays are
 returned 0-based as ``(outer, inner)`` numpy arrays, e.g. ``area[node, level]``.
 """
 from __future__ import annotations
@@ -54,6 +55,28 @@ class Mesh:
         self._d = None
         if upload:
             self.upload()
+
+    @classmethod
+    def from_files(cls, path: str, rotate: bool = True, euler_degrees: bool = False, cyclic_2pi: bool = False,
+                   upload: bool = True) -> "Mesh":
+        """A FESOM mesh directory (nod2d.out, elem2d.out, aux3d.out,
+        edgenum.out, edges.out, edge_tri.out, elvls.out, nlvls.out) as one
+        partition, set up as lib/oce_mesh.F90 mesh_setup does on the sphere.
+        The defaults are the reference's (rotation with the Euler angles
+        50/15/-90 used as given, cyclic_length 360 against radians);
+        euler_degrees and cyclic_2pi select FESOM2's namelist handling."""
+        L = _lib.load()
+        flags = (0 if rotate else 1) | (2 if euler_degrees else 0) | (4 if cyclic_2pi else 0)
+        h = ctypes.c_void_p()
+        _lib.check(L.fgb_hmesh_from_files(str(path).encode(), flags, ctypes.byref(h)), "fgb_hmesh_from_files")
+        self = cls.__new__(cls)
+        self.nx = self.ny = None
+        self.Lx = self.Ly = self.depth = None
+        self.periodic, self.cluster_full, self.orient_left = False, False, False
+        self.path = str(path)
+        self.parts = None
+        self._attach(h, upload)
+        return self
 
     @classmethod
     def union(cls, parts, upload: bool = True) -> "Mesh":

@@ -132,6 +132,16 @@ int fgb_version(void);
 enum { FGB_MESH_CLUSTER_FULL = 1, FGB_MESH_ORIENT_LEFT = 2 };
 int fgb_hmesh_analytic(int nx, int ny, int nl, double Lx, double Ly, double depth, int periodic, int flags,
                        const double* zbar, const int* elem_nlev, fgb_hmesh** out);
+/* A FESOM mesh directory (nod2d.out, elem2d.out, aux3d.out, edgenum.out,
+ * edges.out, edge_tri.out, elvls.out, nlvls.out) as one partition, with the
+ * set-up of lib/oce_mesh.F90:49-94 (mesh_setup) on the sphere and the ALE
+ * arrays of tracer_init_ale_arrays. flags = 0 keeps the reference's defaults
+ * (lib/gen_modules_config.F90:81-88: rotation on, the Euler angles 50/15/-90
+ * used as given, cyclic_length = 360 against radian coordinates);
+ * FGB_MESH_FILE_NO_ROTATION, FGB_MESH_FILE_EULER_DEGREES and
+ * FGB_MESH_FILE_CYCLIC_2PI select FESOM2's namelist handling instead. */
+enum { FGB_MESH_FILE_NO_ROTATION = 1, FGB_MESH_FILE_EULER_DEGREES = 2, FGB_MESH_FILE_CYCLIC_2PI = 4 };
+int fgb_hmesh_from_files(const char* dir, int flags, fgb_hmesh** out);
 void fgb_hmesh_free(fgb_hmesh* h);
 /* No counterpart in the reference (the batching form): the disjoint union of
  * `count` host meshes as one mesh, parts in order (node, edge and element

@@ -30,6 +30,8 @@ static double dmax(double a, double b) { return a > b ? a : b; }
 
 struct omesh {
   int nx, ny, nl, periodic, cluster_full;
+  int cartesian;            /* lib/gen_modules_config.F90:81 (.true. for the analytic mesh) */
+  double cyclic;            /* cyclic_length, lib/gen_modules_config.F90:83 */
   int nod2D, eDim, nod2D_total, elem2D, edge2D, edge2D_in, max_nie;
   double Lx, Ly;
   double* coord;            /* (2, nod2D_total) radians */
@@ -100,11 +102,12 @@ static int pnode(const pctx* c, int i, int j) {
   return c->nod2D_total;
 }
 
-/* trim_cyclic_mp, lib/gen_modules_rotate_grid.F90:216-224 (never fires for the
- * analytic mesh: coordinates are radians, cyclic_length is 360). */
-static double trim_cyclic(double b) {
-  if (b > CYCLIC_LENGTH / 2.0) b = b - CYCLIC_LENGTH;
-  if (b < -CYCLIC_LENGTH / 2.0) b = b + CYCLIC_LENGTH;
+/* trim_cyclic_mp, lib/gen_modules_rotate_grid.F90:216-224. With the
+ * reference's cyclic_length = 360 (degrees, never converted) it never fires on
+ * radian coordinates. */
+static double trim_cyc(const omesh* m, double b) {
+  if (b > m->cyclic / 2.0) b = b - m->cyclic;
+  if (b < -m->cyclic / 2.0) b = b + m->cyclic;
   return b;
 }
 
@@ -153,8 +156,8 @@ static void test_tri(omesh* m) {
     double a0 = A2(m->coord, 2, 1, el[0]), a1 = A2(m->coord, 2, 2, el[0]);
     double b0 = A2(m->coord, 2, 1, el[1]) - a0, b1 = A2(m->coord, 2, 2, el[1]) - a1;
     double c0 = A2(m->coord, 2, 1, el[2]) - a0, c1 = A2(m->coord, 2, 2, el[2]) - a1;
-    b0 = trim_cyclic(b0);
-    c0 = trim_cyclic(c0);
+    b0 = trim_cyc(m, b0);
+    c0 = trim_cyc(m, c0);
     double r = b0 * c1 - b1 * c0;
     if (r > 0.0) {
       int t = el[1];
@@ -164,18 +167,20 @@ static void test_tri(omesh* m) {
   }
 }
 
-/* mesh_areas, lib/oce_mesh.F90:2043-2309 (cartesian, no cavity) */
+/* mesh_areas, lib/oce_mesh.F90:2043-2309 (no cavity) */
 static void mesh_areas(omesh* m) {
   const int nl = m->nl;
   for (int n = 1; n <= m->elem2D; ++n) {
     const int* el = &A2(m->elem2D_nodes, 3, 1, n);
-    double ay = 1.0; /* cartesian: lib/oce_mesh.F90:2093 */
+    double ay = (A2(m->coord, 2, 2, el[0]) + A2(m->coord, 2, 2, el[1]) + A2(m->coord, 2, 2, el[2])) / 3.0;
+    ay = cos(ay);
+    if (m->cartesian) ay = 1.0; /* lib/oce_mesh.F90:2091-2093 */
     double a0 = A2(m->coord, 2, 1, el[1]) - A2(m->coord, 2, 1, el[0]);
     double a1 = A2(m->coord, 2, 2, el[1]) - A2(m->coord, 2, 2, el[0]);
     double b0 = A2(m->coord, 2, 1, el[2]) - A2(m->coord, 2, 1, el[0]);
     double b1 = A2(m->coord, 2, 2, el[2]) - A2(m->coord, 2, 2, el[0]);
-    a0 = trim_cyclic(a0);
-    b0 = trim_cyclic(b0);
+    a0 = trim_cyc(m, a0);
+    b0 = trim_cyc(m, b0);
     a0 = a0 * ay;
     b0 = b0 * ay;
     m->elem_area[n - 1] = 0.5 * fabs(a0 * b1 - b0 * a1);
@@ -206,8 +211,8 @@ static void elem_center(const omesh* m, int elem, double* x, double* y) {
   for (int k = 0; k < 3; ++k) ax[k] = A2(m->coord, 2, 1, el[k]);
   double amin = dmin(dmin(ax[0], ax[1]), ax[2]);
   for (int k = 0; k < 3; ++k) {
-    if (ax[k] - amin >= CYCLIC_LENGTH / 2.0) ax[k] = ax[k] - CYCLIC_LENGTH;
-    if (ax[k] - amin < -CYCLIC_LENGTH / 2.0) ax[k] = ax[k] + CYCLIC_LENGTH;
+    if (ax[k] - amin >= m->cyclic / 2.0) ax[k] = ax[k] - m->cyclic;
+    if (ax[k] - amin < -m->cyclic / 2.0) ax[k] = ax[k] + m->cyclic;
   }
   *x = (ax[0] + ax[1] + ax[2]) / 3.0;
   *y = (A2(m->coord, 2, 2, el[0]) + A2(m->coord, 2, 2, el[1]) + A2(m->coord, 2, 2, el[2])) / 3.0;
@@ -219,13 +224,13 @@ static void mesh_auxiliary_arrays(omesh* m) {
   double* cy = (double*)xcalloc((size_t)m->elem2D, sizeof(double));
   for (int n = 1; n <= m->elem2D; ++n) {
     elem_center(m, n, &cx[n - 1], &cy[n - 1]);
-    m->elem_cos[n - 1] = 1.0; /* cartesian, :2418-2421 */
+    m->elem_cos[n - 1] = m->cartesian ? 1.0 : cos(cy[n - 1]); /* :2408-2421 */
   }
   for (int n = 1; n <= m->edge2D; ++n) {
     int e1 = A2(m->edges, 2, 1, n), e2 = A2(m->edges, 2, 2, n);
     double a0 = A2(m->coord, 2, 1, e2) - A2(m->coord, 2, 1, e1);
     double a1 = A2(m->coord, 2, 2, e2) - A2(m->coord, 2, 2, e1);
-    a0 = trim_cyclic(a0);
+    a0 = trim_cyc(m, a0);
     A2(m->edge_dxdy, 2, 1, n) = a0;
     A2(m->edge_dxdy, 2, 2, n) = a1;
   }
@@ -235,11 +240,11 @@ static void mesh_auxiliary_arrays(omesh* m) {
     /* edge_center, lib/oce_mesh.F90:2001-2019 */
     double p0 = A2(m->coord, 2, 1, e1), p1 = A2(m->coord, 2, 2, e1);
     double q0 = A2(m->coord, 2, 1, e2), q1 = A2(m->coord, 2, 2, e2);
-    if (p0 - q0 > CYCLIC_LENGTH / 2.0) p0 = p0 - CYCLIC_LENGTH;
-    if (p0 - q0 < -CYCLIC_LENGTH / 2.0) q0 = q0 - CYCLIC_LENGTH;
+    if (p0 - q0 > m->cyclic / 2.0) p0 = p0 - m->cyclic;
+    if (p0 - q0 < -m->cyclic / 2.0) q0 = q0 - m->cyclic;
     double ax = 0.5 * (p0 + q0), ay = 0.5 * (p1 + q1);
     double b0 = cx[el1 - 1] - ax, b1 = cy[el1 - 1] - ay;
-    b0 = trim_cyclic(b0);
+    b0 = trim_cyc(m, b0);
     b0 = b0 * m->elem_cos[el1 - 1];
     b0 = b0 * R_EARTH;
     b1 = b1 * R_EARTH;
@@ -248,7 +253,7 @@ static void mesh_auxiliary_arrays(omesh* m) {
     if (el2 > 0) {
       b0 = cx[el2 - 1] - ax;
       b1 = cy[el2 - 1] - ay;
-      b0 = trim_cyclic(b0);
+      b0 = trim_cyc(m, b0);
       b0 = b0 * m->elem_cos[el2 - 1];
       b0 = b0 * R_EARTH;
       b1 = b1 * R_EARTH;
@@ -262,10 +267,10 @@ static void mesh_auxiliary_arrays(omesh* m) {
   for (int elem = 1; elem <= m->elem2D; ++elem) {
     const int* el = &A2(m->elem2D_nodes, 3, 1, elem);
     double dX31 = A2(m->coord, 2, 1, el[2]) - A2(m->coord, 2, 1, el[0]);
-    dX31 = trim_cyclic(dX31);
+    dX31 = trim_cyc(m, dX31);
     dX31 = m->elem_cos[elem - 1] * dX31;
     double dX21 = A2(m->coord, 2, 1, el[1]) - A2(m->coord, 2, 1, el[0]);
-    dX21 = trim_cyclic(dX21);
+    dX21 = trim_cyc(m, dX21);
     dX21 = m->elem_cos[elem - 1] * dX21;
     double dY31 = A2(m->coord, 2, 2, el[2]) - A2(m->coord, 2, 2, el[0]);
     double dY21 = A2(m->coord, 2, 2, el[1]) - A2(m->coord, 2, 2, el[0]);
@@ -360,6 +365,8 @@ static int updn_search(const omesh* m, int node, const double* x) {
     else { v1 = en[2]; v2 = en[0]; v3 = en[1]; }
     double b[2] = {A2(m->coord, 2, 1, v2) - A2(m->coord, 2, 1, v1), A2(m->coord, 2, 2, v2) - A2(m->coord, 2, 2, v1)};
     double c[2] = {A2(m->coord, 2, 1, v3) - A2(m->coord, 2, 1, v1), A2(m->coord, 2, 2, v3) - A2(m->coord, 2, 2, v1)};
+    b[0] = trim_cyc(m, b[0]);
+    c[0] = trim_cyc(m, c[0]);
     wrap_mi(m, b);
     wrap_mi(m, c);
     double cr = c[0] * c[0] + c[1] * c[1];
@@ -380,6 +387,7 @@ static void find_up_downwind_triangles(omesh* m) {
   for (int n = 1; n <= m->edge2D; ++n) {
     int e1 = A2(m->edges, 2, 1, n), e2 = A2(m->edges, 2, 2, n);
     double x[2] = {A2(m->coord, 2, 1, e2) - A2(m->coord, 2, 1, e1), A2(m->coord, 2, 2, e2) - A2(m->coord, 2, 2, e1)};
+    x[0] = trim_cyc(m, x[0]);
     wrap_mi(m, x);
     x[0] = -x[0];
     x[1] = -x[1];
@@ -389,6 +397,36 @@ static void find_up_downwind_triangles(omesh* m) {
     A2(m->edge_up_dn_tri, 2, 2, n) = updn_search(m, e2, x);
   }
 }
+
+/* ALE arrays from zbar (src/fesom_analytic.F90:206-244, the same as
+ * tracer_init_ale_arrays, lib/tracer_c_interface.F90:875-925) and the MUSCL
+ * set-up (lib/oce_muscl_adv.F90:38-357). */
+static void finish_mesh(omesh* m) {
+  const int N = m->nod2D, M = m->elem2D, E = m->edge2D, nl = m->nl, nz = nl - 1;
+  m->hnode = (double*)xcalloc((size_t)nz * N, sizeof(double));
+  m->hnode_new = (double*)xcalloc((size_t)nz * N, sizeof(double));
+  m->helem = (double*)xcalloc((size_t)nz * M, sizeof(double));
+  m->Z_3d_n = (double*)xcalloc((size_t)nz * N, sizeof(double));
+  m->zbar_3d_n = (double*)xcalloc((size_t)nl * N, sizeof(double));
+  for (int n = 1; n <= N; ++n)
+    for (int k = 1; k <= nz; ++k) {
+      A2(m->hnode, nz, k, n) = m->zbar[k - 1] - m->zbar[k];
+      A2(m->hnode_new, nz, k, n) = A2(m->hnode, nz, k, n);
+    }
+  for (int n = 1; n <= M; ++n)
+    for (int k = 1; k <= nz; ++k) A2(m->helem, nz, k, n) = m->zbar[k - 1] - m->zbar[k];
+  for (int n = 1; n <= N; ++n) {
+    for (int k = 1; k <= nl; ++k) A2(m->zbar_3d_n, nl, k, n) = m->zbar[k - 1];
+    for (int k = 1; k <= nz; ++k) A2(m->Z_3d_n, nz, k, n) = m->Z[k - 1];
+  }
+
+  /* MUSCL set-up (lib/oce_muscl_adv.F90:38-357) */
+  m->nboundary_lay = (int*)xcalloc((size_t)N, sizeof(int));
+  m->edge_up_dn_tri = (int*)xcalloc((size_t)2 * E, sizeof(int));
+  muscl_nboundary_lay(m);
+  find_up_downwind_triangles(m);
+}
+
 
 omesh* om_mesh_analytic(int nx, int ny, int nl, double Lx, double Ly, double max_depth,
                         int periodic, int cluster_full, const double* zbar_in, const int* elem_nlev) {
@@ -401,6 +439,8 @@ omesh* om_mesh_analytic2(int nx, int ny, int nl, double Lx, double Ly, double ma
   if (periodic && (nx < 3 || ny < 3)) return NULL;
   omesh* m = (omesh*)xcalloc(1, sizeof(omesh));
   m->nx = nx; m->ny = ny; m->nl = nl; m->periodic = periodic; m->cluster_full = cluster_full;
+  m->cartesian = 1; /* lib/analytic_mesh.F90:162 */
+  m->cyclic = CYCLIC_LENGTH;
   m->Lx = Lx; m->Ly = Ly;
   int n_horiz, n_vert, n_diag;
   if (periodic) {
@@ -636,30 +676,112 @@ omesh* om_mesh_analytic2(int nx, int ny, int nl, double Lx, double Ly, double ma
     find_levels_min_e2n(m);
   }
 
-  /* ALE arrays of the analytic driver, src/fesom_analytic.F90:206-244 */
-  const int N = m->nod2D, nz = nl - 1;
-  m->hnode = (double*)xcalloc((size_t)nz * N, sizeof(double));
-  m->hnode_new = (double*)xcalloc((size_t)nz * N, sizeof(double));
-  m->helem = (double*)xcalloc((size_t)nz * M, sizeof(double));
-  m->Z_3d_n = (double*)xcalloc((size_t)nz * N, sizeof(double));
-  m->zbar_3d_n = (double*)xcalloc((size_t)nl * N, sizeof(double));
-  for (int n = 1; n <= N; ++n)
-    for (int k = 1; k <= nz; ++k) {
-      A2(m->hnode, nz, k, n) = m->zbar[k - 1] - m->zbar[k];
-      A2(m->hnode_new, nz, k, n) = A2(m->hnode, nz, k, n);
-    }
-  for (int n = 1; n <= M; ++n)
-    for (int k = 1; k <= nz; ++k) A2(m->helem, nz, k, n) = m->zbar[k - 1] - m->zbar[k];
-  for (int n = 1; n <= N; ++n) {
-    for (int k = 1; k <= nl; ++k) A2(m->zbar_3d_n, nl, k, n) = m->zbar[k - 1];
-    for (int k = 1; k <= nz; ++k) A2(m->Z_3d_n, nz, k, n) = m->Z[k - 1];
-  }
+  finish_mesh(m);
+  return m;
+}
 
-  /* MUSCL set-up (lib/oce_muscl_adv.F90:38-357) */
-  m->nboundary_lay = (int*)xcalloc((size_t)N, sizeof(int));
-  m->edge_up_dn_tri = (int*)xcalloc((size_t)2 * E, sizeof(int));
-  muscl_nboundary_lay(m);
-  find_up_downwind_triangles(m);
+/* g2r with the rotation matrix of set_mesh_transform_matrix,
+ * lib/gen_modules_rotate_grid.F90:12-88: geographic (glon, glat) -> rotated. */
+static void g2r(const double* r, double glon, double glat, double* rlon, double* rlat) {
+  double xg = cos(glat) * cos(glon), yg = cos(glat) * sin(glon), zg = sin(glat);
+  double xr = r[0] * xg + r[1] * yg + r[2] * zg;
+  double yr = r[3] * xg + r[4] * yg + r[5] * zg;
+  double zr = r[6] * xg + r[7] * yg + r[8] * zg;
+  *rlat = asin(zr);
+  *rlon = (yr == 0.0 && xr == 0.0) ? 0.0 : atan2(yr, xr);
+}
+
+omesh* om_mesh_from_arrays(int nod2D, int elem2D, int edge2D, int edge2D_in, int nl, const double* lonlat,
+                           const int* elem, const int* edges, const int* edge_tri, const int* elvls,
+                           const int* nlvls, const double* zbar_in, int flags) {
+  if (nod2D < 3 || elem2D < 1 || edge2D < 3 || nl < 3) return NULL;
+  omesh* m = (omesh*)xcalloc(1, sizeof(omesh));
+  m->nl = nl;
+  m->cartesian = 0; /* lib/gen_modules_config.F90:81 */
+  m->cyclic = (flags & OM_FILE_CYCLIC_2PI) ? 2.0 * PI_F : CYCLIC_LENGTH;
+  m->nod2D = m->nod2D_total = nod2D;
+  m->elem2D = elem2D;
+  m->edge2D = edge2D;
+  m->edge2D_in = edge2D_in;
+  const int N = nod2D, M = elem2D, E = edge2D;
+
+  /* read_mesh, lib/oce_mesh.F90:230-330: degrees -> radians, then the
+   * rotation when force_rotation (default .true., lib/gen_modules_config.F90:85).
+   * The Euler angles 50, 15, -90 (:86-88) enter cos/sin as they are. */
+  double rm[9];
+  {
+    double al = 50.0, be = 15.0, ga = -90.0;
+    if (flags & OM_FILE_EULER_DEGREES) {
+      al = al * (PI_F / 180.0);
+      be = be * (PI_F / 180.0);
+      ga = ga * (PI_F / 180.0);
+    }
+    rm[0] = cos(ga) * cos(al) - sin(ga) * cos(be) * sin(al);
+    rm[1] = cos(ga) * sin(al) + sin(ga) * cos(be) * cos(al);
+    rm[2] = sin(ga) * sin(be);
+    rm[3] = -sin(ga) * cos(al) - cos(ga) * cos(be) * sin(al);
+    rm[4] = -sin(ga) * sin(al) + cos(ga) * cos(be) * cos(al);
+    rm[5] = cos(ga) * sin(be);
+    rm[6] = sin(be) * sin(al);
+    rm[7] = -sin(be) * cos(al);
+    rm[8] = cos(be);
+  }
+  const double rad = PI_F / 180.0; /* lib/oce_modules.F90:20 */
+  m->coord = (double*)xcalloc((size_t)2 * N, sizeof(double));
+  for (int n = 1; n <= N; ++n) {
+    double x = A2(lonlat, 2, 1, n) * rad, y = A2(lonlat, 2, 2, n) * rad;
+    if (!(flags & OM_FILE_NO_ROTATION)) {
+      double rx = x, ry = y;
+      g2r(rm, rx, ry, &x, &y);
+    }
+    A2(m->coord, 2, 1, n) = x;
+    A2(m->coord, 2, 2, n) = y;
+  }
+  m->elem2D_nodes = (int*)xcalloc((size_t)3 * M, sizeof(int));
+  memcpy(m->elem2D_nodes, elem, (size_t)3 * M * sizeof(int));
+  /* aux3d.out: zbar negative downwards, Z the mid-depths (lib/oce_mesh.F90:445-455) */
+  m->zbar = (double*)xcalloc((size_t)nl, sizeof(double));
+  m->Z = (double*)xcalloc((size_t)nl, sizeof(double));
+  for (int k = 0; k < nl; ++k) m->zbar[k] = zbar_in[k];
+  if (m->zbar[1] > 0.0)
+    for (int k = 0; k < nl; ++k) m->zbar[k] = -m->zbar[k];
+  for (int k = 0; k < nl - 1; ++k) m->Z[k] = 0.5 * (m->zbar[k] + m->zbar[k + 1]);
+
+  test_tri(m);
+  /* load_edges, lib/oce_mesh.F90:1617-1848 (negative edge_tri -> 0) */
+  m->edges = (int*)xcalloc((size_t)2 * E, sizeof(int));
+  m->edge_tri = (int*)xcalloc((size_t)2 * E, sizeof(int));
+  for (size_t i = 0; i < (size_t)2 * E; ++i) {
+    m->edges[i] = edges[i];
+    m->edge_tri[i] = edge_tri[i] < 0 ? 0 : edge_tri[i];
+  }
+  build_nod_in_elem(m, N);
+  /* find_levels, lib/oce_mesh.F90:807-1001 */
+  m->nlevels = (int*)xcalloc((size_t)M, sizeof(int));
+  m->ulevels = (int*)xcalloc((size_t)M, sizeof(int));
+  m->nlevels_nod2D = (int*)xcalloc((size_t)N, sizeof(int));
+  m->ulevels_nod2D = (int*)xcalloc((size_t)N, sizeof(int));
+  m->nlevels_nod2D_min = (int*)xcalloc((size_t)N, sizeof(int));
+  m->ulevels_nod2D_max = (int*)xcalloc((size_t)N, sizeof(int));
+  for (int e = 0; e < M; ++e) {
+    m->nlevels[e] = elvls[e];
+    m->ulevels[e] = 1;
+  }
+  for (int n = 0; n < N; ++n) {
+    m->nlevels_nod2D[n] = nlvls[n];
+    m->ulevels_nod2D[n] = 1;
+  }
+  find_levels_min_e2n(m);
+  m->elem_area = (double*)xcalloc((size_t)M, sizeof(double));
+  m->area = (double*)xcalloc((size_t)nl * N, sizeof(double));
+  m->areasvol = (double*)xcalloc((size_t)nl * N, sizeof(double));
+  mesh_areas(m);
+  m->edge_dxdy = (double*)xcalloc((size_t)2 * E, sizeof(double));
+  m->edge_cross_dxdy = (double*)xcalloc((size_t)4 * E, sizeof(double));
+  m->elem_cos = (double*)xcalloc((size_t)M, sizeof(double));
+  m->gradient_sca = (double*)xcalloc((size_t)6 * M, sizeof(double));
+  mesh_auxiliary_arrays(m);
+  finish_mesh(m);
   return m;
 }
 

@@ -44,6 +44,20 @@ omesh* om_mesh_analytic(int nx, int ny, int nl, double Lx, double Ly, double max
  * the right for horizontal and vertical edges). */
 omesh* om_mesh_analytic2(int nx, int ny, int nl, double Lx, double Ly, double max_depth, int periodic,
                          int cluster_full, int orient_left, const double* zbar, const int* elem_nlev);
+/* A FESOM mesh read from its files (the global mesh as one partition):
+ * read_mesh, test_tri, load_edges, find_neighbors, find_levels,
+ * find_levels_min_e2n, mesh_areas and mesh_auxiliary_arrays of
+ * lib/oce_mesh.F90 with the reference's defaults (cartesian = .false.,
+ * force_rotation = .true., the Euler angles 50/15/-90 used as given,
+ * cyclic_length = 360), then the ALE arrays of tracer_init_ale_arrays and the
+ * MUSCL set-up. lonlat (2,N) degrees as in nod2d.out; elem (3,M), edges (2,E),
+ * edge_tri (2,E) 1-based as in elem2d.out, edges.out, edge_tri.out; elvls (M),
+ * nlvls (N); zbar (nl) as in aux3d.out. Flags select FESOM2's namelist
+ * handling instead: no rotation, Euler angles in degrees, cyclic_length 2*pi. */
+enum { OM_FILE_NO_ROTATION = 1, OM_FILE_EULER_DEGREES = 2, OM_FILE_CYCLIC_2PI = 4 };
+omesh* om_mesh_from_arrays(int nod2D, int elem2D, int edge2D, int edge2D_in, int nl, const double* lonlat,
+                           const int* elem, const int* edges, const int* edge_tri, const int* elvls,
+                           const int* nlvls, const double* zbar, int flags);
 void om_mesh_free(omesh* m);
 /* sizes: [nod2D, nod2D_total, elem2D, edge2D, edge2D_in, nl, max_nie] */
 void om_mesh_sizes(const omesh* m, int* out7);

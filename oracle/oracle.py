@@ -49,6 +49,8 @@ def lib():
         L.om_mesh_analytic2.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                         ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_int, _dp, _ip]
+        L.om_mesh_from_arrays.restype = ctypes.c_void_p
+        L.om_mesh_from_arrays.argtypes = [ctypes.c_int] * 5 + [_dp, _ip, _ip, _ip, _ip, _ip, _dp, ctypes.c_int]
         L.om_mesh_free.argtypes = [ctypes.c_void_p]
         L.om_mesh_sizes.argtypes = [ctypes.c_void_p, _ip]
         L.om_mesh_get_int.restype = ctypes.c_long
@@ -89,8 +91,37 @@ def _f64(a):
     return np.ascontiguousarray(a, dtype=np.float64)
 
 
+def read_fesom_dir(path):
+    """The files of a FESOM mesh directory the reference reads at one
+    partition (lib/oce_mesh.F90:98-806, :807-1001, :1617-1848), parsed as
+    whitespace-separated tokens: nod2d.out, elem2d.out, aux3d.out (levels),
+    edgenum.out, edges.out, edge_tri.out, elvls.out, nlvls.out."""
+    def toks(name):
+        with open(os.path.join(path, name)) as f:
+            return f.read().split()
+
+    t = toks("nod2d.out")
+    N = int(t[0])
+    nod = np.array(t[1:1 + 4 * N], dtype=np.float64).reshape(N, 4)
+    t = toks("elem2d.out")
+    M = int(t[0])
+    elem = np.array(t[1:1 + 3 * M], dtype=np.int64).astype(np.int32).reshape(M, 3)
+    t = toks("aux3d.out")
+    nl = int(t[0])
+    zbar = np.array(t[1:1 + nl], dtype=np.float64)
+    t = toks("edgenum.out")
+    E, E_in = int(t[0]), int(t[1])
+    edges = np.array(toks("edges.out")[:2 * E], dtype=np.int64).astype(np.int32).reshape(E, 2)
+    edge_tri = np.array(toks("edge_tri.out")[:2 * E], dtype=np.int64).astype(np.int32).reshape(E, 2)
+    elvls = np.array(toks("elvls.out")[:M], dtype=np.int64).astype(np.int32)
+    nlvls = np.array(toks("nlvls.out")[:N], dtype=np.int64).astype(np.int32)
+    return dict(lonlat=np.ascontiguousarray(nod[:, 1:3]), coast=nod[:, 3].astype(np.int32), elem=elem, nl=nl,
+                zbar=zbar, edge2D=E, edge2D_in=E_in, edges=edges, edge_tri=edge_tri, elvls=elvls, nlvls=nlvls)
+
+
 class Mesh:
-    """An analytic mesh built by the oracle (lib/analytic_mesh.F90)."""
+    """A mesh built by the oracle: the analytic mesh (lib/analytic_mesh.F90),
+    or a FESOM mesh from its files (``from_files``)."""
 
     def __init__(self, nx, ny, nl, Lx=100000.0, Ly=100000.0, depth=1000.0, periodic=True,
                  cluster_full=False, zbar=None, elem_nlev=None, orient_left=False):
@@ -102,12 +133,33 @@ class Mesh:
                                 int(orient_left), _p(zb), _p(en, _ip))
         if not h:
             raise ValueError("invalid analytic mesh parameters")
+        self._attach(h)
+        self.Lx, self.Ly, self.periodic = Lx, Ly, periodic
+
+    def _attach(self, h):
         self.h = ctypes.c_void_p(h)
         s = np.zeros(7, np.int32)
-        L.om_mesh_sizes(self.h, _p(s, _ip))
+        lib().om_mesh_sizes(self.h, _p(s, _ip))
         (self.nod2D, self.nod2D_total, self.elem2D, self.edge2D, self.edge2D_in, self.nl,
          self.max_nie) = (int(v) for v in s)
-        self.Lx, self.Ly, self.periodic = Lx, Ly, periodic
+
+    @classmethod
+    def from_files(cls, path, rotate=True, euler_degrees=False, cyclic_2pi=False):
+        """A FESOM mesh directory (read_fesom_dir) through om_mesh_from_arrays."""
+        d = read_fesom_dir(path)
+        flags = (0 if rotate else 1) | (2 if euler_degrees else 0) | (4 if cyclic_2pi else 0)
+        arrs = [np.ascontiguousarray(d[k], dtype=np.int32) for k in ("elem", "edges", "edge_tri", "elvls", "nlvls")]
+        lonlat = _f64(d["lonlat"])
+        zb = _f64(d["zbar"])
+        h = lib().om_mesh_from_arrays(len(d["nlvls"]), len(d["elvls"]), d["edge2D"], d["edge2D_in"], d["nl"],
+                                      _p(lonlat), *[_p(a, _ip) for a in arrs], _p(zb), flags)
+        if not h:
+            raise ValueError("invalid mesh files")
+        self = cls.__new__(cls)
+        self._attach(h)
+        self.Lx = self.Ly = 0.0
+        self.periodic = False
+        return self
 
     def __del__(self):
         if getattr(self, "h", None) is not None and _lib is not None:

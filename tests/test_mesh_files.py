@@ -1,0 +1,218 @@
+"""FESOM mesh files: the pi mesh of the reference (tests/golden/pi_mesh.npz,
+written back as a mesh directory) read by the library (fgb_hmesh_from_files,
+tracer_load_mesh_from_files) and by the oracle (its own parser and
+om_mesh_from_arrays).
+
+CPU: the library's set-up (read_mesh, test_tri, load_edges, find_levels,
+mesh_areas and mesh_auxiliary_arrays of lib/oce_mesh.F90 on the sphere) equals
+the oracle's bit for bit under the reference's defaults and under FESOM2's
+namelist handling; the sizes are those python/test_mesh_from_files.py prints;
+malformed directories are refused; in the oracle a zero velocity leaves the
+tracers unchanged and a continuity-consistent flow keeps a uniform tracer
+uniform on this unstructured, ragged, coastal mesh.
+GPU: the step on the pi mesh equals the oracle (FP64 bit for bit, FP32 to
+1e-5), and the reference's mesh-from-files workflow runs through the C ABI.
+"""
+import itertools
+import os
+import zlib
+
+import numpy as np
+import pytest
+
+from fesom_files import load_pi, write_mesh_dir, write_pi
+
+FLAGS = [dict(), dict(euler_degrees=True, cyclic_2pi=True), dict(rotate=False)]
+REAL = ["coord", "elem_area", "area", "areasvol", "edge_dxdy", "edge_cross_dxdy", "elem_cos", "gradient_sca",
+        "hnode", "hnode_new", "helem", "Z_3d_n", "zbar_3d_n"]
+INDEX = {"elem_nodes": ("elem2D_nodes", 1), "edges": ("edges", 1), "edge_tri": ("edge_tri", 1),
+         "edge_up_dn_tri": ("edge_up_dn_tri", 1), "nlevels": ("nlevels", 0), "nlevels_nod2D": ("nlevels_nod2D", 0),
+         "nlevels_nod2D_min": ("nlevels_nod2D_min", 0), "nboundary_lay": ("nboundary_lay", 0),
+         "nod_in_elem2D_num": ("nod_in_elem2D_num", 0)}
+
+
+@pytest.fixture(scope="module")
+def pi_dir(tmp_path_factory):
+    return write_pi(str(tmp_path_factory.mktemp("pi")))
+
+
+def _mesh(path, upload=False, **kw):
+    from fesom2_tracer_dwarf_gb300.mesh import Mesh
+
+    return Mesh.from_files(path, upload=upload, **kw)
+
+
+def test_sizes_as_the_reference_test_prints(pi_dir):
+    m = _mesh(pi_dir)
+    assert (m.nl, m.N, m.E, m.M, m.edge2D_in) == (48, 3140, 8986, 5839, 8531)
+    assert m.nz == 47 and m.max_nie == 8
+    lev = m.get("nlevels_nod2D")
+    assert lev.min() == 5 and lev.max() == 46  # ragged bottom
+
+
+@pytest.mark.parametrize("flags", FLAGS, ids=["reference", "fesom2_namelist", "no_rotation"])
+def test_setup_matches_oracle(pi_dir, oracle_mod, flags):
+    m = _mesh(pi_dir, **flags)
+    om = oracle_mod.Mesh.from_files(pi_dir, **flags)
+    assert (om.nod2D, om.edge2D, om.elem2D, om.nl, om.edge2D_in) == (m.N, m.E, m.M, m.nl, m.edge2D_in)
+    for name in REAL:
+        a = m.get(name)
+        b = om.getd(name).reshape(a.shape)
+        assert np.array_equal(a, b), f"{name}: max |diff| {np.abs(a - b).max()}"
+    for name, (oname, off) in INDEX.items():
+        a = m.get(name)
+        b = om.geti(oname).reshape(a.shape) - off
+        assert np.array_equal(a, b), f"{name}: {(a != b).sum()} entries differ"
+
+
+def test_reference_defaults_leave_the_seam_untrimmed(pi_dir):
+    """cyclic_length stays 360 against radian coordinates, so elements across
+    the rotated grid's seam get the full 2*pi longitude jump in their area;
+    FESOM2's 2*pi trims it (elements of the same order as their neighbours)."""
+    ref = _mesh(pi_dir).get("elem_area")
+    fixed = _mesh(pi_dir, euler_degrees=True, cyclic_2pi=True).get("elem_area")
+    assert ref.max() > 100 * np.median(ref)
+    assert fixed.max() < 50 * np.median(fixed)
+
+
+def test_malformed_directories_are_refused(tmp_path, pi_dir):
+    from fesom2_tracer_dwarf_gb300 import _lib
+
+    with pytest.raises(RuntimeError, match="can not open file"):
+        _mesh(str(tmp_path / "missing"))
+    d = load_pi()
+    elem = d["elem"].copy()
+    elem[7, 1] = 99999
+    p = write_mesh_dir(str(tmp_path / "bad_elem"), d["lonlat"], elem, d["zbar"], d["edges"], d["edge_tri"],
+                       d["edgenum"], d["elvls"], d["nlvls"])
+    with pytest.raises(RuntimeError, match="node index out of range"):
+        _mesh(p)
+    p = write_mesh_dir(str(tmp_path / "short"), d["lonlat"], d["elem"], d["zbar"], d["edges"][:-5],
+                       d["edge_tri"][:-5], d["edgenum"], d["elvls"], d["nlvls"])
+    with pytest.raises(RuntimeError, match="unexpected end of data"):
+        _mesh(p)
+    p = write_mesh_dir(str(tmp_path / "two_levels"), d["lonlat"], d["elem"], d["zbar"][:2], d["edges"],
+                       d["edge_tri"], d["edgenum"], d["elvls"], d["nlvls"])
+    with pytest.raises(RuntimeError, match="less than 3"):
+        _mesh(p)
+    # the path may end without '/'
+    assert _mesh(pi_dir.rstrip("/")).N == 3140
+    assert _lib.load().tracer_load_mesh_from_files(str(tmp_path / "missing").encode()) == -1
+
+
+def _pi_pair(oracle_mod, pi_dir, **flags):
+    return oracle_mod.Mesh.from_files(pi_dir, **flags), _mesh(pi_dir, **flags)
+
+
+@pytest.mark.parametrize("schemes", [("UPW1", "UPW1", "NONE"), ("MUSCL", "PPM", "FCT")])
+def test_oracle_zero_velocity_is_identity(oracle_mod, pi_dir, schemes):
+    """The reference's mesh-from-files test steps with zero velocity."""
+    om, m = _pi_pair(oracle_mod, pi_dir)
+    nz = m.nz
+    T = np.repeat((20.0 - 15.0 * np.arange(nz) / (nz - 1))[None, :], m.N, axis=0)
+    vals = np.ascontiguousarray(np.stack([T, np.full_like(T, 35.0)]))
+    before = vals.copy()
+    W = oracle_mod.Work(om)
+    for _ in range(5):
+        oracle_mod.analytic_step(om, W, 1.0e-3, np.zeros((m.M, nz, 2)), np.zeros((m.N, m.nl)), vals, vals.copy(),
+                                 [schemes + (1.0, 1.0)] * 2, copy_ab=True)
+    assert np.array_equal(vals, before)
+
+
+@pytest.mark.parametrize("schemes", [("MUSCL", "QR4C", "FCT"), ("MFCT", "PPM", "FCT"), ("UPW1", "UPW1", "NONE")])
+def test_oracle_uniform_stays_uniform(oracle_mod, pi_dir, schemes):
+    from fesom2_tracer_dwarf_gb300 import synthetic
+
+    om, m = _pi_pair(oracle_mod, pi_dir, euler_degrees=True, cyclic_2pi=True)
+    rng = np.random.default_rng(31)
+    vel = rng.uniform(-0.2, 0.2, size=(m.M, m.nz, 2))
+    w = synthetic.diagnose_w(m, vel)
+    vals = np.full((1, m.N, m.nz), 12.5)
+    W = oracle_mod.Work(om)
+    for _ in range(3):
+        oracle_mod.analytic_step(om, W, 1800.0, vel, w, vals, vals.copy(), [schemes + (0.7, 0.6)], copy_ab=True)
+    nlev = m.get("nlevels_nod2D")
+    wet = np.arange(m.nz)[None, :] < (nlev - 1)[:, None]
+    assert np.abs(vals[0][wet] - 12.5).max() <= 1e-12 * 12.5
+
+
+torch = pytest.importorskip("torch")
+
+
+def _gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA GPU")
+
+
+SCHEMES = [("UPW1", "UPW1", "NONE"), ("MUSCL", "QR4C", "FCT"), ("MFCT", "PPM", "FCT"), ("MUSCL", "CDIFF", "NONE"),
+           ("UPW1", "PPM", "FCT"), ("MFCT", "QR4C", "NONE")]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("flags,schemes", list(itertools.product([0, 1], SCHEMES)))
+def test_step_on_pi_matches_oracle(oracle_mod, pi_dir, flags, schemes):
+    _gpu()
+    from fesom2_tracer_dwarf_gb300 import engine, synthetic
+
+    kw = FLAGS[flags]
+    om, m = oracle_mod.Mesh.from_files(pi_dir, **kw), _mesh(pi_dir, upload=True, **kw)
+    rng = np.random.default_rng(zlib.crc32(f"pi/{flags}/{schemes}".encode()))
+    vel, w = synthetic.random_flow(m, rng, umax=0.2, wmax=2e-5)
+    T = synthetic.random_field(m, rng, 2)
+    dt = 900.0
+    sch = schemes + (0.7, 0.6)
+    vals = np.ascontiguousarray(T.copy())
+    W = oracle_mod.Work(om)
+    for _ in range(3):
+        oracle_mod.analytic_step(om, W, dt, vel, w, vals, vals.copy(), [sch] * 2, copy_ab=True)
+    for precision in ("fp64", "fp32"):
+        eng = engine.TracerAdvection(m, 2, precision, *schemes, ph=0.7, pv=0.6, copy_ab=True)
+        eng.set_tracers(T)
+        eng.set_velocity(vel, w)
+        eng.step(dt, 3)
+        torch.cuda.synchronize()
+        got = eng.values()
+        if precision == "fp64":
+            assert np.array_equal(got, vals), f"max |diff| {np.abs(got - vals).max()}"
+        else:
+            assert np.abs(got - vals).max() <= 1e-5 * max(1.0, np.abs(vals).max())
+
+
+@pytest.mark.gpu
+def test_reference_mesh_from_files_workflow(oracle_mod, pi_dir):
+    """python/test_mesh_from_files.py through the C ABI: load the pi mesh,
+    allocate T and S, zero velocity, 5 steps of dt = 1e-3, statistics."""
+    _gpu()
+    import ctypes
+
+    from fesom2_tracer_dwarf_gb300.demo_tracer import FESOMTracerAdvection
+
+    t = FESOMTracerAdvection(verbose=False)
+    t.cleanup()
+    try:
+        L = t.lib
+        assert t.initialize_mpi(0) == 0
+        assert L.tracer_load_mesh_from_files(pi_dir.encode()) == 0
+        nz, nn = ctypes.c_int(), ctypes.c_int()
+        assert L.tracer_get_size(ctypes.byref(nz), ctypes.byref(nn)) == 0
+        assert (nz.value + 1, nn.value) == (48, 3140)
+        nl, nod2D = nz.value + 1, nn.value
+        assert t.allocate_tracers(2, nl, nod2D, 2) == 0
+        temp = np.zeros((nz.value, nod2D), order="F")
+        for k in range(nz.value):
+            temp[k, :] = 20.0 - 15.0 * k / max(1, nz.value - 1)
+        assert t.set_values(1, temp) == 0
+        assert t.set_values(2, np.full((nz.value, nod2D), 35.0, order="F")) == 0
+        assert L.tracer_set_velocity_zero(nl, nod2D, 3 * nod2D) == 0
+        assert t.init_ale_arrays() == 0 and t.init_for_advection() == 0 and t.init_complete() == 0
+        om = oracle_mod.Mesh.from_files(pi_dir)
+        ref = om.stats(np.ascontiguousarray(temp.T))
+        for _ in range(5):
+            assert t.advect_step(1.0e-3) == 0
+            st = t.get_statistics()
+            assert st["min"] == ref[0] and st["max"] == ref[1]
+            assert abs(st["sum"] - ref[2]) <= 1e-12 * abs(ref[2])
+        assert np.array_equal(t.get_tracer_values(), temp)
+        assert t.finalize_mpi() == 0
+    finally:
+        t.cleanup()
