@@ -45,13 +45,16 @@ def node_xy(m: Mesh):
 def random_field(m: Mesh, rng, K: int = 1) -> np.ndarray:
     """Smooth random tracer values (K, N, nz) for parity tests."""
     x, y = node_xy(m)
+    # domain extent: the analytic mesh's, else the span of the coordinates
+    Lx = m.Lx or float(np.ptp(x)) or 1.0
+    Ly = m.Ly or float(np.ptp(y)) or 1.0
     out = np.zeros((K, m.N, m.nz))
     z = np.arange(m.nz) / max(m.nz - 1, 1)
     for t in range(K):
         a = rng.uniform(0.5, 2.0, 4)
         ph = rng.uniform(0, 2 * np.pi, 4)
-        base = (a[0] * np.sin(2 * np.pi * x / m.Lx + ph[0]) * np.cos(2 * np.pi * y / m.Ly + ph[1])
-                + a[1] * np.sin(4 * np.pi * x / m.Lx + ph[2]))
+        base = (a[0] * np.sin(2 * np.pi * x / Lx + ph[0]) * np.cos(2 * np.pi * y / Ly + ph[1])
+                + a[1] * np.sin(4 * np.pi * x / Lx + ph[2]))
         out[t] = 10.0 + base[:, None] * (1.0 - 0.5 * z)[None, :] - 3.0 * z[None, :] + a[3] * np.cos(6 * z + ph[3])
         out[t] += rng.normal(0, 0.2, size=(m.N, m.nz))
     return out
