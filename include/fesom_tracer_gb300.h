@@ -78,7 +78,12 @@ int tracer_set_velocity(const double* uv, const double* w, int nl, int nod2D, in
 int tracer_init_complete(void);
 /* lib/tracer_c_interface.F90:769. Restart partitions are not read: -1. */
 int tracer_load_mesh_partition(const char* restart_dir);
-/* lib/tracer_c_interface.F90:830. FESOM ASCII mesh reader: not provided, -1. */
+/* lib/tracer_c_interface.F90:830. Reads the FESOM mesh files of mesh_path
+ * (nod2d.out, elem2d.out, aux3d.out, edgenum.out, edges.out, edge_tri.out,
+ * elvls.out, nlvls.out) as one partition with mesh_setup's set-up and the
+ * reference's defaults (fgb_hmesh_from_files with flags 0) and marks the
+ * system initialised; the dist_<npes>/ lists are not read. -1 with a message
+ * if a file is missing or malformed. */
 int tracer_load_mesh_from_files(const char* mesh_path);
 /* lib/tracer_c_interface.F90:875. Layer thicknesses from zbar. */
 int tracer_init_ale_arrays(void);
