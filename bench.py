@@ -174,6 +174,16 @@ def stage_bytes(m, K, s, ver, fct=True, copy_ab=True, wsplit=False):
     return b
 
 
+NOMINAL_HBM_GBS = 8000.0
+
+
+def compulsory_bytes(s, K, ver):
+    """Lower bound per tracer-cell update, not the roofline: the tracer read
+    and written once (2 s) and the shared fields read once (uv 4, helem 2, w,
+    area, hnode, hnode_new, areasvol, +2 for QR4C's Z and zbar) per K tracers."""
+    return 2 * s + s * (11 + (2 if ver == "QR4C" else 0)) / K
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -533,7 +543,12 @@ def run_gpu(args):
         "step_roofline": {"algorithmic_bytes_per_step": step_bytes,
                           "bytes_per_tracer_cell": step_bytes / cells,
                           "achieved_gbs": step_bytes / (ms / 1e3) / 1e9,
-                          "frac": step_bytes / (ms / 1e3) / 1e9 / peak},
+                          "frac": step_bytes / (ms / 1e3) / 1e9 / peak,
+                          # against the nominal 8.0 TB/s of HBM3e
+                          "frac_nominal": step_bytes / (ms / 1e3) / 1e9 / NOMINAL_HBM_GBS,
+                          # informational: read T once, write T once, the shared fields once
+                          "compulsory_bytes_per_tracer_cell": compulsory_bytes(s, K, cfg["ver"]),
+                          "compulsory_frac": compulsory_bytes(s, K, cfg["ver"]) * cells / (ms / 1e3) / 1e9 / peak},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "steps": e2e_steps, "ms_per_step": e2e_ms / e2e_steps},
         "gpu_launches": launches,
