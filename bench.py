@@ -52,6 +52,13 @@ WORKLOADS = {
     # MUSCL-FCT + PPM; FP32 form against plain FP64 over 100 steps.
     "closed_1024": dict(kind="closed", nx=1025, L=1024e3, nz=64, min_layers=8, K=2, hor="MUSCL", ver="PPM",
                         lim="FCT", dt=400.0, precision="fp32", compare_fp64=True, report_steps=100),
+    # An unstructured global ocean mesh: the reference's pi mesh (coasts,
+    # ragged bottom, 47 layers) with every triangle split into four 5 times
+    # (3.0 M nodes, 9.0 M edges); FP32 form against plain FP64.
+    "pi_refined5": dict(kind="files", refine=5, nz=47, K=4, hor="MUSCL", ver="PPM", lim="FCT", dt=600.0,
+                        precision="fp32", compare_fp64=True, report_steps=3),
+    "pi_refined3": dict(kind="files", refine=3, nz=47, K=4, hor="MUSCL", ver="PPM", lim="FCT", dt=600.0,
+                        precision="fp32", compare_fp64=False),
     # Batching form: 16 periodic meshes of seeded uneven size (64..1024 nodes a
     # side, 16..64 layers), 8 tracers, one launch per stage over all of them,
     # 50 steps per CUDA graph; against per-mesh sequential plain FP64 steps.
@@ -248,6 +255,44 @@ def _flat_part(n, nz, precision, device, dt, cfl, K, seed, upload=True):
     return m, vel, w, T
 
 
+_FILES_CACHE = {}
+
+
+def _files_case(cfg, precision, device, seed):
+    """The refined pi mesh (host set-up shared by both forms), a layered
+    streamfunction flow tapered at the coasts with W from continuity, and T, S
+    and passive blobs; velocity, W and tracers built padded on the device."""
+    import numpy as np
+    import torch
+
+    from fesom2_tracer_dwarf_gb300 import synthetic
+    from fesom2_tracer_dwarf_gb300.mesh import Mesh
+    from fesom2_tracer_dwarf_gb300.meshfiles import refine
+
+    key = (cfg["refine"], cfg["K"], seed)
+    if key not in _FILES_CACHE:
+        with np.load(os.path.join(ROOT, "tests", "golden", "pi_mesh.npz")) as z:
+            base = {k: z[k] for k in z.files}
+        m = Mesh.from_arrays(**refine(base, cfg["refine"]), euler_degrees=True, cyclic_2pi=True)
+        rng = np.random.default_rng(seed)
+        u, s, w = synthetic.layered_flow(m, rng, cfg["dt"], cfl=0.4)
+        T = [synthetic.gaussian_T(m, rng), synthetic.salinity(m, rng)]
+        T += [synthetic.passive_blob(m, rng) for _ in range(cfg["K"] - 2)]
+        _FILES_CACHE.clear()
+        _FILES_CACHE[key] = (m, u, s, w, T)
+    m, u, s, w, T = _FILES_CACHE[key]
+    dt_ = torch.float32 if precision == "fp32" else torch.float64
+    st = torch.zeros(m.LZ, dtype=dt_, device=device)
+    st[: m.nz] = torch.from_numpy(s).to(device, dt_)
+    vel = torch.from_numpy(u).to(device, dt_)[:, None, :] * st[None, :, None]
+    wt = torch.zeros(m.N, m.LW, dtype=dt_, device=device)
+    wt[:, : m.nl] = torch.from_numpy(w).to(device, dt_)
+    T0 = torch.zeros(len(T), m.N, m.LZ, dtype=dt_, device=device)
+    for i, t in enumerate(T):
+        T0[i, :, : m.nz] = torch.from_numpy(t).to(device, dt_)
+    return m, vel, wt, T0
+
+
 def build_case(cfg, precision, device, seed=20260301):
     """Mesh, engine and initial tracer values (engine layout) of a workload."""
     import numpy as np
@@ -268,6 +313,12 @@ def build_case(cfg, precision, device, seed=20260301):
             we = w.clamp(-c, c)
             eng.load_padded(we=we, wi=w - we)
             del we
+    elif cfg["kind"] == "files":
+        m, vel, w, T0 = _files_case(cfg, precision, device, seed)
+        eng = TracerAdvection(m, cfg["K"], precision, *sch, copy_ab=True, device=device,
+                              tracer_vec=cfg.get("tracer_vec") if precision == "fp32" else None)
+        eng.load_padded(T=T0, vel=vel, w=w)
+        del vel, w, T0
     elif cfg["kind"] == "closed":
         rng = np.random.default_rng(seed)
         zb = synthetic.stretched_zbar(cfg["nz"], 5.0, 250.0)
@@ -521,6 +572,11 @@ def run_gpu(args):
     elif cfg["kind"] == "closed":
         mesh_desc = (f"{cfg['nx'] - 1}x{cfg['nx'] - 1} closed basin, seeded bathymetry, "
                      f"{cfg['min_layers']}..{cfg['nz']} layers 5->250 m")
+    elif cfg["kind"] == "files":
+        lev = m.get("nlevels_nod2D") - 1
+        mesh_desc = (f"the reference's pi mesh (global ocean, coasts) with each triangle split into four "
+                     f"{cfg['refine']} times, Morton-ordered nodes; {lev.min()}..{lev.max()} layers "
+                     f"(mean {lev.mean():.1f}) of 47; synthetic layered flow, W from continuity")
     else:
         mesh_desc = "union of %d periodic meshes (n, layers, CFL): %s" % (
             cfg["parts"], ", ".join(f"{n}^2/{z}/{c:.2f}" for n, z, c in batch_parts(cfg)))

@@ -67,7 +67,7 @@ REFERENCE_SYMBOLS = [
 ]
 EXTENSION_SYMBOLS = ["tracer_generate_analytic_mesh", "tracer_set_schemes", "tracer_set_precision"]
 ENGINE_SYMBOLS = [
-    "fgb_last_error", "fgb_version", "fgb_hmesh_analytic", "fgb_hmesh_from_files", "fgb_hmesh_union", "fgb_hmesh_free", "fgb_hmesh_sizes", "fgb_hmesh_get",
+    "fgb_last_error", "fgb_version", "fgb_hmesh_analytic", "fgb_hmesh_from_files", "fgb_hmesh_from_arrays", "fgb_hmesh_union", "fgb_hmesh_free", "fgb_hmesh_sizes", "fgb_hmesh_get",
     "fgb_hmesh_set_vertical", "fgb_mesh_create", "fgb_mesh_free", "fgb_mesh_dims", "fgb_mesh_update_vertical",
     "fgb_workspace_bytes", "fgb_workspace_offsets", "fgb_adv_step", "fgb_adv_stages", "fgb_stats_scratch_bytes",
     "fgb_tracer_stats", "fgb_tracer_stats_grouped", "fgb_last_launch_count", "fgb_static_workspace_bytes", "fgb_adv_step_static",
@@ -95,6 +95,8 @@ def load(build_if_missing: bool = True):
                                               ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                               _dp, _ip, ctypes.POINTER(_vp)]),
         "fgb_hmesh_from_files": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(_vp)]),
+        "fgb_hmesh_from_arrays": (ctypes.c_int, [ctypes.c_int] * 5 + [_dp, _ip, _ip, _ip, _ip, _ip, _dp, ctypes.c_int,
+                                                                     ctypes.POINTER(_vp)]),
         "fgb_hmesh_free": (None, [_vp]),
         "fgb_hmesh_sizes": (ctypes.c_int, [_vp, _llp]),
         "fgb_hmesh_get": (ctypes.c_longlong, [_vp, ctypes.c_char_p, _vp, _ip]),

@@ -151,6 +151,22 @@ int fgb_hmesh_from_files(const char* dir, int flags, fgb_hmesh** out) {
   return 0;
 }
 
+int fgb_hmesh_from_arrays(int nod2D, int elem2D, int edge2D, int edge2D_in, int nl, const double* lonlat,
+                          const int* elem, const int* edges, const int* edge_tri, const int* elvls,
+                          const int* nlvls, const double* zbar, int flags, fgb_hmesh** out) {
+  if (!out || !lonlat || !elem || !edges || !edge_tri || !elvls || !nlvls || !zbar) {
+    set_error("null argument");
+    return -1;
+  }
+  if (flags & ~7) { set_error("unknown mesh-file flags"); return -1; }
+  std::string err;
+  HostMesh* m = build_from_arrays(nod2D, elem2D, edge2D, edge2D_in, nl, lonlat, elem, edges, edge_tri, elvls, nlvls,
+                                  zbar, flags, &err);
+  if (!m) { set_error(err); return -1; }
+  *out = new fgb_hmesh{m};
+  return 0;
+}
+
 int fgb_hmesh_union(const fgb_hmesh* const* parts, int count, fgb_hmesh** out) {
   if (!parts || !out || count < 1) { set_error("bad argument"); return -1; }
   std::vector<const HostMesh*> ps(count);

@@ -81,6 +81,12 @@ constexpr int kFileNoRotation = 1;
 constexpr int kFileEulerDegrees = 2;
 constexpr int kFileCyclic2Pi = 4;
 HostMesh* build_from_files(const std::string& dir, int flags, std::string* err);
+// The same from arrays laid out as the files are: lonlat (N,2) degrees, elem
+// (M,3), edges and edge_tri (E,2) 1-based (edge_tri <= 0: none), elvls (M),
+// nlvls (N), zbar (nl).
+HostMesh* build_from_arrays(int N, int M, int E, int Ein, int nl, const double* lonlat, const int* elem,
+                            const int* edges, const int* edge_tri, const int* elvls, const int* nlvls,
+                            const double* zbar, int flags, std::string* err);
 
 // Derived tables (CSR, cluster, per-edge level windows). Called by the builders.
 void build_tables(HostMesh& m);

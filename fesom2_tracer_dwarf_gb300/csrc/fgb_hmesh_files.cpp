@@ -183,18 +183,50 @@ HostMesh* build_from_files(const std::string& dir_in, int flags, std::string* er
   if (!f.record(&M, 1, &e)) return bad(e);
   if (M < 1) return bad("elem2d.out: no elements");
   std::vector<int> en((size_t)3 * M);
-  for (int k = 0; k < M; ++k) {
+  for (int k = 0; k < M; ++k)
     if (!f.record(&en[3 * k], 3, &e)) return bad(e);
-    for (int j = 0; j < 3; ++j) {
-      if (en[3 * k + j] < 1 || en[3 * k + j] > N) return bad("elem2d.out: node index out of range");
-      en[3 * k + j] -= 1;
-    }
-  }
   // aux3d.out: levels (lib/oce_mesh.F90:425-455)
   if (!f.open(dir + "aux3d.out", &e)) return bad(e);
   int nl = 0;
   if (!f.record(&nl, 1, &e)) return bad(e);
   if (nl < 3) return bad("aux3d.out: number of levels is less than 3");
+  std::vector<double> zbar(nl);
+  if (!f.items(zbar.data(), nl, &e)) return bad(e);
+  // edgenum.out, edges.out, edge_tri.out (load_edges, lib/oce_mesh.F90:1617-1848)
+  if (!f.open(dir + "edgenum.out", &e)) return bad(e);
+  int E = 0, Ein = 0;
+  if (!f.record(&E, 1, &e) || !f.record(&Ein, 1, &e)) return bad(e);
+  if (E < 3 || Ein < 0 || Ein > E) return bad("edgenum.out: bad edge counts");
+  std::vector<int> edges((size_t)2 * E), edge_tri((size_t)2 * E);
+  ListFile g;
+  if (!f.open(dir + "edges.out", &e) || !g.open(dir + "edge_tri.out", &e)) return bad(e);
+  for (int k = 0; k < E; ++k)
+    if (!f.record(&edges[2 * k], 2, &e) || !g.record(&edge_tri[2 * k], 2, &e)) return bad(e);
+  // elvls.out, nlvls.out (find_levels, lib/oce_mesh.F90:807-1001)
+  std::vector<int> elvls(M), nlvls(N);
+  if (!f.open(dir + "elvls.out", &e)) return bad(e);
+  for (int k = 0; k < M; ++k)
+    if (!f.record(&elvls[k], 1, &e)) return bad(e);
+  if (!f.open(dir + "nlvls.out", &e)) return bad(e);
+  for (int k = 0; k < N; ++k)
+    if (!f.record(&nlvls[k], 1, &e)) return bad(e);
+  return build_from_arrays(N, M, E, Ein, nl, lonlat.data(), en.data(), edges.data(), edge_tri.data(), elvls.data(),
+                           nlvls.data(), zbar.data(), flags, err);
+}
+
+HostMesh* build_from_arrays(int N, int M, int E, int Ein, int nl, const double* lonlat, const int* elem,
+                            const int* edges_in, const int* edge_tri_in, const int* elvls, const int* nlvls,
+                            const double* zbar_in, int flags, std::string* err) {
+  auto bad = [&](const std::string& msg) -> HostMesh* {
+    if (err) *err = msg;
+    return nullptr;
+  };
+  if (N < 3 || M < 1 || nl < 3 || E < 3 || Ein < 0 || Ein > E) return bad("bad mesh sizes");
+  std::vector<int> en((size_t)3 * M);
+  for (size_t i = 0; i < (size_t)3 * M; ++i) {
+    if (elem[i] < 1 || elem[i] > N) return bad("elem2d.out: node index out of range");
+    en[i] = elem[i] - 1;
+  }
   auto* mp = new HostMesh();
   HostMesh& m = *mp;
   auto bad_m = [&](const std::string& msg) -> HostMesh* {
@@ -203,52 +235,37 @@ HostMesh* build_from_files(const std::string& dir_in, int flags, std::string* er
   };
   m.nl = nl;
   m.nz = nl - 1;
-  m.zbar.resize(nl);
-  if (!f.items(m.zbar.data(), nl, &e)) return bad_m(e);
-  if (m.zbar[1] > 0.0)
+  m.zbar.assign(zbar_in, zbar_in + nl);
+  if (m.zbar[1] > 0.0)  // zbar is negative (lib/oce_mesh.F90:447)
     for (double& z : m.zbar) z = -z;
   m.Z.resize(nl - 1);
   for (int k = 0; k < nl - 1; ++k) m.Z[k] = 0.5 * (m.zbar[k] + m.zbar[k + 1]);
-  // edgenum.out, edges.out, edge_tri.out (load_edges, lib/oce_mesh.F90:1617-1848)
-  if (!f.open(dir + "edgenum.out", &e)) return bad_m(e);
-  int E = 0, Ein = 0;
-  if (!f.record(&E, 1, &e) || !f.record(&Ein, 1, &e)) return bad_m(e);
-  if (E < 3 || Ein < 0 || Ein > E) return bad_m("edgenum.out: bad edge counts");
   m.edges.resize((size_t)2 * E);
   m.edge_tri.resize((size_t)2 * E);
-  ListFile g;
-  if (!f.open(dir + "edges.out", &e) || !g.open(dir + "edge_tri.out", &e)) return bad_m(e);
   for (int k = 0; k < E; ++k) {
-    int a[2], t[2];
-    if (!f.record(a, 2, &e) || !g.record(t, 2, &e)) return bad_m(e);
     for (int j = 0; j < 2; ++j) {
-      if (a[j] < 1 || a[j] > N) return bad_m("edges.out: node index out of range");
-      if (t[j] > M) return bad_m("edge_tri.out: element index out of range");
-      m.edges[2 * k + j] = a[j] - 1;
-      m.edge_tri[2 * k + j] = t[j] > 0 ? t[j] - 1 : -1;  // where (edge_tri < 0) edge_tri = 0
+      const int a = edges_in[2 * k + j], t = edge_tri_in[2 * k + j];
+      if (a < 1 || a > N) return bad_m("edges.out: node index out of range");
+      if (t > M) return bad_m("edge_tri.out: element index out of range");
+      m.edges[2 * k + j] = a - 1;
+      m.edge_tri[2 * k + j] = t > 0 ? t - 1 : -1;  // where (edge_tri < 0) edge_tri = 0
     }
     if (m.edge_tri[2 * k] < 0) return bad_m("edge_tri.out: an edge without its first element");
   }
-  // elvls.out, nlvls.out (find_levels, lib/oce_mesh.F90:807-1001); ulevels = 1
-  m.nlevels.resize(M);
+  // levels (find_levels); ulevels = 1
+  m.nlevels.assign(elvls, elvls + M);
   m.ulevels.assign(M, 1);
-  m.nlev_nod.resize(N);
+  m.nlev_nod.assign(nlvls, nlvls + N);
   m.ulev_nod.assign(N, 1);
-  if (!f.open(dir + "elvls.out", &e)) return bad_m(e);
-  for (int k = 0; k < M; ++k)
-    if (!f.record(&m.nlevels[k], 1, &e)) return bad_m(e);
-  if (!f.open(dir + "nlvls.out", &e)) return bad_m(e);
-  for (int k = 0; k < N; ++k)
-    if (!f.record(&m.nlev_nod[k], 1, &e)) return bad_m(e);
   for (int k = 0; k < M; ++k)
     if (m.nlevels[k] < 2 || m.nlevels[k] > nl) return bad_m("elvls.out: levels outside 2..nl");
   for (int k = 0; k < N; ++k)
     if (m.nlev_nod[k] < 2 || m.nlev_nod[k] > nl) return bad_m("nlvls.out: levels outside 2..nl");
-
   m.N = N;
   m.M = M;
   m.E = E;
   m.edge2D_in = Ein;
+  std::vector<double> ll(lonlat, lonlat + (size_t)2 * N);
   m.periodic = 0;
   m.cyclic = (flags & kFileCyclic2Pi) ? 2.0 * kPiRef : 360.0;
   const double cyc = m.cyclic;
@@ -263,7 +280,7 @@ HostMesh* build_from_files(const std::string& dir_in, int flags, std::string* er
   const double rad = kPiRef / 180.0;  // lib/oce_modules.F90:20
   m.coord.resize((size_t)2 * N);
   for (int n = 0; n < N; ++n) {
-    double x = lonlat[2 * n] * rad, y = lonlat[2 * n + 1] * rad;
+    double x = ll[2 * n] * rad, y = ll[2 * n + 1] * rad;
     if (!(flags & kFileNoRotation)) {
       const double rx = x, ry = y;
       rot.g2r(rx, ry, x, y);

@@ -79,6 +79,29 @@ class Mesh:
         return self
 
     @classmethod
+    def from_arrays(cls, lonlat, elem, edges, edge_tri, edgenum, elvls, nlvls, zbar, rotate: bool = True,
+                    euler_degrees: bool = False, cyclic_2pi: bool = False, upload: bool = True) -> "Mesh":
+        """The same as ``from_files`` from arrays laid out as the files are
+        (``fgb_hmesh_from_arrays``; e.g. ``meshfiles.refine`` output)."""
+        L = _lib.load()
+        flags = (0 if rotate else 1) | (2 if euler_degrees else 0) | (4 if cyclic_2pi else 0)
+        i32 = [np.ascontiguousarray(a, dtype=np.int32) for a in (elem, edges, edge_tri, elvls, nlvls)]
+        ll = np.ascontiguousarray(lonlat, dtype=np.float64)
+        zb = np.ascontiguousarray(zbar, dtype=np.float64)
+        h = ctypes.c_void_p()
+        rc = L.fgb_hmesh_from_arrays(len(ll), len(i32[0]), int(edgenum[0]), int(edgenum[1]), len(zb),
+                                     ll.ctypes.data_as(_lib._dp), *[a.ctypes.data_as(_lib._ip) for a in i32],
+                                     zb.ctypes.data_as(_lib._dp), flags, ctypes.byref(h))
+        _lib.check(rc, "fgb_hmesh_from_arrays")
+        self = cls.__new__(cls)
+        self.nx = self.ny = None
+        self.Lx = self.Ly = self.depth = None
+        self.periodic, self.cluster_full, self.orient_left = False, False, False
+        self.parts = None
+        self._attach(h, upload)
+        return self
+
+    @classmethod
     def union(cls, parts, upload: bool = True) -> "Mesh":
         """Disjoint union of independent meshes (``fgb_hmesh_union``), one
         mesh that a single launch per stage advances. ``parts`` keeps, per

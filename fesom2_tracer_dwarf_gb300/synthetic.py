@@ -42,12 +42,20 @@ def node_xy(m: Mesh):
     return c[:, 0] * R_EARTH, c[:, 1] * R_EARTH
 
 
+def _xyL(m: Mesh):
+    """Node coordinates (m) and the domain extent: the analytic mesh's Lx, Ly,
+    or for meshes read from files the coordinates shifted to start at 0 and
+    their span."""
+    x, y = node_xy(m)
+    if m.Lx:
+        return x, y, m.Lx, m.Ly
+    x, y = x - x.min(), y - y.min()
+    return x, y, float(x.max()) or 1.0, float(y.max()) or 1.0
+
+
 def random_field(m: Mesh, rng, K: int = 1) -> np.ndarray:
     """Smooth random tracer values (K, N, nz) for parity tests."""
-    x, y = node_xy(m)
-    # domain extent: the analytic mesh's, else the span of the coordinates
-    Lx = m.Lx or float(np.ptp(x)) or 1.0
-    Ly = m.Ly or float(np.ptp(y)) or 1.0
+    x, y, Lx, Ly = _xyL(m)
     out = np.zeros((K, m.N, m.nz))
     z = np.arange(m.nz) / max(m.nz - 1, 1)
     for t in range(K):
@@ -131,15 +139,15 @@ def streamfunction_flow(m: Mesh, rng, dt: float, cfl: float = 0.4, nmodes: int =
     """Horizontal velocity (M, nz, 2) = rotated P1 gradient of a random-phase
     Fourier streamfunction with a depth decay, scaled to the target CFL at dt,
     and W (N, nl) diagnosed from continuity."""
-    x, y = node_xy(m)
+    x, y, Lx, Ly = _xyL(m)
     psi = np.zeros(m.N)
     for _ in range(nmodes):
         kx, ky = rng.integers(1, kmax + 1, size=2)
         ph = rng.uniform(0, 2 * np.pi)
-        psi += np.sin(2 * np.pi * (kx * x / m.Lx + ky * y / m.Ly) + ph) / np.hypot(kx, ky)
+        psi += np.sin(2 * np.pi * (kx * x / Lx + ky * y / Ly) + ph) / np.hypot(kx, ky)
     if psi_wall_zero and not m.periodic:
         # closed basin: taper to zero on the walls
-        psi *= np.sin(np.pi * x / m.Lx) * np.sin(np.pi * y / m.Ly)
+        psi *= np.sin(np.pi * x / Lx) * np.sin(np.pi * y / Ly)
     en = m.get("elem_nodes")
     gs = m.get("gradient_sca")
     dpx = (gs[:, 0:3] * psi[en]).sum(1)
@@ -180,6 +188,85 @@ def streamfunction_flow(m: Mesh, rng, dt: float, cfl: float = 0.4, nmodes: int =
     return vel, w
 
 
+def layered_flow(m: Mesh, rng, dt: float, cfl: float = 0.4, nmodes: int = 8, kmax: int = 8,
+                 efold: float = 500.0, coast_taper: int = 3):
+    """streamfunction_flow for large ragged meshes (ulevels = 1, helem the
+    zbar thicknesses): velocity (M, 2) of the top layer and the depth profile
+    s (nz) -- the layer-z velocity is u * s[z] -- and W (N, nl) from the
+    discrete continuity of diagnose_w, computed per edge side with
+    difference arrays over the layer breakpoints instead of per layer. The
+    streamfunction is tapered to zero over `coast_taper` edge hops from the
+    coast (nodes of edges with one element), so the rotated gradient's volume
+    fluxes telescope around every dual cell and W comes from the bottom steps
+    only. Scaled so that the largest horizontal and vertical Courant numbers
+    at dt are cfl."""
+    x, y, Lx, Ly = _xyL(m)
+    psi = np.zeros(m.N)
+    for _ in range(nmodes):
+        kx, ky = rng.integers(1, kmax + 1, size=2)
+        ph = rng.uniform(0, 2 * np.pi)
+        psi += np.sin(2 * np.pi * (kx * x / Lx + ky * y / Ly) + ph) / np.hypot(kx, ky)
+    if coast_taper > 0:
+        ed0, et0 = m.get("edges"), m.get("edge_tri")
+        hops = np.full(m.N, coast_taper, np.int64)
+        hops[ed0[et0[:, 1] < 0].reshape(-1)] = 0
+        for _ in range(coast_taper):
+            nb = np.minimum(hops[ed0[:, 0]], hops[ed0[:, 1]]) + 1
+            np.minimum.at(hops, ed0[:, 0], nb)
+            np.minimum.at(hops, ed0[:, 1], nb)
+        psi *= np.minimum(hops, coast_taper) / coast_taper
+    en = m.get("elem_nodes")
+    gs = m.get("gradient_sca")
+    u = np.stack([-(gs[:, 3:6] * psi[en]).sum(1), (gs[:, 0:3] * psi[en]).sum(1)], axis=1)
+    zb = m.get("zbar")
+    h = zb[:-1] - zb[1:]
+    s = np.exp(0.5 * (zb[:-1] + zb[1:]) / efold)
+    nz, N = m.nz, m.N
+    ed, et, cr, lev = m.get("edges"), m.get("edge_tri"), m.get("edge_cross_dxdy"), m.get("edge_lev")
+    has2 = et[:, 1] >= 0
+    e1, e2 = et[:, 0], np.where(has2, et[:, 1], 0)
+    # per-side 2-D volume flux factors (the v1, v2 of _edge_vflux without s h)
+    c1 = -u[e1, 1] * cr[:, 0] + u[e1, 0] * cr[:, 1]
+    c2 = np.where(has2, u[e2, 1] * cr[:, 2] - u[e2, 0] * cr[:, 3], 0.0)
+    L1, L2 = lev[:, 1], np.where(has2, lev[:, 3], 0)  # deepest layer of each side
+    # divergence: G[n, z] = sum over incident sides reaching layer z of +-c
+    P = np.zeros((N, nz + 2))
+    for col, sg in ((ed[:, 0], -1.0), (ed[:, 1], 1.0)):
+        np.add.at(P, (col, L1), sg * c1)
+        np.add.at(P, (col, L2), sg * c2)
+    G = np.cumsum(P[:, ::-1], axis=1)[:, ::-1]
+    D = G[:, 1:nz + 1] * (s * h)[None, :]
+    del P, G
+    area = m.get("area")
+    nlev = m.get("nlevels_nod2D")
+    w = np.zeros((N, m.nl))
+    for k in range(nz - 1, -1, -1):
+        wet = k < nlev - 1
+        w[:, k] = np.where(wet, (D[:, k] + w[:, k + 1] * area[:, k + 1]) / np.where(area[:, k] > 0, area[:, k], 1.0),
+                           0.0)
+    del D
+    # horizontal Courant numbers: upwind outflow, piecewise constant between
+    # the two sides' bottoms
+    lmin, lmax = np.minimum(L1, L2), np.maximum(L1, L2)
+    cdeep = np.where(L1 >= L2, c1, c2)
+    Q = np.zeros((N, nz + 2))
+    for col, sg in ((ed[:, 0], 1.0), (ed[:, 1], -1.0)):
+        a = np.maximum(sg * (c1 + c2), 0.0)
+        b = np.maximum(sg * cdeep, 0.0)
+        np.add.at(Q, (col, np.ones_like(lmin)), a)
+        np.add.at(Q, (col, lmin + 1), b - a)
+        np.add.at(Q, (col, lmax + 1), -b)
+    out = np.cumsum(Q, axis=1)[:, 1:nz + 1] * s[None, :]
+    del Q
+    asv = m.get("areasvol")[:, :nz]
+    wetl = np.arange(nz)[None, :] < (nlev - 1)[:, None]
+    ch = float(np.max(np.where(wetl, dt * out / np.where(asv > 0, asv, 1.0), 0.0)))
+    hmin = np.minimum(np.concatenate([h[:1], h[:-1]]), h)  # thinner layer at each interface k < nz
+    cv = float(np.max(np.abs(w[:, :nz]) * dt / hmin[None, :]))
+    scale = cfl / max(ch, cv, 1e-300)
+    return u * scale, s, w * scale
+
+
 def _node_out(m: Mesh, vf: np.ndarray) -> np.ndarray:
     edges = m.get("edges")
     out = np.zeros((m.N,) + vf.shape[1:])
@@ -189,10 +276,10 @@ def _node_out(m: Mesh, vf: np.ndarray) -> np.ndarray:
 
 
 def gaussian_T(m: Mesh, rng) -> np.ndarray:
-    x, y = node_xy(m)
+    x, y, Lx, Ly = _xyL(m)
     zmid = 0.5 * (m.get("zbar_3d_n")[0, :-1] + m.get("zbar_3d_n")[0, 1:])
     H = -m.get("zbar_3d_n")[0, -1]
-    r2 = ((x - 0.5 * m.Lx) ** 2 + (y - 0.5 * m.Ly) ** 2) / (2 * (m.Lx / 8) ** 2)
+    r2 = ((x - 0.5 * Lx) ** 2 + (y - 0.5 * Ly) ** 2) / (2 * (Lx / 8) ** 2)
     zz = (zmid + 0.25 * H) ** 2 / (2 * (0.25 * H) ** 2)
     return 2.0 + 20.0 * np.exp(-r2[:, None] - zz[None, :]) + rng.normal(0, 0.1, size=(m.N, m.nz))
 
@@ -202,17 +289,17 @@ def salinity(m: Mesh, rng) -> np.ndarray:
 
 
 def passive_blob(m: Mesh, rng) -> np.ndarray:
-    x, y = node_xy(m)
+    x, y, Lx, Ly = _xyL(m)
     zmid = 0.5 * (m.get("zbar_3d_n")[0, :-1] + m.get("zbar_3d_n")[0, 1:])
     H = -m.get("zbar_3d_n")[0, -1]
-    cx, cy = rng.uniform(0, m.Lx), rng.uniform(0, m.Ly)
-    sx, sy = rng.uniform(0.05, 0.2) * m.Lx, rng.uniform(0.05, 0.2) * m.Ly
+    cx, cy = rng.uniform(0, Lx), rng.uniform(0, Ly)
+    sx, sy = rng.uniform(0.05, 0.2) * Lx, rng.uniform(0.05, 0.2) * Ly
     cz, sz = -rng.uniform(0, H), rng.uniform(0.1, 0.5) * H
     dx = np.abs(x - cx)
     dy = np.abs(y - cy)
     if m.periodic:
-        dx = np.minimum(dx, m.Lx - dx)
-        dy = np.minimum(dy, m.Ly - dy)
+        dx = np.minimum(dx, Lx - dx)
+        dy = np.minimum(dy, Ly - dy)
     return np.exp(-(dx / sx) ** 2 - (dy / sy) ** 2)[:, None] * np.exp(-((zmid - cz) / sz) ** 2)[None, :]
 
 

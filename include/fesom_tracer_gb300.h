@@ -147,6 +147,13 @@ int fgb_hmesh_analytic(int nx, int ny, int nl, double Lx, double Ly, double dept
  * FGB_MESH_FILE_CYCLIC_2PI select FESOM2's namelist handling instead. */
 enum { FGB_MESH_FILE_NO_ROTATION = 1, FGB_MESH_FILE_EULER_DEGREES = 2, FGB_MESH_FILE_CYCLIC_2PI = 4 };
 int fgb_hmesh_from_files(const char* dir, int flags, fgb_hmesh** out);
+/* The same from arrays laid out as the files are (a host that holds its mesh
+ * in memory): lonlat (nod2D,2) degrees, elem (elem2D,3), edges and edge_tri
+ * (edge2D,2) 1-based with edge_tri <= 0 for none, elvls (elem2D), nlvls
+ * (nod2D), zbar (nl). */
+int fgb_hmesh_from_arrays(int nod2D, int elem2D, int edge2D, int edge2D_in, int nl, const double* lonlat,
+                          const int* elem, const int* edges, const int* edge_tri, const int* elvls,
+                          const int* nlvls, const double* zbar, int flags, fgb_hmesh** out);
 void fgb_hmesh_free(fgb_hmesh* h);
 /* No counterpart in the reference (the batching form): the disjoint union of
  * `count` host meshes as one mesh, parts in order (node, edge and element

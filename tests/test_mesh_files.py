@@ -20,7 +20,7 @@ import zlib
 import numpy as np
 import pytest
 
-from fesom_files import load_pi, write_mesh_dir, write_pi
+from fesom_files import load_pi, write_mesh_dir, write_pi, write_pi_refined
 
 FLAGS = [dict(), dict(euler_degrees=True, cyclic_2pi=True), dict(rotate=False)]
 REAL = ["coord", "elem_area", "area", "areasvol", "edge_dxdy", "edge_cross_dxdy", "elem_cos", "gradient_sca",
@@ -34,6 +34,11 @@ INDEX = {"elem_nodes": ("elem2D_nodes", 1), "edges": ("edges", 1), "edge_tri": (
 @pytest.fixture(scope="module")
 def pi_dir(tmp_path_factory):
     return write_pi(str(tmp_path_factory.mktemp("pi")))
+
+
+@pytest.fixture(scope="module")
+def pi_refined_dir(tmp_path_factory):
+    return write_pi_refined(str(tmp_path_factory.mktemp("pi_refined")), 1)
 
 
 def _mesh(path, upload=False, **kw):
@@ -98,6 +103,54 @@ def test_malformed_directories_are_refused(tmp_path, pi_dir):
     # the path may end without '/'
     assert _mesh(pi_dir.rstrip("/")).N == 3140
     assert _lib.load().tracer_load_mesh_from_files(str(tmp_path / "missing").encode()) == -1
+
+
+def test_refined_mesh(oracle_mod, pi_refined_dir):
+    """meshfiles.refine: four children per triangle, the topology kept
+    (N - E + M of the pi mesh, -7: a sphere with its coasts cut out),
+    edge_tri(1) left of node1 -> node2, node levels the deepest adjacent
+    element's; the library and the oracle set it up identically, and the
+    arrays path equals the files path."""
+    from fesom2_tracer_dwarf_gb300.mesh import Mesh
+    from fesom2_tracer_dwarf_gb300.meshfiles import _xyz, refine
+
+    d = load_pi()
+    r = refine(d, 1)
+    N, M, E = len(r["lonlat"]), len(r["elem"]), len(r["edges"])
+    assert M == 4 * len(d["elem"]) and N == len(d["lonlat"]) + len(d["edges"])
+    assert N - E + M == len(d["lonlat"]) - len(d["edges"]) + len(d["elem"]) == -7
+    xyz = _xyz(r["lonlat"])
+    ed, et, el = r["edges"] - 1, r["edge_tri"] - 1, r["elem"] - 1
+    third = np.array([[v for v in el[t] if v not in e][0] for e, t in zip(ed, et[:, 0])])
+    assert np.all(np.einsum("ij,ij->i", np.cross(xyz[ed[:, 0]], xyz[ed[:, 1]]), xyz[third]) > 0)
+    assert np.all(et[: r["edgenum"][1], 1] >= 0) and np.all(et[r["edgenum"][1]:, 1] < 0)
+    mx = np.zeros(N, int)
+    np.maximum.at(mx, el.reshape(-1), np.repeat(r["elvls"], 3))
+    assert np.array_equal(mx, r["nlvls"])
+    for flags in FLAGS[:2]:
+        m = _mesh(pi_refined_dir, **flags)
+        om = oracle_mod.Mesh.from_files(pi_refined_dir, **flags)
+        a = Mesh.from_arrays(**r, upload=False, **flags)
+        for name in REAL:
+            assert np.array_equal(m.get(name), om.getd(name).reshape(m.get(name).shape)), name
+            assert np.array_equal(m.get(name), a.get(name)), name
+        assert np.array_equal(m.get("edge_up_dn_tri"), om.geti("edge_up_dn_tri") - 1)
+
+
+def test_layered_flow_is_continuity_consistent(pi_refined_dir):
+    """synthetic.layered_flow's W equals diagnose_w of its velocity, and its
+    Courant numbers are at most the target."""
+    from fesom2_tracer_dwarf_gb300 import synthetic
+
+    m = _mesh(pi_refined_dir, euler_degrees=True, cyclic_2pi=True)
+    u, s, w = synthetic.layered_flow(m, np.random.default_rng(6), 600.0, cfl=0.4)
+    vel = u[:, None, :] * s[None, :, None]
+    assert np.abs(w - synthetic.diagnose_w(m, vel)).max() <= 1e-12 * np.abs(w).max()
+    assert synthetic.max_cfl(m, vel, 600.0) <= 0.4 + 1e-12
+    zb = m.get("zbar")
+    h = zb[:-1] - zb[1:]
+    cv = np.abs(w[:, : m.nz]) * 600.0 / np.minimum(np.concatenate([h[:1], h[:-1]]), h)[None, :]
+    assert cv.max() <= 0.4 + 1e-12
 
 
 def _pi_pair(oracle_mod, pi_dir, **flags):
@@ -170,6 +223,38 @@ def test_step_on_pi_matches_oracle(oracle_mod, pi_dir, flags, schemes):
         eng.set_tracers(T)
         eng.set_velocity(vel, w)
         eng.step(dt, 3)
+        torch.cuda.synchronize()
+        got = eng.values()
+        if precision == "fp64":
+            assert np.array_equal(got, vals), f"max |diff| {np.abs(got - vals).max()}"
+        else:
+            assert np.abs(got - vals).max() <= 1e-5 * max(1.0, np.abs(vals).max())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("schemes", [("MUSCL", "PPM", "FCT"), ("UPW1", "QR4C", "NONE")])
+def test_step_on_refined_pi_matches_oracle(oracle_mod, pi_refined_dir, schemes):
+    """The refined pi mesh (12126 nodes, Morton order) with a layered flow:
+    FP64 bit for bit, FP32 within 1e-5, 4 tracers (one FP32 group of 4)."""
+    _gpu()
+    from fesom2_tracer_dwarf_gb300 import engine, synthetic
+
+    kw = FLAGS[1]
+    om, m = oracle_mod.Mesh.from_files(pi_refined_dir, **kw), _mesh(pi_refined_dir, upload=True, **kw)
+    rng = np.random.default_rng(zlib.crc32(f"pir/{schemes}".encode()))
+    u, s, w = synthetic.layered_flow(m, rng, 900.0, cfl=0.5)
+    vel = np.ascontiguousarray(u[:, None, :] * s[None, :, None])
+    T = synthetic.random_field(m, rng, 4)
+    sch = schemes + (1.0, 1.0)
+    vals = np.ascontiguousarray(T.copy())
+    W = oracle_mod.Work(om)
+    for _ in range(3):
+        oracle_mod.analytic_step(om, W, 900.0, vel, w, vals, vals.copy(), [sch] * 4, copy_ab=True)
+    for precision in ("fp64", "fp32"):
+        eng = engine.TracerAdvection(m, 4, precision, *schemes, copy_ab=True)
+        eng.set_tracers(T)
+        eng.set_velocity(vel, w)
+        eng.step(900.0, 3)
         torch.cuda.synchronize()
         got = eng.values()
         if precision == "fp64":
