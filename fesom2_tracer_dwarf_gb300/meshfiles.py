@@ -18,6 +18,8 @@ The library reads mesh directories itself (``Mesh.from_files``,
 Arrays follow the files: ``lonlat`` (N, 2) degrees, ``elem`` (M, 3) 1-based,
 ``elvls`` (M), ``nlvls`` (N), ``zbar`` (nl), ``edges``/``edge_tri`` (E, 2)
 1-based, ``edgenum`` (edge2D, edge2D_in).
+
+    python -m fesom2_tracer_dwarf_gb300.meshfiles SRC_DIR DST_DIR TIMES
 """
 from __future__ import annotations
 
@@ -163,3 +165,37 @@ def refine(mesh, times=1):
     return dict(lonlat=ll, elem=elem0 + 1, elvls=elvls, nlvls=nlvls, zbar=np.asarray(mesh["zbar"], np.float64),
                 edges=edges + 1, edge_tri=np.where(edge_tri >= 0, edge_tri + 1, 0),
                 edgenum=np.array([len(edges), n_in]))
+
+
+def read_fesom_dir(path):
+    """The arrays ``refine`` takes, from a mesh directory (whitespace-separated
+    items as the reference's list-directed reads take them)."""
+    def items(name, dtype):
+        with open(os.path.join(path, name)) as f:
+            return np.array(f.read().split(), dtype=dtype)
+
+    nod = items("nod2d.out", np.float64)
+    N = int(nod[0])
+    el = items("elem2d.out", np.int64)
+    aux = items("aux3d.out", np.float64)
+    nl = int(aux[0])
+    return dict(lonlat=nod[1:1 + 4 * N].reshape(N, 4)[:, 1:3], elem=el[1:1 + 3 * int(el[0])].reshape(-1, 3),
+                elvls=items("elvls.out", np.int64), zbar=aux[1:1 + nl])
+
+
+def main(argv=None):
+    import sys
+
+    args = sys.argv[1:] if argv is None else argv
+    if len(args) != 3:
+        print(__doc__)
+        return 2
+    r = refine(read_fesom_dir(args[0]), int(args[2]))
+    write_fesom_dir(args[1], r["lonlat"], r["elem"], r["zbar"], r["edges"], r["edge_tri"], r["edgenum"], r["elvls"],
+                    r["nlvls"])
+    print(f"{args[1]}: {len(r['lonlat'])} nodes, {len(r['elem'])} elements, {len(r['edges'])} edges")
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

@@ -9,9 +9,11 @@ the oracle's bit for bit under the reference's defaults and under FESOM2's
 namelist handling; the sizes are those python/test_mesh_from_files.py prints;
 malformed directories are refused; in the oracle a zero velocity leaves the
 tracers unchanged and a continuity-consistent flow keeps a uniform tracer
-uniform on this unstructured, ragged, coastal mesh.
-GPU: the step on the pi mesh equals the oracle (FP64 bit for bit, FP32 to
-1e-5), and the reference's mesh-from-files workflow runs through the C ABI.
+uniform on this unstructured, ragged, coastal mesh; the refinement tool keeps
+the topology and orientation, and its layered flow is continuity-consistent.
+GPU: the step on the pi mesh and on its refinement equals the oracle (FP64 bit
+for bit, FP32 to 1e-5), through the engine and through the C ABI, and the
+reference's mesh-from-files workflow runs through the C ABI.
 """
 import itertools
 import os
@@ -261,6 +263,51 @@ def test_step_on_refined_pi_matches_oracle(oracle_mod, pi_refined_dir, schemes):
             assert np.array_equal(got, vals), f"max |diff| {np.abs(got - vals).max()}"
         else:
             assert np.abs(got - vals).max() <= 1e-5 * max(1.0, np.abs(vals).max())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("schemes", [("MUSCL", "QR4C", "FCT"), ("MFCT", "PPM", "FCT")])
+def test_cabi_steps_on_pi_match_oracle(oracle_mod, pi_dir, schemes):
+    """tracer_load_mesh_from_files + tracer_set_velocity on the pi mesh, three
+    tracer_advect_step calls against the oracle's C-ABI step
+    (lib/tracer_c_interface.F90:163-220 semantics), bit for bit."""
+    _gpu()
+    import ctypes
+
+    from fesom2_tracer_dwarf_gb300 import synthetic
+    from fesom2_tracer_dwarf_gb300.demo_tracer import FESOMTracerAdvection
+
+    om, m = oracle_mod.Mesh.from_files(pi_dir), _mesh(pi_dir)
+    rng = np.random.default_rng(zlib.crc32(f"cabi-pi/{schemes}".encode()))
+    vel, w = synthetic.random_flow(m, rng, umax=0.2, wmax=2e-5)
+    T = synthetic.random_field(m, rng, 1)[0]
+    nz, N, E = m.nz, m.N, m.E
+    uv = np.zeros(nz * E * 2)
+    flat = np.ascontiguousarray(vel).reshape(-1)  # vel(2, nz, M) in Fortran order
+    uv[: flat.size] = flat
+    t = FESOMTracerAdvection(verbose=False)
+    t.cleanup()
+    try:
+        L = t.lib
+        assert L.tracer_load_mesh_from_files(pi_dir.encode()) == 0
+        nzc, nn = ctypes.c_int(), ctypes.c_int()
+        assert L.tracer_get_size(ctypes.byref(nzc), ctypes.byref(nn)) == 0 and (nzc.value, nn.value) == (nz, N)
+        assert t.allocate_tracers(1, m.nl, N) == 0
+        assert t.set_values(1, np.asfortranarray(T.T)) == 0
+        assert t.set_velocity(uv.reshape((nz, E, 2), order="F"), np.asfortranarray(w.T)) == 0
+        assert t.set_schemes(1, *schemes) == 0
+        assert t.init_ale_arrays() == 0 and t.init_for_advection() == 0 and t.init_complete() == 0
+        vals = np.ascontiguousarray(T.copy())
+        vab = vals.copy()
+        del_ttf = np.zeros_like(vals)
+        W = oracle_mod.Work(om)
+        for step in range(3):
+            assert t.advect_step(900.0) == 0
+            oracle_mod.cabi_step(om, W, 900.0, vel, w, vals, vab, del_ttf, *schemes)
+            got = t.get_tracer_values()
+            assert np.array_equal(got.T, vals), f"step {step + 1}: max |diff| {np.abs(got.T - vals).max()}"
+    finally:
+        t.cleanup()
 
 
 @pytest.mark.gpu
