@@ -107,6 +107,28 @@ def test_malformed_directories_are_refused(tmp_path, pi_dir):
     assert _lib.load().tracer_load_mesh_from_files(str(tmp_path / "missing").encode()) == -1
 
 
+def test_list_directed_input_forms(tmp_path, pi_dir):
+    """The reader takes what Fortran list-directed input takes: CRLF line
+    ends, blank lines before a record, commas and tabs as separators, D
+    exponents, and extra items after a record's last value (skipped)."""
+    import shutil
+
+    d = load_pi()
+    p = str(tmp_path / "forms")
+    shutil.copytree(pi_dir, p)
+    with open(os.path.join(p, "nod2d.out"), "w", newline="") as f:
+        f.write(f"\r\n  {len(d['lonlat'])}\r\n")
+        for i, (x, y) in enumerate(d["lonlat"]):
+            f.write(f"{i + 1},\t{float(x)!r}, {float(y)!r}  0   trailing items\r\n")
+    with open(os.path.join(p, "aux3d.out"), "w") as f:
+        f.write(f"{len(d['zbar'])}\n\n")
+        zs = [f"{z:.17e}".replace("e", "D") for z in d["zbar"]]
+        f.write(" ".join(zs[:10]) + "\n" + "\n".join(zs[10:]) + "\n")
+    a, b = _mesh(p), _mesh(pi_dir)
+    for name in REAL:
+        assert np.array_equal(a.get(name), b.get(name)), name
+
+
 def test_refined_mesh(oracle_mod, pi_refined_dir):
     """meshfiles.refine: four children per triangle, the topology kept
     (N - E + M of the pi mesh, -7: a sphere with its coasts cut out),
