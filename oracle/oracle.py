@@ -146,7 +146,17 @@ class Mesh:
     @classmethod
     def from_files(cls, path, rotate=True, euler_degrees=False, cyclic_2pi=False):
         """A FESOM mesh directory (read_fesom_dir) through om_mesh_from_arrays."""
-        d = read_fesom_dir(path)
+        return cls.from_arrays(read_fesom_dir(path), rotate, euler_degrees, cyclic_2pi)
+
+    @classmethod
+    def from_arrays(cls, d, rotate=True, euler_degrees=False, cyclic_2pi=False):
+        """om_mesh_from_arrays on a dict laid out as the files are: lonlat,
+        elem, edges, edge_tri, elvls, nlvls, zbar, and edge2D / edge2D_in (or
+        edgenum)."""
+        d = dict(d)
+        if "edgenum" in d:
+            d["edge2D"], d["edge2D_in"] = int(d["edgenum"][0]), int(d["edgenum"][1])
+        d["nl"] = len(d["zbar"])
         flags = (0 if rotate else 1) | (2 if euler_degrees else 0) | (4 if cyclic_2pi else 0)
         arrs = [np.ascontiguousarray(d[k], dtype=np.int32) for k in ("elem", "edges", "edge_tri", "elvls", "nlvls")]
         lonlat = _f64(d["lonlat"])
