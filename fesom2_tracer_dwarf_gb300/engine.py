@@ -266,7 +266,7 @@ class TracerAdvection:
             _lib.check(L.fgb_adv_stages(self.mesh.handle, ctypes.byref(d), stages, stream), "fgb_adv_stages")
             self.launches += L.fgb_last_launch_count()
 
-    def run_host(self, host_in, host_out, dt: float, nsteps: int = 1, copy_streams: int = 4):
+    def run_host(self, host_in, host_out, dt: float, nsteps: int = 1, copy_streams: int = 1):
         """Advance independent batches of tracer fields that live in host
         memory: batch i is copied to the device from ``host_in[i]``, advanced
         ``nsteps`` steps, and copied back into ``host_out[i]`` (tensors of
@@ -276,10 +276,10 @@ class TracerAdvection:
         Three device buffers take turns as the field being stepped, the next
         batch arriving and the previous batch leaving, so the host-to-device
         copy of batch i+1 and the device-to-host copy of batch i-1 run during
-        the steps of batch i on the current stream. Each copy is split into
-        ``copy_streams`` chunks on as many streams per direction (host-device
-        transfers in both directions at once run faster spread over several
-        streams). Needs a copy-AB engine (valuesAB follows the values). Returns
+        the steps of batch i on the current stream. Each copy may be split into
+        ``copy_streams`` chunks on as many streams per direction (which count
+        is fastest depends on the host; one was on the machines measured).
+        Needs a copy-AB engine (valuesAB follows the values). Returns
         on the host when every copy has been issued; synchronise the device
         before reading ``host_out``."""
         if self.TA is not None:
