@@ -333,6 +333,92 @@ def test_cabi_steps_on_pi_match_oracle(oracle_mod, pi_dir, schemes):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("mode", ["w_split", "ab2"])
+def test_wsplit_and_ab2_on_pi(oracle_mod, pi_dir, precision, mode):
+    """w_split (implicit vertical LO step, columns of 4..45 layers) and the AB2
+    time level on the pi mesh, three steps against the oracle."""
+    _gpu()
+    from fesom2_tracer_dwarf_gb300 import engine, synthetic
+
+    kw = FLAGS[1]
+    om, m = oracle_mod.Mesh.from_files(pi_dir, **kw), _mesh(pi_dir, upload=True, **kw)
+    rng = np.random.default_rng(zlib.crc32(f"pi-{mode}".encode()))
+    u, s, w = synthetic.layered_flow(m, rng, 900.0, cfl=0.6)
+    vel = np.ascontiguousarray(u[:, None, :] * s[None, :, None])
+    T = synthetic.random_field(m, rng, 4)
+    vals = np.ascontiguousarray(T.copy())
+    W = oracle_mod.Work(om)
+    if mode == "w_split":
+        c = 0.25 * np.abs(w).max()
+        we = np.clip(w, -c, c)
+        wi = w - we
+        sch = ("MUSCL", "PPM", "FCT")
+        for _ in range(3):
+            oracle_mod.analytic_step(om, W, 900.0, vel, w, vals, vals.copy(), [sch + (1.0, 1.0)] * 4, copy_ab=True,
+                                     wi=wi, we=we)
+        eng = engine.TracerAdvection(m, 4, precision, *sch, copy_ab=True)
+        eng.set_tracers(T)
+        eng.set_velocity(vel, w, we=we, wi=wi)
+    else:
+        sch = ("MFCT", "QR4C", "FCT")
+        vab = vals.copy()
+        for _ in range(3):
+            oracle_mod.analytic_step(om, W, 900.0, vel, w, vals, vab, [sch + (1.0, 1.0)] * 4, ab2_eps=0.1)
+        eng = engine.TracerAdvection(m, 4, precision, *sch, ab2_eps=0.1)
+        eng.set_tracers(T)
+        eng.set_velocity(vel, w)
+    eng.step(900.0, 3)
+    torch.cuda.synchronize()
+    got = eng.values()
+    if precision == "fp64":
+        assert np.array_equal(got, vals), f"max |diff| {np.abs(got - vals).max()}"
+    else:
+        assert np.abs(got - vals).max() <= 1e-5 * max(1.0, np.abs(vals).max())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_union_of_pi_and_grid(precision):
+    """The batching form with a file mesh: the pi mesh and an analytic grid as
+    one union mesh (layers padded to the pi mesh's 47) step as each does alone."""
+    _gpu()
+    from fesom2_tracer_dwarf_gb300 import synthetic
+    from fesom2_tracer_dwarf_gb300.engine import TracerAdvection
+    from fesom2_tracer_dwarf_gb300.mesh import Mesh
+
+    d = load_pi()
+    pi = Mesh.from_arrays(**{k: d[k] for k in ("lonlat", "elem", "edges", "edge_tri", "edgenum", "elvls", "nlvls",
+                                                "zbar")}, euler_degrees=True, cyclic_2pi=True)
+    grid = Mesh(14, 12, 10, periodic=True, orient_left=True)
+    parts = [pi, grid]
+    u = Mesh.union(parts)
+    rng = np.random.default_rng(41)
+    dt, K = 900.0, 4
+    flows = [synthetic.layered_flow(pi, rng, dt, cfl=0.4), synthetic.streamfunction_flow(grid, rng, dt, cfl=0.3)]
+    vel = [np.ascontiguousarray(flows[0][0][:, None, :] * flows[0][1][None, :, None]), flows[1][0]]
+    w = [flows[0][2], flows[1][1]]
+    T = [synthetic.random_field(p, rng, K) for p in parts]
+    sch = ("MUSCL", "PPM", "FCT")
+    eu = TracerAdvection(u, K, precision, *sch, copy_ab=True)
+    eu.set_tracers(u.join_parts(T, axis=1, layer_axis=2))
+    eu.set_velocity(u.join_parts(vel, layer_axis=1), u.join_parts(w, layer_axis=1, layers="nl"))
+    eu.step(dt, 3)
+    got = eu.values()
+    for i, p in enumerate(parts):
+        e = TracerAdvection(p, K, precision, *sch, copy_ab=True)
+        e.set_tracers(T[i])
+        e.set_velocity(vel[i], w[i])
+        e.step(dt, 3)
+        ref = e.values()
+        part = u.part_view(got, i, axis=1)[:, :, : p.nz]
+        if precision == "fp64":
+            assert np.array_equal(part, ref), f"part {i}"
+        else:
+            assert np.abs(part - ref).max() <= 1e-6 * np.abs(ref).max(), f"part {i}"
+
+
+@pytest.mark.gpu
 def test_reference_mesh_from_files_workflow(oracle_mod, pi_dir):
     """python/test_mesh_from_files.py through the C ABI: load the pi mesh,
     allocate T and S, zero velocity, 5 steps of dt = 1e-3, statistics."""
