@@ -713,11 +713,15 @@ def run_reference(args):
     value = sum(r[0] for r in res)
     sample = (f"{cores} concurrent processes of the single-threaded C restatement (the Fortran reference has no "
               f"compiler on this machine), each: {res[0][1]}")
+    # one step of the workload at the sampled rate (flat grids: every column is full)
+    cells = (cfg["nx"] - 1) ** 2 * cfg["nz"] * cfg["K"] if cfg["kind"] == "flat" else None
+    ms_step = cells / value * 1e3 if cells else None
     out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+           "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "config": {"workload": args.workload, "schemes": f"{cfg['hor']}/{cfg['ver']}/{cfg['lim']}",
-                      "layers": nz, "tracers": cfg["K"], "wall_s": el},
+                      "layers": nz, "tracers": cfg["K"], "wall_s": el,
+                      "ms_per_step": "one step of the workload's tracer-cells at the sampled rate"},
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
