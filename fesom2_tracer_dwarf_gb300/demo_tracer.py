@@ -17,6 +17,10 @@ scheme selection and the precision form.
     for _ in range(10):
         tracer.advect_step(1000.0)
         print(tracer.get_statistics())
+
+A FESOM mesh directory (the reference's tests/data/pi, or a refinement of it
+by ``meshfiles``) replaces the analytic mesh with
+``tracer.load_mesh_from_files(path)`` (tracer_load_mesh_from_files).
 """
 from __future__ import annotations
 
