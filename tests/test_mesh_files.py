@@ -161,6 +161,41 @@ def test_refined_mesh(oracle_mod, pi_refined_dir):
         assert np.array_equal(m.get("edge_up_dn_tri"), om.geti("edge_up_dn_tri") - 1)
 
 
+def test_build_edges_on_two_triangles():
+    """meshfiles.build_edges: a quad of two triangles near the equator has one
+    interior edge (listed first) and four coast edges, each with its element
+    on the left of node1 -> node2 (east-north frame seen from outside)."""
+    from fesom2_tracer_dwarf_gb300.meshfiles import _xyz, build_edges, morton_order
+
+    lonlat = np.array([[0.0, 0.0], [1.0, 0.0], [1.0, 1.0], [0.0, 1.0]])
+    elem0 = np.array([[0, 1, 2], [0, 2, 3]])
+    edges, edge_tri, n_in = build_edges(elem0, _xyz(lonlat))
+    assert n_in == 1 and len(edges) == 5
+    assert sorted(edges[0]) == [0, 2] and sorted(edge_tri[0]) == [0, 1]
+    assert np.all(edge_tri[1:, 1] == -1)
+    for (a, b), (t, _) in zip(edges, edge_tri):
+        c = [v for v in elem0[t] if v not in (a, b)][0]
+        (x1, y1), (x2, y2), (x3, y3) = lonlat[a], lonlat[b], lonlat[c]
+        assert (x2 - x1) * (y3 - y1) - (y2 - y1) * (x3 - x1) > 0
+    # Morton order visits the lower-left quadrant before the upper-right one
+    pts = np.array([[0.9, 0.9], [0.1, 0.1], [0.9, 0.1], [0.1, 0.9]])
+    order = morton_order(pts)
+    assert order[0] == 1 and order[-1] == 0
+
+
+def test_refinement_cli_round_trip(tmp_path, pi_dir):
+    """python -m fesom2_tracer_dwarf_gb300.meshfiles SRC DST TIMES writes the
+    directory that refine + write_fesom_dir produce from the same input."""
+    from fesom2_tracer_dwarf_gb300 import meshfiles
+
+    dst = str(tmp_path / "cli")
+    assert meshfiles.main([pi_dir, dst, "1"]) == 0
+    a, b = meshfiles.read_fesom_dir(dst), meshfiles.refine(meshfiles.read_fesom_dir(pi_dir), 1)
+    assert np.array_equal(a["lonlat"], b["lonlat"]) and np.array_equal(a["elem"], b["elem"])
+    assert np.array_equal(a["elvls"], b["elvls"]) and np.array_equal(a["zbar"], b["zbar"])
+    assert _mesh(dst).N == len(b["lonlat"])
+
+
 def test_layered_flow_is_continuity_consistent(pi_refined_dir):
     """synthetic.layered_flow's W equals diagnose_w of its velocity, and its
     Courant numbers are at most the target."""
