@@ -196,6 +196,25 @@ def test_refinement_cli_round_trip(tmp_path, pi_dir):
     assert _mesh(dst).N == len(b["lonlat"])
 
 
+def test_union_with_a_file_mesh_shifts_its_tables(pi_dir):
+    """Mesh.union of the pi mesh and an analytic grid: each part's gather
+    tables and levels reappear shifted by the part offsets, layers padded to
+    the deeper part."""
+    from fesom2_tracer_dwarf_gb300.mesh import Mesh
+
+    parts = [_mesh(pi_dir, euler_degrees=True, cyclic_2pi=True), Mesh(9, 8, 6, periodic=True, upload=False)]
+    u = Mesh.union(parts, upload=False)
+    assert u.N == sum(p.N for p in parts) and u.nl == 48
+    for i, p in enumerate(parts):
+        o = u.parts[i]
+        j0 = u.get("ne_ptr")[o["node"]]
+        pc = p.get("ne_code")
+        assert np.array_equal(u.get("ne_code")[j0: j0 + len(pc)], pc + 2 * o["edge"])
+        assert np.array_equal(u.part_view(u.get("nlevels_nod2D"), i), p.get("nlevels_nod2D"))
+        assert np.array_equal(u.part_view(u.get("area"), i)[:, : p.nl], p.get("area"))
+        assert np.array_equal(u.get("gradient_sca")[o["elem"]: o["elem"] + p.M], p.get("gradient_sca"))
+
+
 def test_layered_flow_is_continuity_consistent(pi_refined_dir):
     """synthetic.layered_flow's W equals diagnose_w of its velocity, and its
     Courant numbers are at most the target."""
