@@ -11,6 +11,11 @@ HBM (they are far larger than the 129 MB L2, so no flush is needed).
   python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME]
   python bench.py --impl reference ...   # the CPU implementation of the path
 
+Other workloads (--workload): the same at 512^2 (precision_512), with w_split
+(wsplit_2048, wsplit_512), the plain FP64 form (fp64_512), a closed ragged
+basin (closed_1024), 16 meshes in one union (batch_16), and the reference's pi
+mesh refined 3 or 5 times (pi_refined3, pi_refined5).
+
 Prints one JSON line (rank 0).
 """
 from __future__ import annotations
