@@ -10,36 +10,36 @@
 // GPU loading this library holds until the process exits.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <string>
 
 #include "fesom_tracer_gb300.h"
 #include "fgb_internal.hpp"
+#include "fgb_static_ws_check.hpp"
 
 namespace {
 
 static __device__ __align__(256) unsigned char g_static_workspace[FGB_STATIC_WORKSPACE_BYTES];
 
 constexpr int kMaxDevices = 64;
-void* g_ws_addr[kMaxDevices] = {nullptr};  // device address of the array, per device
+// Device address of the array, per device. Two threads making their first
+// call on a device at the same time both look it up and store the same
+// value; the atomic slots make that well defined.
+std::atomic<void*> g_ws_addr[kMaxDevices];
 
 // The array's name is a host-side stand-in in host code; its device address
 // comes from cudaGetSymbolAddress, once per device with that device current.
-int static_ws_address(void** out) {
-  int dev = -1;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
-    fgb::set_error("fgb_adv_step_static: no usable current device");
-    return -1;
-  }
-  if (!g_ws_addr[dev]) {
-    void* p = nullptr;
+int static_ws_address(int dev, void** out) {
+  void* p = g_ws_addr[dev].load(std::memory_order_acquire);
+  if (!p) {
     cudaError_t ce = cudaGetSymbolAddress(&p, g_static_workspace);
     if (ce != cudaSuccess || !p) {
       fgb::set_error(std::string("fgb_adv_step_static: cudaGetSymbolAddress failed: ") + cudaGetErrorString(ce));
       return -1;
     }
-    g_ws_addr[dev] = p;
+    g_ws_addr[dev].store(p, std::memory_order_release);
   }
-  *out = g_ws_addr[dev];
+  *out = p;
   return 0;
 }
 
@@ -54,20 +54,22 @@ int fgb_adv_step_static(const fgb_mesh* m, const fgb_step_desc* d, void* stream)
     fgb::set_error("fgb_adv_step_static: null argument");
     return -1;
   }
-  const long long need = fgb_workspace_bytes(m, d->precision, d->ntracers);
-  if (need < 0) {
-    fgb::set_error("fgb_adv_step_static: bad precision or tracer count");
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    fgb::set_error("fgb_adv_step_static: no usable current device");
     return -1;
   }
-  if (need > (long long)FGB_STATIC_WORKSPACE_BYTES) {
-    fgb::set_error("fgb_adv_step_static: this mesh and tracer count need " + std::to_string(need) +
-                   " bytes of scratch, more than the static workspace of " +
-                   std::to_string((long long)FGB_STATIC_WORKSPACE_BYTES) +
-                   " bytes; use fgb_adv_step with a caller-provided workspace");
+  std::string err;
+  const long long need = (d->precision == FGB_FP64 || d->precision == FGB_FP32)
+                             ? fgb_workspace_bytes(m, d->precision, d->ntracers)
+                             : -1;
+  if (fgb::static_ws_precheck(d->precision, d->ntracers, need, (long long)FGB_STATIC_WORKSPACE_BYTES, m->device,
+                              dev, &err)) {
+    fgb::set_error(err);
     return -1;
   }
   void* ws = nullptr;
-  if (static_ws_address(&ws)) return -1;
+  if (static_ws_address(dev, &ws)) return -1;
   fgb_step_desc s = *d;
   s.workspace = ws;
   s.workspace_bytes = (long long)FGB_STATIC_WORKSPACE_BYTES;

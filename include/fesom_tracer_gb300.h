@@ -280,10 +280,17 @@ int fgb_last_launch_count(void);
  * every GPU loading this library holds until the process exits; d->workspace
  * is ignored. The caller still passes T, TA, vel, w and we.
  * - Meshes whose fgb_workspace_bytes(m, precision, ntracers) exceeds
- *   FGB_STATIC_WORKSPACE_BYTES are rejected with -1 and a message.
+ *   FGB_STATIC_WORKSPACE_BYTES are rejected with -1 and a message, and so is
+ *   a call whose current device is not the device the mesh was uploaded on.
  * - The first call on a device looks up the array's device address
  *   (cudaGetSymbolAddress) with that device current; make that first call
  *   before any stream capture.
+ * - Under CUDA's default lazy module loading the array's device memory is
+ *   reserved when this library's module first loads on a device, which is
+ *   that first call at the latest. A host framework whose pool claims the
+ *   free device memory first can make that call fail with out-of-memory:
+ *   make a first (warm-up) call on each device before the pool reserves its
+ *   memory, or load modules eagerly (CUDA_MODULE_LOADING=EAGER).
  * - Every call shares the one array and overwrites it; nothing in it needs to
  *   start at zero (each call writes every scratch value before reading it).
  *   Calls that overlap on the GPU (concurrent streams, or two threads) race on
