@@ -243,6 +243,39 @@ def batch_parts(cfg, seed=20260301):
     return [(int(n), int(z), float(c)) for n, z, c in zip(sizes, layers, cfls)]
 
 
+def workload_config(name, cfg, world=1):
+    """The workload as both arms report it (``config``): the mesh, its sizes
+    and the schemes, from the workload's definition alone (no mesh is built,
+    no library is loaded)."""
+    kind = cfg["kind"]
+    if kind == "flat":
+        n = cfg["nx"] - 1
+        N, E, M = n * n, 3 * n * n, 2 * n * n
+        mesh = f"{n}x{n} doubly periodic analytic grid, dx=1 km, {cfg['nz']} layers 5->250 m"
+    elif kind == "closed":
+        nx = cfg["nx"]
+        N, E, M = nx * nx, 3 * (nx - 1) ** 2 + 2 * (nx - 1), 2 * (nx - 1) ** 2
+        mesh = (f"{nx - 1}x{nx - 1} closed basin ({nx}x{nx} nodes), seeded bathymetry, "
+                f"{cfg['min_layers']}..{cfg['nz']} layers 5->250 m")
+    elif kind == "files":
+        N, E, M = 3140, 8986, 5839  # the reference's pi mesh (tests/data/pi)
+        for _ in range(cfg["refine"]):  # each triangle split into four
+            N, E, M = N + E, 2 * E + 3 * M, 4 * M
+        mesh = (f"the reference's pi mesh (global ocean, coasts, ragged bottom of {cfg['nz']} layers) with each "
+                f"triangle split into four {cfg['refine']} times, Morton-ordered nodes; synthetic layered flow, "
+                f"W from continuity")
+    else:
+        parts = batch_parts(cfg)
+        N = sum(n * n for n, _, _ in parts)
+        E, M = 3 * N, 2 * N
+        mesh = "union of %d periodic meshes (n, layers, CFL): %s" % (
+            cfg["parts"], ", ".join(f"{n}^2/{z}/{c:.2f}" for n, z, c in parts))
+    return {"workload": name, "mesh": mesh, "nodes": N, "edges": E, "elements": M, "tracers": cfg["K"],
+            "schemes": f"{cfg['hor']}/{cfg['ver']}/{cfg['lim']}", "dt_s": cfg["dt"],
+            "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}",
+            "w_split": (f"we = w clipped at {cfg['wsplit']} max|w|, wi = w - we" if cfg.get("wsplit") else None)}
+
+
 def _flat_part(n, nz, precision, device, dt, cfl, K, seed, upload=True):
     import numpy as np
     import torch
@@ -479,36 +512,70 @@ def time_e2e(eng, T0, dt, steps, dist_barrier):
     return start.elapsed_time(end), nbytes, nbytes, nc
 
 
-def cpu_sample(seconds=12.0, nx=129, nz=64, K=4, hor="MUSCL", ver="PPM", lim="FCT", dt=400.0, seed=7):
-    """The oracle (single-threaded C restatement) on a bounded sample of the
-    same workload: same schemes, layers and resolution on a smaller domain."""
-    import numpy as np
+def cpu_sample_case(cfg, n=None, seed=7):
+    """A bounded sample of a workload for the CPU legs, built by the oracle
+    and numpy alone: a doubly periodic n x n grid with the workload's layers,
+    tracers, schemes, dt and CFL (the same dx and flow construction)."""
+    from oracle import workloads as WL
 
-    from fesom2_tracer_dwarf_gb300 import synthetic
-    from fesom2_tracer_dwarf_gb300.mesh import Mesh
+    nz = cfg.get("nz", 48)
+    n = n or min(cfg.get("nx", 513) - 1, 512)
+    m, vel, w, T = WL.flat_case(n, nz, cfg["K"], cfg["dt"], seed=seed)
+    wsp = None
+    if cfg.get("wsplit"):
+        c = float(abs(w).max()) * cfg["wsplit"]
+        we = w.clip(-c, c)
+        wsp = dict(wi=w - we, we=we)
+    desc = f"{n}x{n} periodic, {nz} layers, {cfg['K']} tracers, {cfg['hor']}/{cfg['ver']}/{cfg['lim']}"
+    return m, vel, w, T, wsp, desc
+
+
+def cpu_steps(case, cfg, threads, steps=None, seconds=None, warmup=1):
+    """Whole steps of the oracle on a sample (cpu_sample_case) on `threads`
+    threads: `warmup` untimed steps, then `steps` timed steps (or as many as
+    fit in `seconds`, at least two). Returns (tracer-cell updates/s, timed
+    steps, seconds)."""
+    from oracle import oracle as O
+
+    m, vel, w, T, wsp, _ = case
+    O.set_threads(threads)
+    vals = T.copy()
+    vab = vals.copy()
+    W = O.Work(m)
+    sch = [(cfg["hor"], cfg["ver"], cfg["lim"])] * cfg["K"]
+    kw = wsp or {}
+
+    def one():
+        O.analytic_step(m, W, cfg["dt"], vel, w, vals, vab, sch, copy_ab=True, **kw)
+
+    for _ in range(warmup):
+        one()
+    n, el = 0, 0.0
+    while True:
+        t0 = time.perf_counter()
+        one()
+        el += time.perf_counter() - t0
+        n += 1
+        if (steps is not None and n >= steps) or (steps is None and n >= 2 and el >= seconds):
+            break
+    cells = m.nod2D * (m.nl - 1) * cfg["K"]
+    return cells * n / el, n, el
+
+
+def cpu_baseline(cfg, seconds=12.0):
+    """The oracle on the host cores (all of them, and one) on a 256 x 256
+    sample of the workload, about `seconds` of timed steps each."""
     from oracle import oracle as O
 
     O.build()
-    zb = synthetic.stretched_zbar(nz, 5.0, 250.0)
-    L = (nx - 1) * 1000.0
-    om = O.Mesh(nx, nx, nz + 1, Lx=L, Ly=L, depth=-zb[-1], periodic=True, orient_left=True, zbar=zb)
-    hm = Mesh(nx, nx, nz + 1, Lx=L, Ly=L, depth=-zb[-1], periodic=True, orient_left=True, zbar=zb, upload=False)
-    rng = np.random.default_rng(seed)
-    vel, w = synthetic.streamfunction_flow(hm, rng, dt, cfl=0.4)
-    T = np.ascontiguousarray(np.stack([synthetic.gaussian_T(hm, rng), synthetic.salinity(hm, rng)] +
-                                      [synthetic.passive_blob(hm, rng) for _ in range(K - 2)]))
-    vab = T.copy()
-    W = O.Work(om)
-    cells = om.nod2D * nz * K
-    t0 = time.perf_counter()
-    n = 0
-    while True:
-        O.analytic_step(om, W, dt, vel, w, T, vab, [(hor, ver, lim)] * K, copy_ab=True)
-        n += 1
-        if time.perf_counter() - t0 >= seconds:
-            break
-    el = time.perf_counter() - t0
-    return cells * n / el, f"{nx - 1}x{nx - 1} periodic, {nz} layers, {K} tracers, {hor}/{ver}/{lim}, {n} step(s), {el:.1f} s"
+    case = cpu_sample_case(cfg, n=min(cfg.get("nx", 257) - 1, 256))
+    cores = os.cpu_count() or 1
+    v_all, n_all, el_all = cpu_steps(case, cfg, cores, seconds=seconds)
+    v_one, n_one, el_one = cpu_steps(case, cfg, 1, seconds=seconds)
+    return {"value": v_all, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": (f"{case[5]}: {n_all} whole steps in {el_all:.1f} s on {cores} threads (the C restatement "
+                       f"with OpenMP; the Fortran reference has no compiler here)"),
+            "value_1_thread": v_one, "sample_1_thread": f"{n_one} steps in {el_one:.1f} s on 1 thread"}
 
 
 def time_graph(eng, T0, dt, graph_steps, replays, warmup, dist_barrier):
@@ -588,31 +655,15 @@ def run_gpu(args):
     e2e_steps = max(2, min(nsteps, 20))
     e2e_ms, h2d, d2h, e2e_nc = time_e2e(eng, T0, cfg["dt"], e2e_steps, barrier)
     _, e2e_value = job_rate(e2e_ms / e2e_steps, cells, dist, device)
-    if cfg["kind"] == "flat":
-        mesh_desc = f"{cfg['nx'] - 1}x{cfg['nx'] - 1} doubly periodic analytic grid, dx=1 km, {cfg['nz']} layers 5->250 m"
-    elif cfg["kind"] == "closed":
-        mesh_desc = (f"{cfg['nx'] - 1}x{cfg['nx'] - 1} closed basin, seeded bathymetry, "
-                     f"{cfg['min_layers']}..{cfg['nz']} layers 5->250 m")
-    elif cfg["kind"] == "files":
-        lev = m.get("nlevels_nod2D") - 1
-        mesh_desc = (f"the reference's pi mesh (global ocean, coasts) with each triangle split into four "
-                     f"{cfg['refine']} times, Morton-ordered nodes; {lev.min()}..{lev.max()} layers "
-                     f"(mean {lev.mean():.1f}) of 47; synthetic layered flow, W from continuity")
-    else:
-        mesh_desc = "union of %d periodic meshes (n, layers, CFL): %s" % (
-            cfg["parts"], ", ".join(f"{n}^2/{z}/{c:.2f}" for n, z, c in batch_parts(cfg)))
+    config = workload_config(args.workload, cfg, world)
+    assert (config["nodes"], config["edges"], config["elements"]) == (m.N, m.E, m.M), "workload sizes"
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": nsteps,
         "warmup": args.warmup, "ms_per_step": t_max, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32" if cfg["precision"] == "fp32" else "f64", "data": "synthetic",
-        "config": {"workload": args.workload, "mesh": mesh_desc,
-                   "nodes": m.N, "edges": m.E, "elements": m.M, "tracers": K,
-                   "schemes": f"{cfg['hor']}/{cfg['ver']}/{cfg['lim']}", "form": cfg["precision"], "dt_s": cfg["dt"],
-                   "tracer_cells_per_step": cells, "l2": "inputs larger than L2 (no flush)",
-                   "parallelism": f"replicas x{world}", "cuda_graph_steps": cfg.get("graph_steps"),
-                   "launch_cfg": tuned["cfg"] if tuned else "default",
-                   "w_split": (f"we = w clipped at {cfg['wsplit']} max|w|, wi = w - we" if cfg.get("wsplit")
-                               else None)},
+        "config": config,
+        "form": cfg["precision"], "tracer_cells_per_step": cells, "cuda_graph_steps": cfg.get("graph_steps"),
+        "launch_cfg": tuned["cfg"] if tuned else "default",
         "stage_ms": {k: round(v, 4) for k, v in per.items()},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
@@ -677,11 +728,11 @@ def run_gpu(args):
         result["fp64"] = {"value": job_rate(ms64, cells, dist, device)[1], "ms_per_step": ms64, "steps": n64,
                           "mode": "per-mesh sequential eager launches", "gpu_launches": l64}
         result["fp32_over_fp64"] = value / result["fp64"]["value"]
+    if cfg["kind"] == "files":
+        lev = m.get("nlevels_nod2D") - 1
+        result["mesh_layers"] = {"min": int(lev.min()), "max": int(lev.max()), "mean": float(lev.mean())}
     if rank == 0 and not args.no_cpu:
-        nz = cfg.get("nz", 64)
-        v, sample = cpu_sample(seconds=args.cpu_seconds, K=K, nz=nz, hor=cfg["hor"], ver=cfg["ver"], lim=cfg["lim"],
-                               dt=cfg["dt"])
-        result["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample}
+        result["cpu_baseline"] = cpu_baseline(cfg, seconds=args.cpu_seconds)
     if rank == 0:
         print(json.dumps(result), flush=True)
     if dist is not None:
@@ -691,43 +742,40 @@ def run_gpu(args):
 # ---------------------------------------------------------------------------
 # Reference arm: the CPU implementation of the path on all host cores
 # ---------------------------------------------------------------------------
-def _ref_worker(args):
-    seconds, nx, nz, K, hor, ver, lim, dt, seed = args
-    sys.path.insert(0, ROOT)
-    return cpu_sample(seconds=seconds, nx=nx, nz=nz, K=K, hor=hor, ver=ver, lim=lim, dt=dt, seed=seed)
-
-
 def run_reference(args):
+    """The reference's algorithm on the host CPU: the oracle (the C
+    restatement of the Fortran; no Fortran compiler exists on these machines)
+    with OpenMP on every host core. Each step is one whole step on a bounded
+    sample of the workload (a 512 x 512 periodic grid with the workload's
+    layers, tracers, schemes and dt, built by the oracle and numpy: no product
+    library is loaded); `warmup` untimed steps, then `steps` steps timed one
+    by one. Under torchrun only rank 0 runs."""
     rank, world, _ = _env_rank()
     if rank != 0:
         return
-    import multiprocessing as mp
-
-    cfg = WORKLOADS[args.workload]
-    cores = os.cpu_count() or 1
-    ctx = mp.get_context("spawn")
     from oracle import oracle as O
 
     O.build()
-    with ctx.Pool(cores) as pool:
-        t0 = time.perf_counter()
-        nz = cfg.get("nz", 48)  # the batching form's parts have 16..64 layers
-        res = pool.map(_ref_worker, [(args.cpu_seconds, 65, nz, cfg["K"], cfg["hor"], cfg["ver"],
-                                      cfg["lim"], cfg["dt"], 100 + i) for i in range(cores)])
-        el = time.perf_counter() - t0
-    value = sum(r[0] for r in res)
-    sample = (f"{cores} concurrent processes of the single-threaded C restatement (the Fortran reference has no "
-              f"compiler on this machine), each: {res[0][1]}")
-    # one step of the workload at the sampled rate (flat grids: every column is full)
-    cells = (cfg["nx"] - 1) ** 2 * cfg["nz"] * cfg["K"] if cfg["kind"] == "flat" else None
-    ms_step = cells / value * 1e3 if cells else None
-    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+    cfg = WORKLOADS[args.workload]
+    cores = os.cpu_count() or 1
+    case = cpu_sample_case(cfg)
+    O.set_threads(cores)
+    # keep the whole run within a few minutes: a smaller sample if one step is slow
+    _, _, el = cpu_steps(case, cfg, cores, steps=1, warmup=0)
+    if el * (args.steps + args.warmup) > 240.0:
+        case = cpu_sample_case(cfg, n=256)
+    t0 = time.perf_counter()
+    value, n, el = cpu_steps(case, cfg, cores, steps=args.steps, warmup=args.warmup)
+    wall = time.perf_counter() - t0
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": n,
+           "warmup": args.warmup, "ms_per_step": el / n * 1e3, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": args.workload, "schemes": f"{cfg['hor']}/{cfg['ver']}/{cfg['lim']}",
-                      "layers": nz, "tracers": cfg["K"], "wall_s": el,
-                      "ms_per_step": "one step of the workload's tracer-cells at the sampled rate"},
-           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+           "config": workload_config(args.workload, cfg, world),
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                            "sample": (f"each step one whole step of a {case[5]} sample of the workload; "
+                                       f"the C restatement of the Fortran with OpenMP on {cores} threads "
+                                       f"(no Fortran compiler on this machine); {n} timed steps, {wall:.1f} s "
+                                       f"with the warm-up")},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 

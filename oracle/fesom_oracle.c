@@ -7,12 +7,53 @@
  * its floating-point evaluation order (the file is compiled with
  * -ffp-contract=off so that no multiply-add is fused). Citations are
  * path:line inside the reference project.
+ *
+ * Threads (OpenMP, om_set_threads) change no result: loops whose iterations
+ * write disjoint data (per node column, per edge, per element) are split
+ * across threads, and every edge scatter keeps the reference's order per
+ * node -- each thread owns a contiguous range of nodes and walks all edges in
+ * ascending index, applying only the updates of its own nodes.
  */
 #include "fesom_oracle.h"
 
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+void om_set_threads(int n) {
+#ifdef _OPENMP
+  omp_set_num_threads(n > 0 ? n : 1);
+#else
+  (void)n;
+#endif
+}
+
+int om_get_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+#define OMP_FOR _Pragma("omp parallel for schedule(static)")
+/* inside a scatter region: does this thread apply the updates of node n? */
+#define OWNS(n) ((n) >= own_lo && (n) < own_hi)
+
+/* Node range [*lo, *hi) (1-based) whose scatter updates the calling thread
+ * applies: the whole mesh outside a parallel region. */
+static void owner_range(int N, int* lo, int* hi) {
+#ifdef _OPENMP
+  const long t = omp_get_thread_num(), nt = omp_get_num_threads();
+#else
+  const long t = 0, nt = 1;
+#endif
+  *lo = 1 + (int)(N * t / nt);
+  *hi = 1 + (int)(N * (t + 1) / nt);
+}
 
 #define R_EARTH 6367500.0              /* lib/oce_modules.F90:24 */
 #define PI_F 3.14159265358979          /* lib/oce_modules.F90:19 (truncated literal) */
@@ -943,6 +984,7 @@ static void edge_info(const omesh* m, int edge, edgeinfo* s) {
 static void hor_upw1(const omesh* m, const double* vel, const double* ttf, double* flux, int init_zero) {
   const int nzl = m->nl - 1;
   if (init_zero) memset(flux, 0, sizeof(double) * (size_t)nzl * m->edge2D);
+  OMP_FOR
   for (int edge = 1; edge <= m->edge2D; ++edge) {
     edgeinfo s;
     edge_info(m, edge, &s);
@@ -970,6 +1012,7 @@ static void hor_muscl(const omesh* m, const double* vel, const double* ttf, doub
                       const double* grad, int use_clo, int init_zero) {
   const int nzl = m->nl - 1;
   if (init_zero) memset(flux, 0, sizeof(double) * (size_t)nzl * m->edge2D);
+  OMP_FOR
   for (int edge = 1; edge <= m->edge2D; ++edge) {
     edgeinfo s;
     edge_info(m, edge, &s);
@@ -1008,6 +1051,7 @@ static void hor_muscl(const omesh* m, const double* vel, const double* ttf, doub
  * ulevels..nlevels-1 (coefficients lib/oce_mesh.F90:2512-2534). */
 static void tracer_gradient_elements(const omesh* m, const double* ttf, double* tr_xy) {
   const int nzl = m->nl - 1;
+  OMP_FOR
   for (int elem = 1; elem <= m->elem2D; ++elem) {
     const int* en = &A2(m->elem2D_nodes, 3, 1, elem);
     const double* g = &A2(m->gradient_sca, 6, 1, elem);
@@ -1038,6 +1082,7 @@ static void node_mean_grad(const omesh* m, const double* tr_xy, int node, int nz
 /* fill_up_dn_grad, lib/oce_muscl_adv.F90:361-530 */
 static void fill_up_dn_grad(const omesh* m, const double* tr_xy, double* grad) {
   const int nzl = m->nl - 1;
+  OMP_FOR
   for (int edge = 1; edge <= m->edge2D; ++edge) {
     int n1 = A2(m->edges, 2, 1, edge), n2 = A2(m->edges, 2, 2, edge);
     int up = A2(m->edge_up_dn_tri, 2, 1, edge), dn = A2(m->edge_up_dn_tri, 2, 2, edge);
@@ -1099,6 +1144,7 @@ static void fill_up_dn_grad(const omesh* m, const double* tr_xy, double* grad) {
 static void ver_upw1(const omesh* m, const double* W, const double* ttf, double* flux, int init_zero) {
   const int nl = m->nl, nzl = nl - 1;
   if (init_zero) memset(flux, 0, sizeof(double) * (size_t)nl * m->nod2D);
+  OMP_FOR
   for (int n = 1; n <= m->nod2D; ++n) {
     int nzmax = m->nlevels_nod2D[n - 1], nzmin = m->ulevels_nod2D[n - 1];
     int nz = nzmin;
@@ -1116,6 +1162,7 @@ static void ver_qr4c(const omesh* m, const double* W, const double* ttf, double 
                      int init_zero) {
   const int nl = m->nl, nzl = nl - 1;
   if (init_zero) memset(flux, 0, sizeof(double) * (size_t)nl * m->nod2D);
+  OMP_FOR
   for (int n = 1; n <= m->nod2D; ++n) {
     int nzmax = m->nlevels_nod2D[n - 1], nzmin = m->ulevels_nod2D[n - 1];
     int nz = nzmin;
@@ -1145,8 +1192,11 @@ static void ver_qr4c(const omesh* m, const double* W, const double* ttf, double 
 static void ver_ppm(const omesh* m, double dt, const double* W, const double* ttf, double* flux, int init_zero) {
   const int nl = m->nl, nzl = nl - 1;
   if (init_zero) memset(flux, 0, sizeof(double) * (size_t)nl * m->nod2D);
+#pragma omp parallel
+  {
   double* tv = (double*)xcalloc((size_t)nl + 1, sizeof(double)) - 1;
   double* tvert = (double*)xcalloc((size_t)nl + 1, sizeof(double)) - 1;
+#pragma omp for schedule(static)
   for (int n = 1; n <= m->nod2D; ++n) {
     int nzmax = m->nlevels_nod2D[n - 1], nzmin = m->ulevels_nod2D[n - 1];
 #define HN(nz) A2(m->hnode_new, nzl, nz, n)
@@ -1213,13 +1263,17 @@ static void ver_ppm(const omesh* m, double dt, const double* W, const double* tt
   }
   free(tv + 1);
   free(tvert + 1);
+  }
 }
 
 /* adv_tra_ver_cdiff, :648-712 */
 static void ver_cdiff(const omesh* m, const double* W, const double* ttf, double* flux, int init_zero) {
   const int nl = m->nl, nzl = nl - 1;
   if (init_zero) memset(flux, 0, sizeof(double) * (size_t)nl * m->nod2D);
+#pragma omp parallel
+  {
   double* tvert = (double*)xcalloc((size_t)nl + 1, sizeof(double)) - 1;
+#pragma omp for schedule(static)
   for (int n = 1; n <= m->nod2D; ++n) {
     int nzmax = m->nlevels_nod2D[n - 1] - 1, nzmin = m->ulevels_nod2D[n - 1];
     tvert[nzmin] = -((WW(nzmin) * TT(nzmin)) * AREA(nzmin));
@@ -1231,6 +1285,7 @@ static void ver_cdiff(const omesh* m, const double* W, const double* ttf, double
     for (int nz = nzmin; nz <= nzmax; ++nz) FV(nz) = tvert[nz] - FV(nz);
   }
   free(tvert + 1);
+  }
 }
 
 #undef TT
@@ -1263,12 +1318,14 @@ static void oce_tra_adv_fct(const omesh* m, omwork* wk, double dt, const double*
   double *fmax = wk->fct_ttf_max, *fmin = wk->fct_ttf_min, *fplus = wk->fct_plus, *fminus = wk->fct_minus;
   double *tmax = wk->tvert_max, *tmin = wk->tvert_min, *AUX = wk->aux;
   /* a1 */
+  OMP_FOR
   for (int n = 1; n <= m->nod2D; ++n)
     for (int nz = m->ulevels_nod2D[n - 1]; nz <= m->nlevels_nod2D[n - 1] - 1; ++nz) {
       A2(fmax, nzl, nz, n) = dmax(A2(LO, nzl, nz, n), A2(ttf, nzl, nz, n));
       A2(fmin, nzl, nz, n) = dmin(A2(LO, nzl, nz, n), A2(ttf, nzl, nz, n));
     }
   /* a2 */
+  OMP_FOR
   for (int elem = 1; elem <= m->elem2D; ++elem) {
     const int* en = &A2(m->elem2D_nodes, 3, 1, elem);
     int nu1 = m->ulevels[elem - 1], nl1 = m->nlevels[elem - 1];
@@ -1285,6 +1342,7 @@ static void oce_tra_adv_fct(const omesh* m, omwork* wk, double dt, const double*
       }
   }
   /* a3 */
+  OMP_FOR
   for (int n = 1; n <= m->nod2D; ++n) {
     int nu1 = m->ulevels_nod2D[n - 1], nl1 = m->nlevels_nod2D[n - 1];
     for (int nz = nu1; nz <= nl1 - 1; ++nz) {
@@ -1298,6 +1356,7 @@ static void oce_tra_adv_fct(const omesh* m, omwork* wk, double dt, const double*
       }
     }
   }
+  OMP_FOR
   for (int n = 1; n <= m->nod2D; ++n) {
     int nu1 = m->ulevels_nod2D[n - 1], nl1 = m->nlevels_nod2D[n - 1];
     A2(fmax, nzl, nu1, n) = A2(tmax, nzl, nu1, n) - A2(LO, nzl, nu1, n);
@@ -1313,29 +1372,43 @@ static void oce_tra_adv_fct(const omesh* m, omwork* wk, double dt, const double*
     A2(fmin, nzl, nz, n) = A2(tmin, nzl, nz, n) - A2(LO, nzl, nz, n);
   }
   /* b1 */
+  OMP_FOR
   for (int n = 1; n <= m->nod2D; ++n)
     for (int nz = m->ulevels_nod2D[n - 1]; nz <= m->nlevels_nod2D[n - 1] - 1; ++nz) {
       A2(fplus, nzl, nz, n) = 0.0;
       A2(fminus, nzl, nz, n) = 0.0;
     }
+  OMP_FOR
   for (int n = 1; n <= m->nod2D; ++n)
     for (int nz = m->ulevels_nod2D[n - 1]; nz <= m->nlevels_nod2D[n - 1] - 1; ++nz) {
       double a = A2(adf_v, nl, nz, n), b = A2(adf_v, nl, nz + 1, n);
       A2(fplus, nzl, nz, n) = A2(fplus, nzl, nz, n) + (dmax(0.0, a) + dmax(0.0, -b));
       A2(fminus, nzl, nz, n) = A2(fminus, nzl, nz, n) + (dmin(0.0, a) + dmin(0.0, -b));
     }
+#pragma omp parallel
+  {
+  int own_lo, own_hi;
+  owner_range(m->nod2D, &own_lo, &own_hi);
   for (int edge = 1; edge <= m->edge2D; ++edge) {
+    const int o1 = OWNS(A2(m->edges, 2, 1, edge)), o2 = OWNS(A2(m->edges, 2, 2, edge));
+    if (!o1 && !o2) continue;
     int n1, n2, nu12, nl12;
     edge_scatter_range(m, edge, &n1, &n2, &nu12, &nl12);
     for (int nz = nu12; nz <= nl12; ++nz) {
       double f = A2(adf_h, nzl, nz, edge);
-      A2(fplus, nzl, nz, n1) = A2(fplus, nzl, nz, n1) + dmax(0.0, f);
-      A2(fminus, nzl, nz, n1) = A2(fminus, nzl, nz, n1) + dmin(0.0, f);
-      A2(fplus, nzl, nz, n2) = A2(fplus, nzl, nz, n2) + dmax(0.0, -f);
-      A2(fminus, nzl, nz, n2) = A2(fminus, nzl, nz, n2) + dmin(0.0, -f);
+      if (o1) {
+        A2(fplus, nzl, nz, n1) = A2(fplus, nzl, nz, n1) + dmax(0.0, f);
+        A2(fminus, nzl, nz, n1) = A2(fminus, nzl, nz, n1) + dmin(0.0, f);
+      }
+      if (o2) {
+        A2(fplus, nzl, nz, n2) = A2(fplus, nzl, nz, n2) + dmax(0.0, -f);
+        A2(fminus, nzl, nz, n2) = A2(fminus, nzl, nz, n2) + dmin(0.0, -f);
+      }
     }
   }
+  }
   /* b2 */
+  OMP_FOR
   for (int n = 1; n <= m->nod2D; ++n)
     for (int nz = m->ulevels_nod2D[n - 1]; nz <= m->nlevels_nod2D[n - 1] - 1; ++nz) {
       double av = A2(m->areasvol, nl, nz, n);
@@ -1345,6 +1418,7 @@ static void oce_tra_adv_fct(const omesh* m, omwork* wk, double dt, const double*
       A2(fminus, nzl, nz, n) = dmin(1.0, A2(fmin, nzl, nz, n) / flux);
     }
   /* b3 vertical */
+  OMP_FOR
   for (int n = 1; n <= m->nod2D; ++n) {
     int nu1 = m->ulevels_nod2D[n - 1], nl1 = m->nlevels_nod2D[n - 1];
     int nz = nu1;
@@ -1366,6 +1440,7 @@ static void oce_tra_adv_fct(const omesh* m, omwork* wk, double dt, const double*
     }
   }
   /* b3 horizontal */
+  OMP_FOR
   for (int edge = 1; edge <= m->edge2D; ++edge) {
     int n1, n2, nu12, nl12;
     edge_scatter_range(m, edge, &n1, &n2, &nu12, &nl12);
@@ -1387,24 +1462,36 @@ static void oce_tra_adv_fct(const omesh* m, omwork* wk, double dt, const double*
 static void flux2dtracer(const omesh* m, double dt, double* dttf_h, double* dttf_v, const double* flux_h,
                          const double* flux_v, int use_lo, const double* ttf, const double* lo) {
   const int nl = m->nl, nzl = nl - 1;
-  if (use_lo)
+  if (use_lo) {
+    OMP_FOR
     for (int n = 1; n <= m->nod2D; ++n)
       for (int nz = m->ulevels_nod2D[n - 1]; nz <= m->nlevels_nod2D[n - 1] - 1; ++nz)
         A2(dttf_v, nzl, nz, n) = A2(dttf_v, nzl, nz, n) - A2(ttf, nzl, nz, n) * A2(m->hnode, nzl, nz, n) +
                                  A2(lo, nzl, nz, n) * A2(m->hnode_new, nzl, nz, n);
+  }
+  OMP_FOR
   for (int n = 1; n <= m->nod2D; ++n)
     for (int nz = m->ulevels_nod2D[n - 1]; nz <= m->nlevels_nod2D[n - 1] - 1; ++nz)
       A2(dttf_v, nzl, nz, n) = A2(dttf_v, nzl, nz, n) +
                                ((A2(flux_v, nl, nz, n) - A2(flux_v, nl, nz + 1, n)) * dt) / A2(m->areasvol, nl, nz, n);
+#pragma omp parallel
+  {
+  int own_lo, own_hi;
+  owner_range(m->nod2D, &own_lo, &own_hi);
   for (int edge = 1; edge <= m->edge2D; ++edge) {
+    const int o1 = OWNS(A2(m->edges, 2, 1, edge)), o2 = OWNS(A2(m->edges, 2, 2, edge));
+    if (!o1 && !o2) continue;
     int n1, n2, nu12, nl12;
     edge_scatter_range(m, edge, &n1, &n2, &nu12, &nl12);
     for (int nz = nu12; nz <= nl12; ++nz) {
-      A2(dttf_h, nzl, nz, n1) =
-          A2(dttf_h, nzl, nz, n1) + (A2(flux_h, nzl, nz, edge) * dt) / A2(m->areasvol, nl, nz, n1);
-      A2(dttf_h, nzl, nz, n2) =
-          A2(dttf_h, nzl, nz, n2) - (A2(flux_h, nzl, nz, edge) * dt) / A2(m->areasvol, nl, nz, n2);
+      if (o1)
+        A2(dttf_h, nzl, nz, n1) =
+            A2(dttf_h, nzl, nz, n1) + (A2(flux_h, nzl, nz, edge) * dt) / A2(m->areasvol, nl, nz, n1);
+      if (o2)
+        A2(dttf_h, nzl, nz, n2) =
+            A2(dttf_h, nzl, nz, n2) - (A2(flux_h, nzl, nz, edge) * dt) / A2(m->areasvol, nl, nz, n2);
     }
+  }
   }
 }
 
@@ -1415,12 +1502,15 @@ static void flux2dtracer(const omesh* m, double dt, double* dttf_h, double* dttf
  * reference computes first is not used by the coefficients and is omitted. */
 static void vert_impl(const omesh* m, double dt, const double* W, double* ttf) {
   const int nl = m->nl, nzl = nl - 1;
+#pragma omp parallel
+  {
   double* a = (double*)xcalloc(nl + 1, sizeof(double));
   double* b = (double*)xcalloc(nl + 1, sizeof(double));
   double* c = (double*)xcalloc(nl + 1, sizeof(double));
   double* tr = (double*)xcalloc(nl + 1, sizeof(double));
   double* cp = (double*)xcalloc(nl + 1, sizeof(double));
   double* tp = (double*)xcalloc(nl + 1, sizeof(double));
+#pragma omp for schedule(static)
   for (int n = 1; n <= m->nod2D; ++n) {
     for (int k = 0; k <= nl; ++k) a[k] = b[k] = c[k] = tr[k] = tp[k] = cp[k] = 0.0;
     const int nzmax = m->nlevels_nod2D[n - 1], nzmin = m->ulevels_nod2D[n - 1];
@@ -1474,6 +1564,7 @@ static void vert_impl(const omesh* m, double dt, const double* W, double* ttf) {
   free(tr);
   free(cp);
   free(tp);
+  }
 }
 
 /* ------------------------------------------------------------------------- */
@@ -1493,15 +1584,23 @@ int om_do_oce_adv_tra(const omesh* m, omwork* wk, double dt, const double* vel, 
   if (lim == OM_LIM_FCT) {
     hor_upw1(m, vel, ttf, Fh, 1);
     memset(LO, 0, sizeof(double) * (size_t)nzl * m->nod2D);
+#pragma omp parallel
+    {
+    int own_lo, own_hi;
+    owner_range(m->nod2D, &own_lo, &own_hi);
     for (int edge = 1; edge <= m->edge2D; ++edge) {
+      const int o1 = OWNS(A2(m->edges, 2, 1, edge)), o2 = OWNS(A2(m->edges, 2, 2, edge));
+      if (!o1 && !o2) continue;
       int n1, n2, nu12, nl12;
       edge_scatter_range(m, edge, &n1, &n2, &nu12, &nl12);
       for (int nz = nu12; nz <= nl12; ++nz) {
-        A2(LO, nzl, nz, n1) = A2(LO, nzl, nz, n1) + A2(Fh, nzl, nz, edge);
-        A2(LO, nzl, nz, n2) = A2(LO, nzl, nz, n2) - A2(Fh, nzl, nz, edge);
+        if (o1) A2(LO, nzl, nz, n1) = A2(LO, nzl, nz, n1) + A2(Fh, nzl, nz, edge);
+        if (o2) A2(LO, nzl, nz, n2) = A2(LO, nzl, nz, n2) - A2(Fh, nzl, nz, edge);
       }
     }
+    }
     ver_upw1(m, we, ttf, Fv, 1);
+    OMP_FOR
     for (int n = 1; n <= m->nod2D; ++n)
       for (int nz = m->ulevels_nod2D[n - 1]; nz <= m->nlevels_nod2D[n - 1] - 1; ++nz)
         A2(LO, nzl, nz, n) =
@@ -1571,9 +1670,11 @@ int om_analytic_step_split(const omesh* m, omwork* wk, int ntr, double dt, const
     rc = om_do_oce_adv_tra(m, wk, dt, vel, w, wi, we, val, vab, hor[t], ver[t], lim[t], ph[t], pv[t], use_wsplit, dh,
                            dv);
     if (old) memcpy(old, val, blk * sizeof(double));
+    OMP_FOR
     for (int k = 1; k <= N; ++k)
       for (int kz = m->ulevels_nod2D[k - 1]; kz <= m->nlevels_nod2D[k - 1] - 1; ++kz)
         A2(del_ttf, nzl, kz, k) = A2(del_ttf, nzl, kz, k) + A2(dh, nzl, kz, k) + A2(dv, nzl, kz, k);
+    OMP_FOR
     for (int k = 1; k <= N; ++k)
       for (int kz = m->ulevels_nod2D[k - 1]; kz <= m->nlevels_nod2D[k - 1] - 1; ++kz)
         A2(val, nzl, kz, k) = A2(val, nzl, kz, k) + A2(del_ttf, nzl, kz, k) / A2(m->hnode_new, nzl, kz, k);

@@ -111,6 +111,11 @@ void om_init_dwarf_fields(const omesh* m, double Lx, double Ly, double* T, doubl
  * over values(:, 1:myDim_nod2D). */
 void om_stats(const omesh* m, const double* values, double* out4);
 
+/* Threads of the parallel loops (OpenMP; 1 when built without it). Results
+ * do not depend on the thread count. */
+void om_set_threads(int n);
+int om_get_threads(void);
+
 #ifdef __cplusplus
 }
 #endif

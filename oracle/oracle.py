@@ -79,8 +79,19 @@ def lib():
                                    ctypes.c_double, _dp]
         L.om_init_dwarf_fields.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, _dp, _dp]
         L.om_stats.argtypes = [ctypes.c_void_p, _dp, _dp]
+        L.om_set_threads.argtypes = [ctypes.c_int]
+        L.om_get_threads.restype = ctypes.c_int
         _lib = L
     return _lib
+
+
+def set_threads(n: int) -> None:
+    """Threads of the oracle's parallel loops; results do not depend on it."""
+    lib().om_set_threads(int(n))
+
+
+def get_threads() -> int:
+    return int(lib().om_get_threads())
 
 
 def _p(a, t=_dp):

@@ -38,7 +38,8 @@ def _rank_main(rank, world, port, out):
 def test_job_rate_two_gloo_ranks():
     import torch.multiprocessing as tmp
 
-    mgr = tmp.Manager()
+    # spawn, not fork: other tests may have started threads (the oracle's OpenMP pool) in this process
+    mgr = tmp.get_context("spawn").Manager()
     out = mgr.dict()
     tmp.spawn(_rank_main, args=(2, _free_port(), out), nprocs=2, join=True)
     for r in range(2):

@@ -78,3 +78,49 @@ def test_dwarf_linear_drift_frozen_ab(oracle_mod):
     assert np.allclose(d, d[0], rtol=1e-9)
     sums = np.array([s[2] for s in stats])
     assert np.all(np.abs(sums - 32490.0) / 32490.0 < 1e-14)
+
+
+SCHEMES = [(h, v, l) for h in ("UPW1", "MUSCL", "MFCT") for v in ("UPW1", "QR4C", "PPM", "CDIFF")
+           for l in ("NONE", "FCT") if not (v == "CDIFF" and l == "NONE")]
+
+
+def _random_case(O, rng, periodic, ragged):
+    nx, ny, nl = 15, 13, 11
+    en = None
+    if ragged:
+        en = rng.integers(4, nl + 1, size=2 * (nx - 1) * (ny - 1)).astype(np.int32)
+    m = O.Mesh(nx, ny, nl, periodic=periodic, elem_nlev=en)
+    nz = m.nl - 1
+    vel = rng.uniform(-0.3, 0.3, size=(m.elem2D, nz, 2))
+    w = rng.uniform(-2e-3, 2e-3, size=(m.nod2D, m.nl))
+    nlev = m.geti("nlevels_nod2D")
+    for n in range(m.nod2D):
+        w[n, nlev[n] - 1:] = 0.0
+    T = 10.0 + rng.normal(0.0, 1.0, size=(2, m.nod2D, nz))
+    return m, vel, w, np.ascontiguousarray(T)
+
+
+@pytest.mark.parametrize("periodic,ragged", [(True, False), (False, True)])
+def test_threads_change_no_result(oracle_mod, periodic, ragged):
+    """The oracle's OpenMP loops keep every result bit for bit: 1 thread
+    against 5 (node ranges that cut the mesh unevenly), every scheme
+    combination, two steps with copy-AB, and w_split under FCT."""
+    O = oracle_mod
+    rng = np.random.default_rng(11)
+    m, vel, w, T = _random_case(O, rng, periodic, ragged)
+    wi = 0.5 * w
+    before = O.get_threads()
+    try:
+        for sch in SCHEMES:
+            outs = []
+            for nt in (1, 5):
+                O.set_threads(nt)
+                vals, vab = T.copy(), T.copy()
+                W = O.Work(m)
+                kw = dict(wi=wi, we=w - wi) if sch[2] == "FCT" and sch[1] != "UPW1" else {}
+                for _ in range(2):
+                    O.analytic_step(m, W, 300.0, vel, w, vals, vab, [sch] * 2, copy_ab=True, **kw)
+                outs.append(vals)
+            assert np.array_equal(outs[0], outs[1]), sch
+    finally:
+        O.set_threads(before)
