@@ -39,7 +39,7 @@ UNIT = "tracer-cell updates/s"
 WORKLOADS = {
     # The precision form at scale: 2048^2 x 64 doubly periodic, 4 tracers (default).
     "precision_2048": dict(kind="flat", nx=2049, L=2048e3, nz=64, K=4, hor="MUSCL", ver="PPM", lim="FCT",
-                           dt=400.0, precision="fp32", compare_fp64=True, report_steps=3),
+                           dt=400.0, precision="fp32", compare_fp64=True, report_steps=100),
     # The default workload with w_split: w = we + wi, we clipped at a quarter of
     # max |w|; the LO stage adds the implicit vertical solve with wi.
     "wsplit_2048": dict(kind="flat", nx=2049, L=2048e3, nz=64, K=4, hor="MUSCL", ver="PPM", lim="FCT",
@@ -391,41 +391,76 @@ def build_case(cfg, precision, device, seed=20260301):
 
 
 def precision_report(m, e32, T32, e64, T64, dt, steps):
-    """FP32 form against plain FP64 from the same initial values after
-    `steps` steps: per tracer the max-norm error relative to max |T|, the
-    relative change of the volume integral sum(T hnode_new areasvol) of each
-    form, and the FCT extremum violations (wet cells outside the initial
-    [min, max], and the largest excursion relative to the initial range)."""
+    """The FP32 form against the plain FP64 form from the same initial values
+    after `steps` steps. Per tracer: the max-norm error relative to max |T|,
+    the relative change of the volume integral sum(T hnode_new areasvol) --
+    with the FP64 geometry, and with the FP32-rounded geometry the FP32 form
+    itself runs on (its discrete invariant) -- and the FCT extremum
+    violations (wet cells outside the initial [min, max], and the largest
+    excursion relative to the initial range). The FP32 form runs three ways,
+    which separates the error sources: "compensated" (the default: compensated
+    flux-divergence and FCT +/- sums), "plain_sums" (plain FP32 sums) and
+    "anomaly" (compensated, each tracer stored as T - c about its initial
+    mean where that shrinks the stored values, offsets="auto")."""
     import torch
 
-    e32.T.copy_(T32)
     e64.T.copy_(T64)
-    e32.step(dt, steps)
     e64.step(dt, steps)
     torch.cuda.synchronize()
     dev = e64.T.device
     nz = m.nz
     nlev = torch.as_tensor(m.get("nlevels_nod2D"), device=dev)
     wet = (torch.arange(nz, device=dev)[None, :] < (nlev - 1)[:, None])
-    vol = torch.as_tensor(m.get("areasvol")[:, :nz] * m.get("hnode_new"), device=dev) * wet
-    init = e64.from_layout(T64)[:, :, :nz]
-    a = e32.from_layout(e32.T)[:, :, :nz].double()
-    if e32.offsets is not None:  # anomaly storage
-        a = a + torch.as_tensor(e32.offsets, device=a.device)[:, None, None]
+    av, hnn = m.get("areasvol")[:, :nz], m.get("hnode_new")
+    vol = torch.as_tensor(av * hnn, device=dev) * wet
+    vol32 = torch.as_tensor(av.astype("float32").astype("float64") * hnn.astype("float32").astype("float64"),
+                            device=dev) * wet
+    init = e64.from_layout(T64)[:, :, :nz].double()
     b = e64.from_layout(e64.T)[:, :, :nz]
-    out = {"steps": steps, "max_rel_err": [], "sum_rel_err_fp32": [], "sum_rel_err_fp64": [],
-           "violations_fp32": [], "violations_fp64": [], "max_excursion_fp32": [], "max_excursion_fp64": []}
-    for t in range(init.shape[0]):
-        s0 = float((init[t] * vol).sum())
-        lo = float(init[t][wet].min())
-        hi = float(init[t][wet].max())
-        rng = max(hi - lo, 1e-300)
-        out["max_rel_err"].append(float((a[t] - b[t])[wet].abs().max()) / float(b[t][wet].abs().max()))
-        for name, x in (("fp32", a[t]), ("fp64", b[t])):
-            out[f"sum_rel_err_{name}"].append(abs(float((x * vol).sum()) - s0) / abs(s0))
-            xv = x[wet]
-            out[f"violations_{name}"].append(int(((xv < lo) | (xv > hi)).sum()))
-            out[f"max_excursion_{name}"].append(max(0.0, lo - float(xv.min()), float(xv.max()) - hi) / rng)
+    K = init.shape[0]
+    s0 = [float((init[t] * vol).sum()) for t in range(K)]
+    s0_32 = [float((init[t] * vol32).sum()) for t in range(K)]
+    bounds = [(float(init[t][wet].min()), float(init[t][wet].max())) for t in range(K)]
+
+    def extrema(x, t):
+        lo, hi = bounds[t]
+        xv = x[wet]
+        return int(((xv < lo) | (xv > hi)).sum()), max(0.0, lo - float(xv.min()), float(xv.max()) - hi) / max(hi - lo,
+                                                                                                             1e-300)
+
+    out = {"steps": steps, "fp64": {"sum_rel_err": [abs(float((b[t] * vol).sum()) - s0[t]) / abs(s0[t])
+                                                    for t in range(K)],
+                                    "violations": [extrema(b[t], t)[0] for t in range(K)],
+                                    "max_excursion": [extrema(b[t], t)[1] for t in range(K)]}}
+    plain0, req0 = e32.plain_sums, e32._offsets_req
+    for name, plain, offs in (("compensated", False, None), ("plain_sums", True, None), ("anomaly", False, "auto")):
+        e32.plain_sums = plain
+        e32._offsets_req = offs
+        e32.load_padded(T=e64.from_layout(T64).clone() if offs else None)
+        if not offs:
+            e32.offsets = None
+            e32.T.copy_(T32)
+        e32.step(dt, steps)
+        torch.cuda.synchronize()
+        a = e32.from_layout(e32.T)[:, :, :nz].double()
+        if e32.offsets is not None:
+            a = a + torch.as_tensor(e32.offsets, device=a.device)[:, None, None]
+        r = {"max_rel_err": [float((a[t] - b[t])[wet].abs().max()) / float(b[t][wet].abs().max()) for t in range(K)],
+             "sum_rel_err": [abs(float((a[t] * vol).sum()) - s0[t]) / abs(s0[t]) for t in range(K)],
+             "sum_rel_err_fp32_geometry": [abs(float((a[t] * vol32).sum()) - s0_32[t]) / abs(s0_32[t])
+                                           for t in range(K)],
+             "violations": [extrema(a[t], t)[0] for t in range(K)],
+             "max_excursion": [extrema(a[t], t)[1] for t in range(K)]}
+        if offs:
+            r["offsets"] = [float(c) for c in e32.offsets]
+        out[name] = r
+    e32.plain_sums, e32._offsets_req = plain0, req0
+    e32.offsets = None
+    e32.T.copy_(T32)
+    # the default form's figures under the keys of earlier reports
+    out["max_rel_err"] = out["compensated"]["max_rel_err"]
+    out["sum_rel_err_fp32"] = out["compensated"]["sum_rel_err"]
+    out["sum_rel_err_fp64"] = out["fp64"]["sum_rel_err"]
     return out
 
 
@@ -692,15 +727,8 @@ def run_gpu(args):
         result["fp64"] = {"value": job_rate(ms64, cells, dist, device)[1], "ms_per_step": ms64, "steps": n64,
                           "stage_ms": {k: round(v, 3) for k, v in per64.items()}, "gpu_launches": l64}
         result["fp32_over_fp64"] = value / result["fp64"]["value"]
-        if cfg.get("report_steps"):
+        if cfg.get("report_steps") and not args.no_report:
             result["precision_report"] = precision_report(m, eng, T0, e64, T64, cfg["dt"], cfg["report_steps"])
-            # the same with the FP32 form storing anomalies about each tracer's initial mean where that
-            # shrinks the stored values (offsets="auto"; the passive blobs touch zero and keep offset 0)
-            eng._offsets_req = "auto"
-            eng.load_padded(T=e64.from_layout(T64).clone())
-            result["precision_report_anomaly"] = precision_report(m, eng, eng.T.clone(), e64, T64, cfg["dt"],
-                                                                  cfg["report_steps"])
-            result["precision_report_anomaly"]["offsets"] = [float(c) for c in eng.offsets]
         del e64
     elif cfg.get("compare_fp64") == "sequential" and not args.no_fp64:
         # per-mesh sequential plain FP64 steps (eager launches, one mesh after another)
@@ -780,6 +808,25 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def run_profile(args):
+    """The kernels of `args.profile` plain steps of a workload, nothing else
+    timed or launched by this library (the command the ncu summaries cite)."""
+    import torch
+
+    from fesom2_tracer_dwarf_gb300 import _lib
+
+    _lib.load()
+    cfg = WORKLOADS[args.workload]
+    m, eng, _ = build_case(cfg, args.precision or cfg["precision"], "cuda:0")
+    if args.launch_cfg:
+        eng.set_launch([int(x) for x in args.launch_cfg.split(",")])
+    torch.cuda.synchronize()
+    eng.step(cfg["dt"], args.profile)
+    torch.cuda.synchronize()
+    print(json.dumps({"workload": args.workload, "form": eng.precision, "steps": args.profile,
+                      "launch_cfg": eng.cfg, "launches": eng.launches}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -791,8 +838,18 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-report", action="store_true", help="skip the FP32-vs-FP64 precision report")
     ap.add_argument("--no-tune", action="store_true", help="use the default launch configuration")
+    ap.add_argument("--profile", type=int, default=0, metavar="N",
+                    help="build the workload, run N plain steps (for a profiler) and exit")
+    ap.add_argument("--precision", choices=["fp32", "fp64"], default=None,
+                    help="with --profile: the form to run (default: the workload's)")
+    ap.add_argument("--launch-cfg", default=None,
+                    help="with --profile: launch configuration, comma-separated (default: the library's)")
     args = ap.parse_args()
+    if args.profile:
+        run_profile(args)
+        return
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
     if args.impl == "reference":

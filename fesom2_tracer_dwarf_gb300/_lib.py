@@ -53,6 +53,7 @@ class StepDesc(ctypes.Structure):
         ("wi", _vp),
         ("ab_order", ctypes.c_int),
         ("ab_eps", ctypes.c_double),
+        ("fp32_plain_sums", ctypes.c_int),
     ]
 
 

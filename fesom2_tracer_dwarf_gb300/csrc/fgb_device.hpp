@@ -122,6 +122,7 @@ struct FastPtrs {
   int ab2;  // TAout = ab_old * T_old + ab_new * T_new (else T_new)
   float ab_old, ab_new;
   int wsplit_fused;  // w_split: the LO kernel also solves the implicit vertical step
+  int comp;          // compensated flux-divergence and FCT +/- sums (fgb_step_desc.fp32_plain_sums == 0)
 };
 
 // Shared-memory shape of the w_split kernel (kf_vert_impl): a warp holds

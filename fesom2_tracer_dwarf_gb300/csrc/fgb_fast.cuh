@@ -138,6 +138,19 @@ __device__ __forceinline__ V<KV> muls(const V<KV>& a, float s) {
 }
 #undef FGB_F2
 
+// Error-free addition (Knuth's TwoSum: six additions, exact for any order of
+// magnitudes): s + x = s' + e exactly; s <- s', c <- c + e. Summing with it
+// keeps each sum's rounding error in c, so a compensated sum (s, c) of FP32
+// terms is exact to the rounding of c.
+template <int KV>
+__device__ __forceinline__ void two_sum(V<KV>& s, V<KV>& c, const V<KV>& x) {
+  const V<KV> t = add(s, x);
+  const V<KV> bp = sub(t, s);
+  const V<KV> e = add(sub(s, sub(t, bp)), sub(x, bp));
+  s = t;
+  c = add(c, e);
+}
+
 // Division by the fast single-precision reciprocal (about 2 ulp); the FP32
 // form's bar is a tolerance against FP64, not bit parity.
 __device__ __forceinline__ float fdv(float a, float b) { return __fdividef(a, b); }
@@ -945,7 +958,7 @@ __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
 // FCT stage 2: bounds a1-a3, antidiffusive sums b1 and limiting factors b2
 // (lib/oce_adv_tra_fct.F90:98-374).
 // ---------------------------------------------------------------------------
-template <int KV, int NS>
+template <int KV, int NS, bool COMP>
 __global__ void __launch_bounds__(128, (NS == 1 ? 10 : 7)) kf_ratio(DMesh m, FastPtrs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
@@ -1017,7 +1030,7 @@ __global__ void __launch_bounds__(128, (NS == 1 ? 10 : 7)) kf_ratio(DMesh m, Fas
     float* __restrict__ Rg = a.rpm + 2 * gi * a.gN;
     for (unsigned base = 0; base < LZ; base += kW * NS) {
       unsigned kk[NS];
-      V<KV> pl[NS], mi[NS];
+      V<KV> pl[NS], mi[NS], plc[NS], mic[NS];
 #pragma unroll
       for (int i = 0; i < NS; ++i) {
         const unsigned k = base + lane + kW * i;
@@ -1028,6 +1041,8 @@ __global__ void __launch_bounds__(128, (NS == 1 ? 10 : 7)) kf_ratio(DMesh m, Fas
           pl[i].v[t] = fmaxf(0.f, ad0.v[t]) + fmaxf(0.f, -ad1.v[t]);
           mi[i].v[t] = fminf(0.f, ad0.v[t]) + fminf(0.f, -ad1.v[t]);
         }
+        plc[i] = splat<KV>(0.f);
+        mic[i] = plc[i];
       }
 #pragma unroll (NS == 1 ? 6 : 3)
       for (int j = 0; j < nb.deg; ++j) {
@@ -1038,13 +1053,33 @@ __global__ void __launch_bounds__(128, (NS == 1 ? 10 : 7)) kf_ratio(DMesh m, Fas
 #pragma unroll
         for (int i = 0; i < NS; ++i) f[i] = ld<KV>(Fg, ed * LZ + kk[i]);
 #pragma unroll
-        for (int i = 0; i < NS; ++i)
+        for (int i = 0; i < NS; ++i) {
+          if (COMP) {
+            V<KV> xp, xm;
 #pragma unroll
-          for (int t = 0; t < KV; ++t) {
-            const float x = sg * f[i].v[t];
-            pl[i].v[t] += fmaxf(0.f, x);
-            mi[i].v[t] += fminf(0.f, x);
+            for (int t = 0; t < KV; ++t) {
+              const float x = sg * f[i].v[t];
+              xp.v[t] = fmaxf(0.f, x);
+              xm.v[t] = fminf(0.f, x);
+            }
+            two_sum(pl[i], plc[i], xp);
+            two_sum(mi[i], mic[i], xm);
+          } else {
+#pragma unroll
+            for (int t = 0; t < KV; ++t) {
+              const float x = sg * f[i].v[t];
+              pl[i].v[t] += fmaxf(0.f, x);
+              mi[i].v[t] += fminf(0.f, x);
+            }
           }
+        }
+      }
+      if (COMP) {
+#pragma unroll
+        for (int i = 0; i < NS; ++i) {
+          pl[i] = add(pl[i], plc[i]);
+          mi[i] = add(mi[i], mic[i]);
+        }
       }
 #pragma unroll
       for (int i = 0; i < NS; ++i) {
@@ -1079,7 +1114,8 @@ __global__ void __launch_bounds__(128, (NS == 1 ? 10 : 7)) kf_ratio(DMesh m, Fas
 // more resident warps.
 
 // LEAN: fewer registers (64, one cluster node in flight) for more resident warps.
-template <int KV, bool LEAN>
+// COMP: the +/- sums of the antidiffusive fluxes are compensated sums.
+template <int KV, bool LEAN, bool COMP>
 __global__ void __launch_bounds__(128, LEAN ? 8 : 7) kf_ratio64(DMesh m, FastPtrs a) {
   const int lane = threadIdx.x & (kW - 1);
   const int n = blockIdx.x * (blockDim.x / kW) + threadIdx.x / kW;
@@ -1157,7 +1193,7 @@ __global__ void __launch_bounds__(128, LEAN ? 8 : 7) kf_ratio64(DMesh m, FastPtr
       }
     }
     // antidiffusive sums b1 (lib/oce_adv_tra_fct.F90:255-346)
-    V<KV> pl[2], mi[2];
+    V<KV> pl[2], mi[2], plc[2], mic[2];
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
       const V<KV> ad0 = ld<KV>(adfv, n * LW + kk[i]), ad1 = ld<KV>(adfv, n * LW + kk[i] + 1);
@@ -1166,6 +1202,8 @@ __global__ void __launch_bounds__(128, LEAN ? 8 : 7) kf_ratio64(DMesh m, FastPtr
         pl[i].v[t] = fmaxf(0.f, ad0.v[t]) + fmaxf(0.f, -ad1.v[t]);
         mi[i].v[t] = fminf(0.f, ad0.v[t]) + fminf(0.f, -ad1.v[t]);
       }
+      plc[i] = splat<KV>(0.f);
+      mic[i] = plc[i];
     }
 #pragma unroll 2
     for (int j = 0; j < deg; ++j) {
@@ -1176,13 +1214,33 @@ __global__ void __launch_bounds__(128, LEAN ? 8 : 7) kf_ratio64(DMesh m, FastPtr
 #pragma unroll
       for (int i = 0; i < 2; ++i) f[i] = ld<KV>(Fg, ed * LZ + kk[i]);
 #pragma unroll
-      for (int i = 0; i < 2; ++i)
+      for (int i = 0; i < 2; ++i) {
+        if (COMP) {
+          V<KV> xp, xm;
 #pragma unroll
-        for (int t = 0; t < KV; ++t) {
-          const float x = sg * f[i].v[t];
-          pl[i].v[t] += fmaxf(0.f, x);
-          mi[i].v[t] += fminf(0.f, x);
+          for (int t = 0; t < KV; ++t) {
+            const float x = sg * f[i].v[t];
+            xp.v[t] = fmaxf(0.f, x);
+            xm.v[t] = fminf(0.f, x);
+          }
+          two_sum(pl[i], plc[i], xp);
+          two_sum(mi[i], mic[i], xm);
+        } else {
+#pragma unroll
+          for (int t = 0; t < KV; ++t) {
+            const float x = sg * f[i].v[t];
+            pl[i].v[t] += fmaxf(0.f, x);
+            mi[i].v[t] += fminf(0.f, x);
+          }
         }
+      }
+    }
+    if (COMP) {
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        pl[i] = add(pl[i], plc[i]);
+        mi[i] = add(mi[i], mic[i]);
+      }
     }
     // factors b2 (lib/oce_adv_tra_fct.F90:363-374)
     float* __restrict__ Rg = a.rpm + 2 * gi * a.gN;
@@ -1261,7 +1319,14 @@ __device__ __forceinline__ void finish_node(const DMesh& m, const FastPtrs& a, i
 // fetched together with the first neighbours, and three incident edges are in
 // flight per round.
 // DEL: a persistent del_ttf is read and written (the reference C interface).
-template <int KV, int NS, bool DEL>
+// COMP: the limited edge fluxes are formed as one rounded product p = ae * f,
+// the same number at both ends of the edge (+p at the first node, -p at the
+// second), and summed with the vertical fluxes of the layer's two interfaces
+// (each interface flux once with each sign) as a compensated sum, so the
+// divergence cancels between neighbours to the last bit of the sum; without
+// DEL the new value is then LO + T (1 - hnode/hnode_new) + S dt / (areasvol
+// hnode_new), the update of the reference in exact arithmetic.
+template <int KV, int NS, bool DEL, bool COMP>
 __global__ void __launch_bounds__(128, (NS == 1 ? 9 : 4)) kf_update(DMesh m, FastPtrs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
@@ -1317,7 +1382,7 @@ __global__ void __launch_bounds__(128, (NS == 1 ? 9 : 4)) kf_update(DMesh m, Fas
     float* del = DEL ? a.del + gi * a.gN : nullptr;
     for (unsigned base = 0; base < LZ; base += kW * NS) {
       unsigned kk[NS];
-      V<KV> dh[NS], rpn[NS], rmn[NS], lo[NS], Tn[NS], d0[NS];
+      V<KV> dh[NS], dc[NS], rpn[NS], rmn[NS], lo[NS], Tn[NS], d0[NS];
       float av[NS], hnn[NS], hn[NS];
 #pragma unroll
       for (int i = 0; i < NS; ++i) {
@@ -1325,6 +1390,7 @@ __global__ void __launch_bounds__(128, (NS == 1 ? 9 : 4)) kf_update(DMesh m, Fas
         kk[i] = k < LZ ? k : LZ - 1;
         const unsigned kr = kk[i] < (unsigned)nz ? kk[i] : (unsigned)nz - 1;
         dh[i] = splat<KV>(0.f);
+        dc[i] = splat<KV>(0.f);
         rpn[i] = sRp[kr];
         rmn[i] = sRm[kr];
         // the final update's inputs travel with the first neighbours
@@ -1349,7 +1415,13 @@ __global__ void __launch_bounds__(128, (NS == 1 ? 9 : 4)) kf_update(DMesh m, Fas
         }
 #pragma unroll
         for (int i = 0; i < NS; ++i) {
-          if (role) {  // this node is the edge's second node
+          if (COMP) {
+            // the same min of the same two factors at both ends: ae and p are equal there
+            const V<KV> ae = role ? vsel_min(f[i], rpo[i], rmn[i], rmo[i], rpn[i])
+                                  : vsel_min(f[i], rpn[i], rmo[i], rmn[i], rpo[i]);
+            const V<KV> p = mul(ae, f[i]);
+            two_sum(dh[i], dc[i], role ? sub(splat<KV>(0.f), p) : p);
+          } else if (role) {  // this node is the edge's second node
             const V<KV> ae = vsel_min(f[i], rpo[i], rmn[i], rmo[i], rpn[i]);
             dh[i] = sub(dh[i], mul(ae, f[i]));
           } else {
@@ -1367,11 +1439,21 @@ __global__ void __launch_bounds__(128, (NS == 1 ? 9 : 4)) kf_update(DMesh m, Fas
         if (z >= nzmin && z <= nzmax - 1) {
           const float r = fdv(dt, av[i]);
           const float ra = hn[i] / hnn[i];  // IEEE: exactly 1 for an unchanged layer
-          // -T hnode + LO hnode_new as hnode_new (LO - T hnode / hnode_new): exactly
-          // zero when LO equals T and the layer keeps its thickness
-          const V<KV> dv = fmas(sub(lo[i], muls(Tn[i], ra)), hnn[i], muls(sub(sLv[k], sLv[k + 1]), r));
-          enew = add(add(d0[i], muls(dh[i], r)), dv);
-          tnew = fmas(enew, fdv(1.f, hnn[i]), Tn[i]);
+          if (COMP && !DEL) {
+            // S = horizontal + vertical antidiffusive divergence, compensated
+            two_sum(dh[i], dc[i], sLv[k]);
+            two_sum(dh[i], dc[i], sub(splat<KV>(0.f), sLv[k + 1]));
+            const float q = fdv(dt, av[i] * hnn[i]);
+            const V<KV> base = fmas(Tn[i], 1.f - ra, lo[i]);  // T (1 - ra) is exactly 0 when ra = 1
+            tnew = fmas(dh[i], q, fmas(dc[i], q, base));
+          } else {
+            if (COMP) dh[i] = add(dh[i], dc[i]);
+            // -T hnode + LO hnode_new as hnode_new (LO - T hnode / hnode_new): exactly
+            // zero when LO equals T and the layer keeps its thickness
+            const V<KV> dv = fmas(sub(lo[i], muls(Tn[i], ra)), hnn[i], muls(sub(sLv[k], sLv[k + 1]), r));
+            enew = add(add(d0[i], muls(dh[i], r)), dv);
+            tnew = fmas(enew, fdv(1.f, hnn[i]), Tn[i]);
+          }
         }
         st<KV>(Tg, n * LZ + k, tnew);
         if (DEL) st<KV>(del, n * LZ + k, enew);

@@ -64,23 +64,40 @@ void launch_nofct_f(const DMesh& m, const FastPtrs& a, int nw, cudaStream_t s) {
   kf_nofct<VER, KV, NS><<<(m.N + nw - 1) / nw, nw * kW, sm, s>>>(m, a);
 }
 
+template <int KV, int NS, bool COMP>
+void launch_ratio_fc(const DMesh& m, const FastPtrs& a, int nw, cudaStream_t s) {
+  const size_t sm = nw * warp_bytes<KV>(0, kRatioVec, m.LW);
+  allow_smem_f(kf_ratio<KV, NS, COMP>, sm);
+  kf_ratio<KV, NS, COMP><<<(m.N + nw - 1) / nw, nw * kW, sm, s>>>(m, a);
+}
 template <int KV, int NS>
 void launch_ratio_f(const DMesh& m, const FastPtrs& a, int nw, cudaStream_t s) {
-  const size_t sm = nw * warp_bytes<KV>(0, kRatioVec, m.LW);
-  allow_smem_f(kf_ratio<KV, NS>, sm);
-  kf_ratio<KV, NS><<<(m.N + nw - 1) / nw, nw * kW, sm, s>>>(m, a);
+  if (a.comp) launch_ratio_fc<KV, NS, true>(m, a, nw, s);
+  else launch_ratio_fc<KV, NS, false>(m, a, nw, s);
 }
 
+template <int KV, int NS, bool DEL, bool COMP>
+void launch_update_fc(const DMesh& m, const FastPtrs& a, int nw, cudaStream_t s) {
+  const size_t sm = nw * warp_bytes<KV>(0, kUpdVec, m.LW);
+  allow_smem_f(kf_update<KV, NS, DEL, COMP>, sm);
+  kf_update<KV, NS, DEL, COMP><<<(m.N + nw - 1) / nw, nw * kW, sm, s>>>(m, a);
+}
 template <int KV, int NS>
 void launch_update_f(const DMesh& m, const FastPtrs& a, int nw, cudaStream_t s) {
-  const size_t sm = nw * warp_bytes<KV>(0, kUpdVec, m.LW);
   if (a.del) {
-    allow_smem_f(kf_update<KV, NS, true>, sm);
-    kf_update<KV, NS, true><<<(m.N + nw - 1) / nw, nw * kW, sm, s>>>(m, a);
+    if (a.comp) launch_update_fc<KV, NS, true, true>(m, a, nw, s);
+    else launch_update_fc<KV, NS, true, false>(m, a, nw, s);
   } else {
-    allow_smem_f(kf_update<KV, NS, false>, sm);
-    kf_update<KV, NS, false><<<(m.N + nw - 1) / nw, nw * kW, sm, s>>>(m, a);
+    if (a.comp) launch_update_fc<KV, NS, false, true>(m, a, nw, s);
+    else launch_update_fc<KV, NS, false, false>(m, a, nw, s);
   }
+}
+
+template <int KV, bool LEAN>
+void launch_ratio64(const DMesh& m, const FastPtrs& a, int nw, cudaStream_t s) {
+  const unsigned grid = (m.N + nw - 1) / nw;
+  if (a.comp) kf_ratio64<KV, LEAN, true><<<grid, nw * kW, 0, s>>>(m, a);
+  else kf_ratio64<KV, LEAN, false><<<grid, nw * kW, 0, s>>>(m, a);
 }
 
 template <int KV, int VER>
@@ -136,9 +153,8 @@ int launch_fast(const DMesh& m, const FastPtrs& a, const LaunchArgs& L, cudaStre
     if (L.mask & FGB_STAGE_RATIO) {
       if (m.LZ <= 2 * kW && (L.ns_ratio == 0 || L.ns_ratio >= 3)) {
         // whole column per warp, no shared memory
-        const unsigned grid = (m.N + L.nw_ratio - 1) / L.nw_ratio;
-        if (L.ns_ratio == 4) kf_ratio64<KV, true><<<grid, L.nw_ratio * kW, 0, s>>>(m, a);
-        else kf_ratio64<KV, false><<<grid, L.nw_ratio * kW, 0, s>>>(m, a);
+        if (L.ns_ratio == 4) launch_ratio64<KV, true>(m, a, L.nw_ratio, s);
+        else launch_ratio64<KV, false>(m, a, L.nw_ratio, s);
       } else if (L.ns_ratio == 1) {
         launch_ratio_f<KV, 1>(m, a, L.nw_ratio, s);
       } else {

@@ -69,7 +69,7 @@ class TracerAdvection:
     def __init__(self, mesh: Mesh, ntracers: int, precision: str = "fp64", hor: str = "UPW1",
                  ver: str = "UPW1", lim: str = "NONE", ph: float = 1.0, pv: float = 1.0,
                  copy_ab: bool = False, device: str = "cuda", tracer_vec: int | None = None,
-                 ab2_eps: float | None = None, offsets=None):
+                 ab2_eps: float | None = None, offsets=None, plain_sums: bool = False):
         _require_cuda()
         if ab2_eps is not None and copy_ab:
             raise ValueError("copy_ab and ab2_eps are two choices of the valuesAB time level; give one")
@@ -87,6 +87,8 @@ class TracerAdvection:
         self.set_schemes(hor, ver, lim, ph, pv)
         self.copy_ab = copy_ab
         self.ab2_eps = None if ab2_eps is None else float(ab2_eps)
+        # FP32 form: plain FP32 sums instead of the compensated flux-divergence and FCT +/- sums
+        self.plain_sums = bool(plain_sums)
         if isinstance(offsets, str):
             if offsets not in ("mean", "auto"):
                 raise ValueError('offsets must be None, "mean", "auto" or one value per tracer')
@@ -254,6 +256,7 @@ class TracerAdvection:
         d.del_ = None
         d.workspace = self.workspace.data_ptr()
         d.workspace_bytes = self.workspace.numel()
+        d.fp32_plain_sums = int(self.plain_sums)
         for i, c in enumerate(self.cfg):
             d.cfg[i] = c
         return d

@@ -250,6 +250,12 @@ typedef struct {
    * runs after every stage that reads TA. */
   int ab_order;
   double ab_eps;
+  /* FP32 form: 0 (default) forms the flux divergence of the update and the
+   * FCT +/- sums of the limiter as compensated sums (FP32 pairs with
+   * error-free additions, the same rounded product at both ends of an edge),
+   * so that the edge fluxes cancel between neighbouring nodes to the last bit
+   * of the sum; 1 plain FP32 sums. The FP64 form ignores it. */
+  int fp32_plain_sums;
 } fgb_step_desc;
 
 /* Full step: vflux, hflux, and the FCT (lo, ratio, update) or plain update. */
