@@ -1107,6 +1107,9 @@ __global__ void __launch_bounds__(128, (NS == 1 ? 10 : 7)) kf_ratio(DMesh m, Fas
   }
 }
 
+// Shared memory of one warp of kf_ratio64: bmax, bmin of the lane's two layers.
+__host__ __device__ constexpr size_t ratio64_warp_bytes(int KV) { return (size_t)4 * kW * KV * 4; }
+
 // Columns of at most 64 layers: one warp holds the whole column (lanes own
 // layers l and l + 32), so the vertical bound window (layers k-1, k, k+1) comes
 // from neighbouring lanes by shuffles and the kernel needs no shared memory;
@@ -1115,11 +1118,14 @@ __global__ void __launch_bounds__(128, (NS == 1 ? 10 : 7)) kf_ratio(DMesh m, Fas
 
 // LEAN: fewer registers (64, one cluster node in flight) for more resident warps.
 // COMP: the +/- sums of the antidiffusive fluxes are compensated sums.
+// Shared memory: ratio64_warp_bytes per warp, where the finished bounds wait.
 template <int KV, bool LEAN, bool COMP>
 __global__ void __launch_bounds__(128, LEAN ? 8 : 7) kf_ratio64(DMesh m, FastPtrs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kW - 1);
   const int n = blockIdx.x * (blockDim.x / kW) + threadIdx.x / kW;
   if (n >= m.N) return;
+  V<KV>* sB = reinterpret_cast<V<KV>*>(smem_raw) + (size_t)(threadIdx.x / kW) * 4 * kW;
   const GeoPtrs<float>& g = m.g32;
   const unsigned LZ = m.LZ, LW = m.LW;
   const int j0 = m.ne_ptr[n], deg = m.ne_ptr[n + 1] - j0;
@@ -1192,6 +1198,13 @@ __global__ void __launch_bounds__(128, LEAN ? 8 : 7) kf_ratio64(DMesh m, FastPtr
         }
       }
     }
+    // the finished bounds wait in this lane's shared-memory slots while the
+    // sums are formed (fewer live registers)
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      sB[i * kW + lane] = bmax[i];
+      sB[(2 + i) * kW + lane] = bmin[i];
+    }
     // antidiffusive sums b1 (lib/oce_adv_tra_fct.F90:255-346)
     V<KV> pl[2], mi[2], plc[2], mic[2];
 #pragma unroll
@@ -1241,6 +1254,11 @@ __global__ void __launch_bounds__(128, LEAN ? 8 : 7) kf_ratio64(DMesh m, FastPtr
         pl[i] = add(pl[i], plc[i]);
         mi[i] = add(mi[i], mic[i]);
       }
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      bmax[i] = sB[i * kW + lane];
+      bmin[i] = sB[(2 + i) * kW + lane];
     }
     // factors b2 (lib/oce_adv_tra_fct.F90:363-374)
     float* __restrict__ Rg = a.rpm + 2 * gi * a.gN;
@@ -1327,7 +1345,7 @@ __device__ __forceinline__ void finish_node(const DMesh& m, const FastPtrs& a, i
 // DEL the new value is then LO + T (1 - hnode/hnode_new) + S dt / (areasvol
 // hnode_new), the update of the reference in exact arithmetic.
 template <int KV, int NS, bool DEL, bool COMP>
-__global__ void __launch_bounds__(128, (NS == 1 ? 9 : 4)) kf_update(DMesh m, FastPtrs a) {
+__global__ void __launch_bounds__(128, (NS == 1 ? (COMP ? 8 : 9) : 4)) kf_update(DMesh m, FastPtrs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
   const int n = blockIdx.x * (blockDim.x / kW) + wib;

@@ -5,6 +5,7 @@
 
 #include "fesom_tracer_gb300.h"
 #include "fgb_fast.cuh"
+#include "fgb_fast_lo64.cuh"
 #include "fgb_fast_tile.cuh"
 
 namespace fgb {
@@ -96,14 +97,34 @@ void launch_update_f(const DMesh& m, const FastPtrs& a, int nw, cudaStream_t s) 
 template <int KV, bool LEAN>
 void launch_ratio64(const DMesh& m, const FastPtrs& a, int nw, cudaStream_t s) {
   const unsigned grid = (m.N + nw - 1) / nw;
-  if (a.comp) kf_ratio64<KV, LEAN, true><<<grid, nw * kW, 0, s>>>(m, a);
-  else kf_ratio64<KV, LEAN, false><<<grid, nw * kW, 0, s>>>(m, a);
+  const size_t sm = nw * ratio64_warp_bytes(KV);
+  if (a.comp) kf_ratio64<KV, LEAN, true><<<grid, nw * kW, sm, s>>>(m, a);
+  else kf_ratio64<KV, LEAN, false><<<grid, nw * kW, sm, s>>>(m, a);
+}
+
+template <int KV, int VER, bool TASEP, bool WESEP>
+void launch_lo64(const DMesh& m, const FastPtrs& a, cudaStream_t s) {
+  const size_t sm = kLo64Warps * lo64_warp_bytes(KV, VER, TASEP);
+  allow_smem_f(kf_lo64<VER, KV, TASEP, WESEP>, sm);
+  kf_lo64<VER, KV, TASEP, WESEP><<<(m.N + kLo64Warps - 1) / kLo64Warps, kLo64Warps * kW, sm, s>>>(m, a);
 }
 
 template <int KV, int VER>
 void launch_lo_ns(const DMesh& m, const FastPtrs& a, const LaunchArgs& L, cudaStream_t s) {
-  if (L.ns_lo == 1) launch_lo_f<KV, VER, 1>(m, a, L.nw_lo, s);
-  else launch_lo_f<KV, VER, 2>(m, a, L.nw_lo, s);
+  if (L.ns_lo == 3) {  // whole column per warp (at most 64 layers, no w_split)
+    const bool tasep = a.TA != a.T, wesep = a.we != a.w;
+    if (tasep) {
+      if (wesep) launch_lo64<KV, VER, true, true>(m, a, s);
+      else launch_lo64<KV, VER, true, false>(m, a, s);
+    } else {
+      if (wesep) launch_lo64<KV, VER, false, true>(m, a, s);
+      else launch_lo64<KV, VER, false, false>(m, a, s);
+    }
+  } else if (L.ns_lo == 1) {
+    launch_lo_f<KV, VER, 1>(m, a, L.nw_lo, s);
+  } else {
+    launch_lo_f<KV, VER, 2>(m, a, L.nw_lo, s);
+  }
 }
 
 template <int KV, int VER>

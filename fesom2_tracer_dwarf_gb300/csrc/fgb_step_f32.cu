@@ -96,7 +96,9 @@ int launch_stages_f32(const DMesh& m, const fgb_step_desc& d, int mask, cudaStre
   L.nw_upd = pick(d.cfg[3], 1, 2, 4, 4);
   auto ns = [](int want, int def) { return (want == 1 || want == 2) ? want : def; };
   L.ns_h = ns(d.cfg[7], 2);
-  L.ns_lo = ns(d.cfg[4], 2);
+  // LO: 3 (the default where it applies) the whole-column kernel for columns
+  // of at most 64 layers without w_split; 1 or 2 layers per lane per pass
+  L.ns_lo = (d.cfg[4] == 1 || d.cfg[4] == 2) ? d.cfg[4] : (m.LZ <= 64 && !(d.lim == FGB_LIM_FCT && d.wi) ? 3 : 2);
   // ratio: 1 or 2 layers per lane with shared-memory staging, or 3 (the default)
   // the whole column per warp without shared memory
   L.ns_ratio = (d.cfg[5] >= 1 && d.cfg[5] <= 4) ? d.cfg[5] : 0;
