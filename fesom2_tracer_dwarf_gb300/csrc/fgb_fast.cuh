@@ -774,9 +774,10 @@ __device__ __forceinline__ void vimpl_row(int k, int k0, int k1, float W0, float
 
 // ---------------------------------------------------------------------------
 // FCT stage 1: low-order solution and vertical antidiffusive flux
-// (lib/oce_adv_tra_driver.F90:91-235). Low-order edge flux of edge j at this
-// node: role 0 -(vp T_n + vm T_o)/2, role 1 +(vp T_o + vm T_n)/2, with
-// vp = v + |v|, vm = v - |v|; the T_n coefficients are summed first.
+// (lib/oce_adv_tra_driver.F90:91-235). The low-order edge flux
+// -(T1 (v + |v|) + T2 (v - |v|)) / 2 is exactly -v T_up with T_up the value
+// at the upwind node; this node adds -v T_up (role 0, the edge's first node)
+// or +v T_up (role 1), the same rounded product at both ends of the edge.
 // ---------------------------------------------------------------------------
 template <int VER, int KV, int NS, bool WSPLIT>
 __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
@@ -868,16 +869,15 @@ __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
     for (unsigned base = 0; base < LZ; base += kW * NS) {
       unsigned kk[NS];
       bool in[NS];
-      float cn[NS];
-      V<KV> acc[NS];
+      V<KV> acc[NS], tnk[NS];
       float hnv[NS], hnnv[NS], avv[NS];
 #pragma unroll
       for (int i = 0; i < NS; ++i) {
         const unsigned k = base + lane + kW * i;
         in[i] = k < LZ;
         kk[i] = in[i] ? k : LZ - 1;
-        cn[i] = 0.f;
         acc[i] = splat<KV>(0.f);
+        tnk[i] = sT[kk[i]];
         hnv[i] = g.hnode[n * LZ + kk[i]];
         hnnv[i] = g.hnode_new[n * LZ + kk[i]];
         avv[i] = g.areasvol[n * LZ + kk[i]];
@@ -896,11 +896,12 @@ __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
         }
 #pragma unroll
         for (int i = 0; i < NS; ++i) {
-          const float vp = v[i] + fabsf(v[i]), vmn = v[i] - fabsf(v[i]);
-          const float cnj = role ? 0.5f * vmn : -0.5f * vp;
-          const float coj = role ? 0.5f * vp : -0.5f * vmn;
-          cn[i] += cnj;
-          acc[i] = fmas(to[i], coj, acc[i]);
+          const bool own_up = (v[i] >= 0.f) != role;  // the flux leaves this node
+          V<KV> tu;
+#pragma unroll
+          for (int c = 0; c < KV; ++c) tu.v[c] = own_up ? tnk[i].v[c] : to[i].v[c];
+          const V<KV> p = muls(tu, v[i]);
+          acc[i] = role ? add(acc[i], p) : sub(acc[i], p);
         }
       }
       V<KV> lk[NS];
@@ -910,8 +911,8 @@ __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
         if (!in[i]) continue;
         const unsigned k = kk[i];
         const int z = (int)k + 1;
-        const V<KV> tn = sT[k];
-        V<KV> l = fmas(tn, cn[i], acc[i]);
+        const V<KV> tn = tnk[i];
+        V<KV> l = acc[i];
         if (z >= nzmin && z <= nzmax - 1) {
           const float hn = hnv[i], hnn = hnnv[i], av = avv[i];
           const float ra = hn / hnn, rb = fdv(dt, av * hnn);  // ra IEEE: exactly 1 for an unchanged layer

@@ -102,11 +102,16 @@ void launch_ratio64(const DMesh& m, const FastPtrs& a, int nw, cudaStream_t s) {
   else kf_ratio64<KV, LEAN, false><<<grid, nw * kW, sm, s>>>(m, a);
 }
 
+template <int KV, int VER, bool TASEP, bool WESEP, bool COMP>
+void launch_lo64c(const DMesh& m, const FastPtrs& a, cudaStream_t s) {
+  const size_t sm = kLo64Warps * lo64_warp_bytes(KV, VER, TASEP);
+  allow_smem_f(kf_lo64<VER, KV, TASEP, WESEP, COMP>, sm);
+  kf_lo64<VER, KV, TASEP, WESEP, COMP><<<(m.N + kLo64Warps - 1) / kLo64Warps, kLo64Warps * kW, sm, s>>>(m, a);
+}
 template <int KV, int VER, bool TASEP, bool WESEP>
 void launch_lo64(const DMesh& m, const FastPtrs& a, cudaStream_t s) {
-  const size_t sm = kLo64Warps * lo64_warp_bytes(KV, VER, TASEP);
-  allow_smem_f(kf_lo64<VER, KV, TASEP, WESEP>, sm);
-  kf_lo64<VER, KV, TASEP, WESEP><<<(m.N + kLo64Warps - 1) / kLo64Warps, kLo64Warps * kW, sm, s>>>(m, a);
+  if (a.comp) launch_lo64c<KV, VER, TASEP, WESEP, true>(m, a, s);
+  else launch_lo64c<KV, VER, TASEP, WESEP, false>(m, a, s);
 }
 
 template <int KV, int VER>

@@ -33,7 +33,7 @@ __host__ __device__ constexpr size_t lo64_warp_bytes(int KV, int ver, bool tasep
          (ver == 3 ? 2 * 64 * 4 : 0) + (ver == 1 ? (64 + 68) * 4 : 0) + kMaxDegF * sizeof(int2);
 }
 
-template <int VER, int KV, bool TASEP, bool WESEP>
+template <int VER, int KV, bool TASEP, bool WESEP, bool COMP>
 __global__ void __launch_bounds__(kLo64Warps * kW, 7) kf_lo64(DMesh m, FastPtrs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
@@ -239,9 +239,13 @@ __global__ void __launch_bounds__(kLo64Warps * kW, 7) kf_lo64(DMesh m, FastPtrs 
     }
     __syncwarp();
     // LO horizontal fluxes (upwind, lib/oce_adv_tra_hor.F90:218-220) gathered
-    // over the incident edges in ascending edge order, T_n coefficients first
-    float cn[2] = {0.f, 0.f};
-    V<KV> acc[2] = {splat<KV>(0.f), splat<KV>(0.f)};
+    // over the incident edges in ascending edge order. The upwind flux
+    // -(T1 (v + |v|) + T2 (v - |v|)) / 2 is exactly -v T_up, T_up the value at
+    // the upwind node: each node adds -v T_up (first node) or +v T_up (second
+    // node), one rounded product that is the same number at both ends of the
+    // edge, so the low-order fluxes cancel between neighbours; with COMP the
+    // products are summed with compensation.
+    V<KV> acc[2] = {splat<KV>(0.f), splat<KV>(0.f)}, accc[2] = {splat<KV>(0.f), splat<KV>(0.f)};
     const unsigned kc[2] = {(unsigned)min(k[0], LZ - 1), (unsigned)min(k[1], LZ - 1)};
 #pragma unroll 2
     for (int j = 0; j < deg; ++j) {
@@ -257,9 +261,14 @@ __global__ void __launch_bounds__(kLo64Warps * kW, 7) kf_lo64(DMesh m, FastPtrs 
       }
 #pragma unroll
       for (int s = 0; s < 2; ++s) {
-        const float vp = v[s] + fabsf(v[s]), vmn = v[s] - fabsf(v[s]);
-        cn[s] += role ? 0.5f * vmn : -0.5f * vp;
-        acc[s] = fmas(to[s], role ? 0.5f * vp : -0.5f * vmn, acc[s]);
+        // this node is upwind when the flux leaves it: v >= 0 at the first node, v < 0 at the second
+        const bool own_up = (v[s] >= 0.f) != role;
+        V<KV> tu;
+#pragma unroll
+        for (int c = 0; c < KV; ++c) tu.v[c] = own_up ? t[s].v[c] : to[s].v[c];
+        const V<KV> p = muls(tu, v[s]);
+        if (COMP) two_sum(acc[s], accc[s], role ? p : sub(splat<KV>(0.f), p));
+        else acc[s] = role ? add(acc[s], p) : sub(acc[s], p);
       }
     }
     float* __restrict__ lo = a.lo + gi * a.gN;
@@ -267,7 +276,7 @@ __global__ void __launch_bounds__(kLo64Warps * kW, 7) kf_lo64(DMesh m, FastPtrs 
     for (int s = 0; s < 2; ++s) {
       if (!lay[s]) continue;
       const int z = k[s] + 1;
-      V<KV> l = fmas(t[s], cn[s], acc[s]);
+      V<KV> l = COMP ? add(acc[s], accc[s]) : acc[s];
       if (z >= nzmin && z <= nzmax - 1) l = fmas(add(l, sub(flo[s], sF[k[s] + 1])), rb[s], muls(t[s], ra[s]));
       st<KV>(lo, (unsigned)n * LZ + k[s], l);
     }
