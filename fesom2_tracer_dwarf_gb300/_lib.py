@@ -14,7 +14,7 @@ from . import build as _build
 HOR = {"UPW1": 0, "MUSCL": 1, "MFCT": 2}
 VER = {"UPW1": 0, "QR4C": 1, "CDIFF": 2, "PPM": 3}
 LIM = {"NONE": 0, "FCT": 1}
-FP64, FP32 = 0, 1
+FP64, FP32, FP64_FAST = 0, 1, 2
 NCFG = 12  # launch knobs of fgb_step_desc.cfg
 STAGE_VFLUX, STAGE_HFLUX, STAGE_LO, STAGE_RATIO, STAGE_UPDATE = 1, 2, 4, 8, 16
 STAGE_ALL = 31

@@ -33,6 +33,7 @@ SOURCES = [
     ("fgb_capi.cpp", "cxx", []),
     ("fgb_api.cu", "nvcc", []),
     ("fgb_step_f64.cu", "nvcc", ["-fmad=false"]),
+    ("fgb_step_f64fast.cu", "nvcc", []),
     ("fgb_step_f32.cu", "nvcc", []),
     ("fgb_fast_kv1.cu", "nvcc", []),
     ("fgb_fast_kv2.cu", "nvcc", []),

@@ -418,6 +418,7 @@ int fgb_adv_stages(const fgb_mesh* m, const fgb_step_desc* d, int mask, void* st
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (d->precision == FGB_FP64) rc = launch_stages_f64(m->d, *d, mask, s, &n, &err);
   else if (d->precision == FGB_FP32) rc = launch_stages_f32(m->d, *d, mask, s, &n, &err);
+  else if (d->precision == FGB_FP64_FAST) rc = launch_stages_f64fast(m->d, *d, mask, s, &n, &err);
   else { err = "unknown precision"; rc = -1; }
   g_last_launches = n;
   if (rc) set_error(err);

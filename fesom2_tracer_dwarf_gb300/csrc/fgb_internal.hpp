@@ -42,6 +42,8 @@ int launch_stages_f64(const DMesh& m, const fgb_step_desc& d, int mask, cudaStre
                       std::string* err);
 int launch_stages_f32(const DMesh& m, const fgb_step_desc& d, int mask, cudaStream_t s, int* nlaunch,
                       std::string* err);
+int launch_stages_f64fast(const DMesh& m, const fgb_step_desc& d, int mask, cudaStream_t s, int* nlaunch,
+                          std::string* err);
 
 void set_error(const std::string& msg);
 

@@ -18,7 +18,22 @@
 
 #include "fgb_device.hpp"
 
+#ifndef FGB_FAST64
+#define FGB_FAST64 0
+#endif
+
 namespace fgb {
+// Two compilations of these kernels live side by side, kept apart by their
+// inline namespace: the bit-exact FP64 form (no fused multiply-add, every
+// division as the reference writes it) and, with FGB_FAST64, the fast FP64
+// form (fused multiply-add; divisions by constants become products with the
+// reciprocal constant, and dt / areasvol and 1 / hnode_new are formed once
+// per layer and shared by the tracers and edges of a node).
+#if FGB_FAST64
+inline namespace fast64 {
+#else
+inline namespace exact64 {
+#endif
 
 constexpr int kWarp = 32;
 
@@ -49,6 +64,33 @@ template <>
 __device__ __forceinline__ double fdiv<double>(double a, double b) { return a / b; }
 template <>
 __device__ __forceinline__ float fdiv<float>(float a, float b) { return __fdividef(a, b); }
+// a / c for a constant c: the reference's division, or (fast form) the product
+// with the reciprocal constant.
+template <typename R>
+__device__ __forceinline__ R fdivc(R a, R c) {
+  if constexpr (FGB_FAST64) return a * (R(1) / c);
+  else return fdiv(a, c);
+}
+// (x dt) / areasvol: the reference's order, or (fast form) x times the
+// layer's dt / areasvol, formed once.
+template <typename R>
+__device__ __forceinline__ R dt_per_vol(R x, R dt, R av, R rdt_av) {
+  if constexpr (FGB_FAST64) return x * rdt_av;
+  else return fdiv(x * dt, av);
+}
+// a / g for a geometric g shared by the tracers of a column: the reference's
+// division, or (fast form) the product with 1 / g, which the compiler forms
+// once for all tracers.
+template <typename R>
+__device__ __forceinline__ R fdivg(R a, R g) {
+  if constexpr (FGB_FAST64) return a * (R(1) / g);
+  else return fdiv(a, g);
+}
+template <typename R>
+__device__ __forceinline__ R rdt_vol(R dt, R av) {
+  if constexpr (FGB_FAST64) return dt / av;
+  else return R(0);  // unused by the exact form
+}
 
 // Layer membership of the horizontal-flux segments A-E of
 // lib/oce_adv_tra_hor.F90:171-252 (1-based layer z): which elements' volume
@@ -213,11 +255,11 @@ __device__ __forceinline__ R ho_flux(R v, R vp, R vm, R ta1, R ta2, R g1, R g2, 
   if (HOR == 0) return -(R(0.5) * (ta1 * vp + ta2 * vm));
   R Tm2, Tm1;
   if (HOR == 1) {
-    Tm2 = ta2 - fdiv(R(2) * (ta2 - ta1) + ex * g2 + ey * g4, R(6)) * c2;
-    Tm1 = ta1 + fdiv(R(2) * (ta2 - ta1) + ex * g1 + ey * g3, R(6)) * c1;
+    Tm2 = ta2 - fdivc(R(2) * (ta2 - ta1) + ex * g2 + ey * g4, R(6)) * c2;
+    Tm1 = ta1 + fdivc(R(2) * (ta2 - ta1) + ex * g1 + ey * g3, R(6)) * c1;
   } else {
-    Tm2 = ta2 - fdiv(R(2) * (ta2 - ta1) + ex * g2 + ey * g4, R(6));
-    Tm1 = ta1 + fdiv(R(2) * (ta2 - ta1) + ex * g1 + ey * g3, R(6));
+    Tm2 = ta2 - fdivc(R(2) * (ta2 - ta1) + ex * g2 + ey * g4, R(6));
+    Tm1 = ta1 + fdivc(R(2) * (ta2 - ta1) + ex * g1 + ey * g3, R(6));
   }
   const R cHO = vp * Tm1 + vm * Tm2;
   return -((R(0.5) * (R(1) - ph)) * cHO) - ((v * ph) * R(0.5)) * (Tm1 + Tm2);
@@ -373,12 +415,12 @@ __device__ __forceinline__ R ver_qr4c(const Col<R>& c, int z, int nzmin, int nzm
   }
   const R T0 = c.T[z - 1], Tm1 = c.T[z - 2], Tm2 = c.T[z - 3], Tp1 = c.T[z];
   const R Z0 = c.Z[z - 1], Zm1 = c.Z[z - 2], Zm2 = c.Z[z - 3], Zp1 = c.Z[z];
-  const R qc = fdiv(Tm1 - T0, Zm1 - Z0);
-  const R qu = fdiv(T0 - Tp1, Z0 - Zp1);
-  const R qd = fdiv(Tm2 - Tm1, Zm2 - Zm1);
+  const R qc = fdivg(Tm1 - T0, Zm1 - Z0);
+  const R qu = fdivg(T0 - Tp1, Z0 - Zp1);
+  const R qd = fdivg(Tm2 - Tm1, Zm2 - Zm1);
   const R zb = c.zb[z - 1];
-  const R tm1 = T0 + fdiv((R(2) * qc + qu) * (zb - Z0), R(3));
-  const R tm2 = Tm1 + fdiv((R(2) * qc + qd) * (zb - Zm1), R(3));
+  const R tm1 = T0 + fdivc((R(2) * qc + qu) * (zb - Z0), R(3));
+  const R tm2 = Tm1 + fdivc((R(2) * qc + qd) * (zb - Zm1), R(3));
   const R tm = (W + rabs(W)) * tm1 + (W - rabs(W)) * tm2;
   return (-((R(0.5) * (R(1) - num_ord)) * tm) - (num_ord * (R(0.5) * (tm1 + tm2))) * W) * c.area[z - 1] - fold;
 }
@@ -437,14 +479,14 @@ __device__ __forceinline__ R ppm_layer_x(R aL, R aR, R T0, R x, bool upper, R ar
     aL = T0;
     aR = T0;
   }
-  if ((aR - aL) * (T0 - R(0.5) * (aL + aR)) > fdiv((aR - aL) * (aR - aL), R(6))) aL = R(3) * T0 - R(2) * aR;
-  if ((aR - aL) * (T0 - R(0.5) * (aR + aL)) < -fdiv((aR - aL) * (aR - aL), R(6))) aR = R(3) * T0 - R(2) * aL;
+  if ((aR - aL) * (T0 - R(0.5) * (aL + aR)) > fdivc((aR - aL) * (aR - aL), R(6))) aL = R(3) * T0 - R(2) * aR;
+  if ((aR - aL) * (T0 - R(0.5) * (aR + aL)) < -fdivc((aR - aL) * (aR - aL), R(6))) aR = R(3) * T0 - R(2) * aL;
   const R aj = R(6) * (T0 - R(0.5) * (aL + aR));
   if (upper) {
-    R tv = -aL - (R(0.5) * x) * ((aR - aL) + (R(1) - fdiv(R(2), R(3)) * x) * aj);
+    R tv = -aL - (R(0.5) * x) * ((aR - aL) + (R(1) - fdivc(R(2), R(3)) * x) * aj);
     return (tv * area) * W;
   }
-  R tv = -aR + (R(0.5) * x) * ((aR - aL) - (R(1) - fdiv(R(2), R(3)) * x) * aj);
+  R tv = -aR + (R(0.5) * x) * ((aR - aL) - (R(1) - fdivc(R(2), R(3)) * x) * aj);
   return (tv * area) * W;
 }
 
@@ -735,13 +777,21 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_fct_lo(DMesh 
       const vec2<R> hn = ld2(g.hnode + n * LZ + k0), hnn = ld2(g.hnode_new + n * LZ + k0);
       const vec2<R> av = ld2(g.areasvol + n * LZ + k0);
       const bool w0 = z0 >= nzmin && z0 <= nzmax - 1, w1 = z1 >= nzmin && z1 <= nzmax - 1;
+      // fast form: dt / areasvol and 1 / hnode_new of the two layers, once
+      const vec2<R> rd{rdt_vol(dt, av.x), rdt_vol(dt, av.y)};
+      const vec2<R> rh{FGB_FAST64 ? R(1) / hnn.x : R(0), FGB_FAST64 ? R(1) / hnn.y : R(0)};
 #pragma unroll
       for (int i = 0; i < KC; ++i) {
         const R* Ti = sT + i * LW;
         const R* Fi = sFv + i * LW;
         R l0 = acc0[i], l1 = acc1[i];
-        if (w0) l0 = fdiv(Ti[k0] * hn.x + fdiv((acc0[i] + (Fi[k0] - Fi[k0 + 1])) * dt, av.x), hnn.x);
-        if (w1) l1 = fdiv(Ti[k0 + 1] * hn.y + fdiv((acc1[i] + (Fi[k0 + 1] - Fi[k0 + 2])) * dt, av.y), hnn.y);
+        if constexpr (FGB_FAST64) {
+          if (w0) l0 = (Ti[k0] * hn.x + (acc0[i] + (Fi[k0] - Fi[k0 + 1])) * rd.x) * rh.x;
+          if (w1) l1 = (Ti[k0 + 1] * hn.y + (acc1[i] + (Fi[k0 + 1] - Fi[k0 + 2])) * rd.y) * rh.y;
+        } else {
+          if (w0) l0 = fdiv(Ti[k0] * hn.x + fdiv((acc0[i] + (Fi[k0] - Fi[k0 + 1])) * dt, av.x), hnn.x);
+          if (w1) l1 = fdiv(Ti[k0 + 1] * hn.y + fdiv((acc1[i] + (Fi[k0 + 1] - Fi[k0 + 2])) * dt, av.y), hnn.y);
+        }
         st2(a.lo + (t0 + i) * a.sN + n * LZ + k0, l0, l1);
       }
     }
@@ -899,9 +949,10 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_fct_ratio(DMe
             bmin = rmin(rmin(mns[k - 1], mns[k]), mns[k + 1]) - lov;
           }
           const R avk = l ? av.y : av.x;
-          R flux = fdiv((l ? pl1[i] : pl0[i]) * dt, avk) + R(1e-16);
+          const R rdk = rdt_vol(dt, avk);
+          R flux = dt_per_vol((l ? pl1[i] : pl0[i]), dt, avk, rdk) + R(1e-16);
           out_p[l] = rmin(R(1), fdiv(bmax, flux));
-          flux = fdiv((l ? mi1[i] : mi0[i]) * dt, avk) - R(1e-16);
+          flux = dt_per_vol((l ? mi1[i] : mi0[i]), dt, avk, rdk) - R(1e-16);
           out_m[l] = rmin(R(1), fdiv(bmin, flux));
         }
         st4(a.rpm + 2 * ((t0 + i) * a.sN + n * LZ + k0), out_p[0], out_m[0], out_p[1], out_m[1]);
@@ -973,6 +1024,7 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_fct_update(DM
     for (int p = lane; 2 * p < m.LZ; p += kWarp) {
       const int k0 = 2 * p, z0 = k0 + 1, z1 = k0 + 2;
       const vec2<R> av = ld2(g.areasvol + n * LZ + k0);
+      const vec2<R> rd{rdt_vol(dt, av.x), rdt_vol(dt, av.y)};  // fast form only
       R dh0[KC], dh1[KC];
 #pragma unroll
       for (int i = 0; i < KC; ++i) dh0[i] = dh1[i] = R(0);
@@ -994,20 +1046,21 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_fct_update(DM
             else { ae0 = rmin(ae0, rmo.x); ae0 = rmin(ae0, rpn0); }
             if (f.y >= R(0)) { ae1 = rmin(ae1, rpo.y); ae1 = rmin(ae1, rmn1); }
             else { ae1 = rmin(ae1, rmo.y); ae1 = rmin(ae1, rpn1); }
-            if (a0) dh0[i] = dh0[i] - fdiv((ae0 * f.x) * dt, av.x);
-            if (a1) dh1[i] = dh1[i] - fdiv((ae1 * f.y) * dt, av.y);
+            if (a0) dh0[i] = dh0[i] - dt_per_vol(ae0 * f.x, dt, av.x, rd.x);
+            if (a1) dh1[i] = dh1[i] - dt_per_vol(ae1 * f.y, dt, av.y, rd.y);
           } else {
             if (f.x >= R(0)) { ae0 = rmin(ae0, rpn0); ae0 = rmin(ae0, rmo.x); }
             else { ae0 = rmin(ae0, rmn0); ae0 = rmin(ae0, rpo.x); }
             if (f.y >= R(0)) { ae1 = rmin(ae1, rpn1); ae1 = rmin(ae1, rmo.y); }
             else { ae1 = rmin(ae1, rmn1); ae1 = rmin(ae1, rpo.y); }
-            if (a0) dh0[i] = dh0[i] + fdiv((ae0 * f.x) * dt, av.x);
-            if (a1) dh1[i] = dh1[i] + fdiv((ae1 * f.y) * dt, av.y);
+            if (a0) dh0[i] = dh0[i] + dt_per_vol(ae0 * f.x, dt, av.x, rd.x);
+            if (a1) dh1[i] = dh1[i] + dt_per_vol(ae1 * f.y, dt, av.y, rd.y);
           }
         }
       }
       const vec2<R> hn = ld2(g.hnode + n * LZ + k0), hnn = ld2(g.hnode_new + n * LZ + k0);
       const bool w0 = z0 >= nzmin && z0 <= nzmax - 1, w1 = z1 >= nzmin && z1 <= nzmax - 1;
+      const vec2<R> rh{FGB_FAST64 ? R(1) / hnn.x : R(0), FGB_FAST64 ? R(1) / hnn.y : R(0)};
 #pragma unroll
       for (int i = 0; i < KC; ++i) {
         R* __restrict__ T = a.T + (t0 + i) * a.sT + n * LZ + k0;
@@ -1017,11 +1070,18 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_fct_update(DM
         R* del = a.del ? a.del + (t0 + i) * a.sN + n * LZ + k0 : nullptr;
         const vec2<R> d0 = del ? ld2(del) : vec2<R>{R(0), R(0)};
         R dv0 = (R(0) - Tn.x * hn.x) + lo.x * hnn.x;
-        dv0 = dv0 + fdiv((Lv[k0] - Lv[k0 + 1]) * dt, av.x);
+        dv0 = dv0 + dt_per_vol(Lv[k0] - Lv[k0 + 1], dt, av.x, rd.x);
         R dv1 = (R(0) - Tn.y * hn.y) + lo.y * hnn.y;
-        dv1 = dv1 + fdiv((Lv[k0 + 1] - Lv[k0 + 2]) * dt, av.y);
+        dv1 = dv1 + dt_per_vol(Lv[k0 + 1] - Lv[k0 + 2], dt, av.y, rd.y);
         const R e0 = d0.x + dh0[i] + dv0, e1 = d0.y + dh1[i] + dv1;
-        const R n0 = w0 ? Tn.x + fdiv(e0, hnn.x) : Tn.x, n1v = w1 ? Tn.y + fdiv(e1, hnn.y) : Tn.y;
+        R n0 = Tn.x, n1v = Tn.y;
+        if constexpr (FGB_FAST64) {
+          if (w0) n0 = Tn.x + e0 * rh.x;
+          if (w1) n1v = Tn.y + e1 * rh.y;
+        } else {
+          if (w0) n0 = Tn.x + fdiv(e0, hnn.x);
+          if (w1) n1v = Tn.y + fdiv(e1, hnn.y);
+        }
         st2(T, n0, n1v);
         if (del) st2(del, w0 ? e0 : d0.x, w1 ? e1 : d0.y);
         if (a.TAout) {
@@ -1083,6 +1143,7 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_nofct_update(
     for (int p = lane; 2 * p < m.LZ; p += kWarp) {
       const int k0 = 2 * p, z0 = k0 + 1, z1 = k0 + 2;
       const vec2<R> av = ld2(g.areasvol + n * LZ + k0);
+      const vec2<R> rd{rdt_vol(dt, av.x), rdt_vol(dt, av.y)};  // fast form only
       R dh0[KC], dh1[KC];
 #pragma unroll
       for (int i = 0; i < KC; ++i) dh0[i] = dh1[i] = R(0);
@@ -1094,16 +1155,17 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_nofct_update(
         for (int i = 0; i < KC; ++i) {
           const vec2<R> f = ld2(a.adfh + (t0 + i) * a.sE + (size_t)q.e * LZ + k0);
           if (q.role) {
-            if (a0) dh0[i] = dh0[i] - fdiv(f.x * dt, av.x);
-            if (a1) dh1[i] = dh1[i] - fdiv(f.y * dt, av.y);
+            if (a0) dh0[i] = dh0[i] - dt_per_vol(f.x, dt, av.x, rd.x);
+            if (a1) dh1[i] = dh1[i] - dt_per_vol(f.y, dt, av.y, rd.y);
           } else {
-            if (a0) dh0[i] = dh0[i] + fdiv(f.x * dt, av.x);
-            if (a1) dh1[i] = dh1[i] + fdiv(f.y * dt, av.y);
+            if (a0) dh0[i] = dh0[i] + dt_per_vol(f.x, dt, av.x, rd.x);
+            if (a1) dh1[i] = dh1[i] + dt_per_vol(f.y, dt, av.y, rd.y);
           }
         }
       }
       const vec2<R> hnn = ld2(g.hnode_new + n * LZ + k0);
       const bool w0 = z0 >= nzmin && z0 <= nzmax - 1, w1 = z1 >= nzmin && z1 <= nzmax - 1;
+      const vec2<R> rh{FGB_FAST64 ? R(1) / hnn.x : R(0), FGB_FAST64 ? R(1) / hnn.y : R(0)};
 #pragma unroll
       for (int i = 0; i < KC; ++i) {
         const R* F = sF + i * LW;
@@ -1111,10 +1173,17 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_nofct_update(
         const vec2<R> Tn = ld2(T);
         R* del = a.del ? a.del + (t0 + i) * a.sN + n * LZ + k0 : nullptr;
         const vec2<R> d0 = del ? ld2(del) : vec2<R>{R(0), R(0)};
-        const R dv0 = R(0) + fdiv((F[k0] - F[k0 + 1]) * dt, av.x);
-        const R dv1 = R(0) + fdiv((F[k0 + 1] - F[k0 + 2]) * dt, av.y);
+        const R dv0 = R(0) + dt_per_vol(F[k0] - F[k0 + 1], dt, av.x, rd.x);
+        const R dv1 = R(0) + dt_per_vol(F[k0 + 1] - F[k0 + 2], dt, av.y, rd.y);
         const R e0 = d0.x + dh0[i] + dv0, e1 = d0.y + dh1[i] + dv1;
-        const R n0 = w0 ? Tn.x + fdiv(e0, hnn.x) : Tn.x, n1v = w1 ? Tn.y + fdiv(e1, hnn.y) : Tn.y;
+        R n0 = Tn.x, n1v = Tn.y;
+        if constexpr (FGB_FAST64) {
+          if (w0) n0 = Tn.x + e0 * rh.x;
+          if (w1) n1v = Tn.y + e1 * rh.y;
+        } else {
+          if (w0) n0 = Tn.x + fdiv(e0, hnn.x);
+          if (w1) n1v = Tn.y + fdiv(e1, hnn.y);
+        }
         st2(T, n0, n1v);
         if (del) st2(del, w0 ? e0 : d0.x, w1 ? e1 : d0.y);
         if (a.TAout) {
@@ -1128,4 +1197,5 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_nofct_update(
   }
 }
 
+}  // inline namespace
 }  // namespace fgb

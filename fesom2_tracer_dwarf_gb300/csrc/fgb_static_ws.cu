@@ -60,7 +60,7 @@ int fgb_adv_step_static(const fgb_mesh* m, const fgb_step_desc* d, void* stream)
     return -1;
   }
   std::string err;
-  const long long need = (d->precision == FGB_FP64 || d->precision == FGB_FP32)
+  const long long need = (d->precision == FGB_FP64 || d->precision == FGB_FP32 || d->precision == FGB_FP64_FAST)
                              ? fgb_workspace_bytes(m, d->precision, d->ntracers)
                              : -1;
   if (fgb::static_ws_precheck(d->precision, d->ntracers, need, (long long)FGB_STATIC_WORKSPACE_BYTES, m->device,

@@ -5,15 +5,16 @@
 
 namespace fgb {
 
-// precision: FGB_FP64 (0) or FGB_FP32 (1); need: the scratch bytes the mesh
+// precision: FGB_FP64 (0), FGB_FP32 (1) or FGB_FP64_FAST (2); need: the scratch bytes the mesh
 // and tracer count take (fgb_workspace_bytes), cap: the static array's size.
 // mesh_device: the device the mesh was uploaded on; current_device: the
 // calling thread's current device. Returns 0 when the call may proceed, else
 // -1 with the reason in *err.
 inline int static_ws_precheck(int precision, int ntracers, long long need, long long cap, int mesh_device,
                               int current_device, std::string* err) {
-  if (precision != 0 && precision != 1) {
-    *err = "fgb_adv_step_static: unknown precision " + std::to_string(precision) + " (FGB_FP64 or FGB_FP32)";
+  if (precision != 0 && precision != 1 && precision != 2) {
+    *err = "fgb_adv_step_static: unknown precision " + std::to_string(precision) +
+           " (FGB_FP64, FGB_FP32 or FGB_FP64_FAST)";
     return -1;
   }
   if (ntracers < 1) {

@@ -12,6 +12,11 @@
 #include "fgb_vimpl.cuh"
 
 namespace fgb {
+#if FGB_FAST64
+inline namespace fast64 {
+#else
+inline namespace exact64 {
+#endif
 
 constexpr int kEdgeWarps = 8;  // default edges per block
 constexpr int kNodeWarps = 4;  // default node columns per block (the kernels' launch bound)
@@ -197,4 +202,5 @@ int launch_stages(const DMesh& m, const fgb_step_desc& d, int mask, cudaStream_t
   return 0;
 }
 
+}  // inline namespace
 }  // namespace fgb

@@ -18,6 +18,11 @@
 #include "fgb_device.hpp"
 
 namespace fgb {
+#if FGB_FAST64
+inline namespace fast64 {
+#else
+inline namespace exact64 {
+#endif
 
 constexpr int kVimplTracers = 8;  // tracer columns staged per warp and pass
 constexpr int kVimplWarps = 4;    // node columns per block
@@ -149,4 +154,5 @@ inline void launch_vert_impl(const DMesh& m, const GeoPtrs<R>& g, R* lo, const R
   k_vert_impl<R><<<grid, block, smem, s>>>(m, g, lo, wi, K, V, sG, dt);
 }
 
+}  // inline namespace
 }  // namespace fgb

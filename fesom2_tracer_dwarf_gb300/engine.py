@@ -42,8 +42,8 @@ import torch
 from . import _lib
 from .mesh import Mesh
 
-_DT = {"fp64": torch.float64, "fp32": torch.float32}
-_PREC = {"fp64": _lib.FP64, "fp32": _lib.FP32}
+_DT = {"fp64": torch.float64, "fp32": torch.float32, "fp64fast": torch.float64}
+_PREC = {"fp64": _lib.FP64, "fp32": _lib.FP32, "fp64fast": _lib.FP64_FAST}
 
 
 def _require_cuda():
@@ -78,9 +78,9 @@ class TracerAdvection:
         self.mesh, self.K, self.precision = mesh, int(ntracers), precision
         self.dtype = _DT[precision]
         if tracer_vec is None:
-            tracer_vec = 1 if precision == "fp64" else next(v for v in (4, 2, 1) if self.K % v == 0)
-        if tracer_vec not in (1, 2, 4) or self.K % tracer_vec or (precision == "fp64" and tracer_vec != 1):
-            raise ValueError("tracer_vec must be 1 (FP64) or 1, 2, 4 dividing ntracers (FP32)")
+            tracer_vec = 1 if precision != "fp32" else next(v for v in (4, 2, 1) if self.K % v == 0)
+        if tracer_vec not in (1, 2, 4) or self.K % tracer_vec or (precision != "fp32" and tracer_vec != 1):
+            raise ValueError("tracer_vec must be 1 (FP64 forms) or 1, 2, 4 dividing ntracers (FP32)")
         self.V = int(tracer_vec)
         self.G = self.K // self.V
         self.device = torch.device(device)

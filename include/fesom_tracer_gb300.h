@@ -112,7 +112,13 @@ typedef struct fgb_mesh fgb_mesh;   /* device-resident mesh */
 enum { FGB_HOR_UPW1 = 0, FGB_HOR_MUSCL = 1, FGB_HOR_MFCT = 2 };
 enum { FGB_VER_UPW1 = 0, FGB_VER_QR4C = 1, FGB_VER_CDIFF = 2, FGB_VER_PPM = 3 };
 enum { FGB_LIM_NONE = 0, FGB_LIM_FCT = 1 };
-enum { FGB_FP64 = 0, FGB_FP32 = 1 };
+/* FGB_FP64: the bit-exact FP64 form (the reference's evaluation order, no
+ * fused multiply-add). FGB_FP32: FP32 storage and arithmetic, tracers grouped
+ * by fgb_step_desc.tracer_vec. FGB_FP64_FAST: FP64 storage and arithmetic with
+ * fused multiply-add and divisions by constants and by the layer volumes
+ * replaced by products with reciprocals formed once per layer; the FP64
+ * layout and workspace, results within 1e-12 (relative) of FGB_FP64. */
+enum { FGB_FP64 = 0, FGB_FP32 = 1, FGB_FP64_FAST = 2 };
 
 /* Stages of one step (bit mask for fgb_adv_stages). */
 enum {

@@ -12,8 +12,8 @@
 
 The FP64 form must equal the oracle bit for bit (do_oce_adv_tra,
 lib/oce_adv_tra_driver.F90:23-294, in the reference's evaluation order); the
-FP32 form is held to the FP32 bar of the other tests (relative max-norm 1e-5)
-against the same oracle run. The oracle runs on every host core (its loops
+fast FP64 form is held to 1e-12 and the FP32 form to the FP32 bar of the other
+tests (relative max-norm 1e-5) against the same oracle run. The oracle runs on every host core (its loops
 are threaded without changing any result).
 """
 import os
@@ -26,6 +26,7 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 REL_TOL_FP32 = 1e-5
+REL_TOL_FAST64 = 1e-12
 
 
 @pytest.fixture(scope="module")
@@ -119,6 +120,10 @@ def test_config2_512_fp64_bit_exact(config2, hor, flow):
     for t in range(2):
         rel = float(np.abs(got32[t] - vals[t]).max() / np.abs(vals[t]).max())
         assert rel <= REL_TOL_FP32, f"FP32 form, tracer {t}: {rel:.3g}"
+    gotf = _run(O, om, m, engine, vel, w, T, sch, steps, dt, "fp64fast")
+    for t in range(2):
+        rel = float(np.abs(gotf[t] - vals[t]).max() / np.abs(vals[t]).max())
+        assert rel <= REL_TOL_FAST64, f"fast FP64 form, tracer {t}: {rel:.3g}"
 
 
 def test_config3_closed_1024_fp64_bit_exact(pkg, oracle_mod):

@@ -186,3 +186,39 @@ def test_fp32_form_close(pkg, oracle_mod):
     torch.cuda.synchronize()
     rel = _max_err(eng.values(), vals) / float(np.max(np.abs(vals)))
     assert rel <= 1e-5, rel
+
+
+FAST64_TOL = 1e-12  # relative max-norm of the fast FP64 form against the oracle
+
+
+@pytest.mark.parametrize("meshname", ["periodic", "closed_left", "ragged"])
+@pytest.mark.parametrize("hor,ver,lim", list(itertools.product(["UPW1", "MUSCL", "MFCT"],
+                                                                ["UPW1", "QR4C", "CDIFF", "PPM"],
+                                                                ["NONE", "FCT"])))
+def test_fast_fp64_within_1e12(pkg, oracle_mod, meshname, hor, ver, lim):
+    """The fast FP64 form (fused multiply-add, reciprocal products) over five
+    steps with copy-AB, against the oracle: relative max-norm <= 1e-12."""
+    mesh_mod, engine, synthetic = pkg
+    O = oracle_mod
+    kw = _ragged() if meshname == "ragged" else MESHES[meshname]
+    om, m = _pair(O, mesh_mod, **kw)
+    rng = np.random.default_rng(zlib.crc32(f"fast/{meshname}/{hor}/{ver}/{lim}".encode()))
+    vel, w = synthetic.random_flow(m, rng)
+    K = 2
+    T = synthetic.random_field(m, rng, K)
+    dt, steps = 400.0, 5
+    vals = np.ascontiguousarray(T.copy())
+    vab = vals.copy()
+    W = O.Work(om)
+    for _ in range(steps):
+        O.analytic_step(om, W, dt, vel, w, vals, vab, [(hor, ver, lim, 0.7, 0.6)] * K, copy_ab=True)
+    eng = engine.TracerAdvection(m, K, "fp64fast", hor, ver, lim, ph=0.7, pv=0.6, copy_ab=True)
+    eng.set_tracers(T)
+    eng.set_velocity(vel, w)
+    eng.step(dt, steps)
+    torch.cuda.synchronize()
+    nlev = m.get("nlevels_nod2D")
+    wet = np.arange(m.nz)[None, :] < (nlev - 1)[:, None]
+    got = eng.values()
+    rel = max(float(np.abs(got[t] - vals[t])[wet].max() / np.abs(vals[t][wet]).max()) for t in range(K))
+    assert rel <= FAST64_TOL, f"{meshname} {hor}/{ver}/{lim}: fast FP64 relative error {rel:.3g}"

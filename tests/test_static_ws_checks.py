@@ -62,8 +62,8 @@ def test_rejects_a_mesh_on_another_device(checker):
 
 
 def test_rejects_an_unknown_precision(checker):
-    rc, msg = checker(2, 1, 1 << 20, CAP, 0, 0)
-    assert rc == -1 and "unknown precision 2" in msg
+    rc, msg = checker(3, 1, 1 << 20, CAP, 0, 0)
+    assert rc == -1 and "unknown precision 3" in msg
 
 
 def test_rejects_a_bad_tracer_count(checker):
