@@ -718,15 +718,23 @@ def run_gpu(args):
         "clocks": clocks,
     }
     if cfg.get("compare_fp64") is True and not args.no_fp64:
-        m64, e64, T64 = build_case(cfg, "fp64", device)
-        if not args.no_tune:
-            autotune.tune(e64, cfg["dt"], reps=1)
+        # the plain FP64 path: the fast FP64 form (fused multiply-add, shared
+        # reciprocals; within 1e-12 of the bit-exact form) is the denominator of
+        # fp32_over_fp64, the bit-exact form is timed beside it
         n64 = max(2, min(args.steps, args.fp64_steps))
-        tot64, per64, l64 = time_engine(e64, T64, cfg["dt"], n64, min(args.warmup, 2), barrier)
-        ms64 = tot64 / n64
-        result["fp64"] = {"value": job_rate(ms64, cells, dist, device)[1], "ms_per_step": ms64, "steps": n64,
-                          "stage_ms": {k: round(v, 3) for k, v in per64.items()}, "gpu_launches": l64}
+        for key, prec in (("fp64", "fp64fast"), ("fp64_exact", "fp64")):
+            m64, e64, T64 = build_case(cfg, prec, device)
+            if not args.no_tune:
+                autotune.tune(e64, cfg["dt"], reps=1)
+            tot64, per64, l64 = time_engine(e64, T64, cfg["dt"], n64, min(args.warmup, 2), barrier)
+            ms64 = tot64 / n64
+            result[key] = {"form": prec, "value": job_rate(ms64, cells, dist, device)[1], "ms_per_step": ms64,
+                           "steps": n64, "stage_ms": {k: round(v, 3) for k, v in per64.items()},
+                           "gpu_launches": l64}
+            if key == "fp64":
+                del e64, m64, T64
         result["fp32_over_fp64"] = value / result["fp64"]["value"]
+        result["fp32_over_fp64_exact"] = value / result["fp64_exact"]["value"]
         if cfg.get("report_steps") and not args.no_report:
             result["precision_report"] = precision_report(m, eng, T0, e64, T64, cfg["dt"], cfg["report_steps"])
         del e64

@@ -51,9 +51,13 @@ def stage_candidates(stage: str, K: int, precision: str = "fp64", wsplit: bool =
         return [{0: w} for w in EDGE_WARPS]
     slot = {"lo": 0, "ratio": 1, "update": 2}[stage]
     if precision == "fp32":
-        # the ratio kernel also has variants without shared memory (3; 4: fewer registers)
-        slices = SLICES + ((3, 4) if stage == "ratio" else ())
+        # the ratio kernel also has variants without shared memory (3; 4: fewer registers); the
+        # LO stage a whole-column kernel (3: columns of at most 64 layers, not under w_split;
+        # its block shape is fixed, so one candidate)
+        slices = SLICES + ((3, 4) if stage in ("ratio", "update") else ())
         cands = [{1 + slot: w, 4 + slot: ns} for w, ns in product(NODE_WARPS, slices)]
+        if stage == "lo" and not wsplit:
+            cands.append({1 + slot: 0, 4 + slot: 3})
         if stage == "lo" and wsplit:
             cands = [{**c, 8: solver} for c in cands for solver in (0, 1)]
         return cands

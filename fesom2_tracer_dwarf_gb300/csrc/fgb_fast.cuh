@@ -1345,8 +1345,11 @@ __device__ __forceinline__ void finish_node(const DMesh& m, const FastPtrs& a, i
 // divergence cancels between neighbours to the last bit of the sum; without
 // DEL the new value is then LO + T (1 - hnode/hnode_new) + S dt / (areasvol
 // hnode_new), the update of the reference in exact arithmetic.
-template <int KV, int NS, bool DEL, bool COMP>
-__global__ void __launch_bounds__(128, (NS == 1 ? (COMP ? 8 : 9) : 4)) kf_update(DMesh m, FastPtrs a) {
+// UE: incident edges unrolled (their gathers in flight together); deeper
+// unrolling takes registers, so fewer warps are resident.
+template <int KV, int NS, bool DEL, bool COMP, int UE = 2>
+__global__ void __launch_bounds__(128, (NS == 1 ? (UE >= 8 ? 4 : UE >= 4 ? 6 : (COMP ? 8 : 9)) : 4))
+    kf_update(DMesh m, FastPtrs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
   const int n = blockIdx.x * (blockDim.x / kW) + wib;
@@ -1420,7 +1423,7 @@ __global__ void __launch_bounds__(128, (NS == 1 ? (COMP ? 8 : 9) : 4)) kf_update
         hnn[i] = g.hnode_new[n * LZ + kk[i]];
         hn[i] = g.hnode[n * LZ + kk[i]];
       }
-#pragma unroll 2
+#pragma unroll UE
       for (int j = 0; j < nb.deg; ++j) {
         const int2 q = nb.get(m, j);
         const unsigned ed = (unsigned)(q.x >> 1);

@@ -102,7 +102,8 @@ int launch_stages_f32(const DMesh& m, const fgb_step_desc& d, int mask, cudaStre
   // ratio: 1 or 2 layers per lane with shared-memory staging, or 3 (the default)
   // the whole column per warp without shared memory
   L.ns_ratio = (d.cfg[5] >= 1 && d.cfg[5] <= 4) ? d.cfg[5] : 0;
-  L.ns_upd = ns(d.cfg[6], 1);
+  // update: 1 or 2 layers per lane per pass; 3, 4: one layer, 4 or 8 edges unrolled
+  L.ns_upd = (d.cfg[6] >= 1 && d.cfg[6] <= 4) ? d.cfg[6] : 1;
   L.vimpl_thomas = d.cfg[8] == 1;
   // the tiled edge kernel stages rows with 16-byte asynchronous copies
   auto al16 = [](const void* p) { return p == nullptr || reinterpret_cast<uintptr_t>(p) % 16 == 0; };

@@ -24,7 +24,9 @@ def test_candidates_cover_allowed_values():
         "hflux", 4, "fp32")
     lo32 = autotune.stage_candidates("lo", 4, "fp32")
     lo32s = autotune.stage_candidates("lo", 4, "fp32", wsplit=True)
-    assert len(lo32s) == 2 * len(lo32) and {1: 2, 4: 1, 8: 1} in lo32s and {1: 2, 4: 1, 8: 0} in lo32s
+    # the whole-column LO kernel is a candidate only without w_split
+    assert {1: 0, 4: 3} in lo32 and all(c.get(4) != 3 for c in lo32s)
+    assert len(lo32s) == 2 * (len(lo32) - 1) and {1: 2, 4: 1, 8: 1} in lo32s and {1: 2, 4: 1, 8: 0} in lo32s
 
 
 def test_cache_file_round_trip(tmp_path):
