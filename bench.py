@@ -397,11 +397,13 @@ def precision_report(m, e32, T32, e64, T64, dt, steps):
     with the FP64 geometry, and with the FP32-rounded geometry the FP32 form
     itself runs on (its discrete invariant) -- and the FCT extremum
     violations (wet cells outside the initial [min, max], and the largest
-    excursion relative to the initial range). The FP32 form runs three ways,
-    which separates the error sources: "compensated" (the default: compensated
-    flux-divergence and FCT +/- sums), "plain_sums" (plain FP32 sums) and
-    "anomaly" (compensated, each tracer stored as T - c about its initial
-    mean where that shrinks the stored values, offsets="auto")."""
+    excursion relative to the initial range). The FP32 form runs several ways,
+    which separates the error sources: "residual" (each value carries its FP32
+    rounding residual, compensated flux-divergence and FCT +/- sums),
+    "residual_plain_sums" (the same with plain FP32 sums), "compensated" (no
+    residual: FP32 storage rounding), "plain_sums" (neither) and "anomaly"
+    (compensated sums, no residual, each tracer stored as T - c about its
+    initial mean where that shrinks the stored values, offsets="auto")."""
     import torch
 
     e64.T.copy_(T64)
@@ -432,19 +434,19 @@ def precision_report(m, e32, T32, e64, T64, dt, steps):
                                                     for t in range(K)],
                                     "violations": [extrema(b[t], t)[0] for t in range(K)],
                                     "max_excursion": [extrema(b[t], t)[1] for t in range(K)]}}
-    plain0, req0 = e32.plain_sums, e32._offsets_req
-    for name, plain, offs in (("compensated", False, None), ("plain_sums", True, None), ("anomaly", False, "auto")):
+    plain0, req0, res0 = e32.plain_sums, e32._offsets_req, e32.residual
+    variants = (("residual", False, True, None), ("residual_plain_sums", True, True, None),
+                ("compensated", False, False, None), ("plain_sums", True, False, None),
+                ("anomaly", False, False, "auto"))
+    for name, plain, res, offs in variants:
         e32.plain_sums = plain
+        e32.set_residual(res)
         e32._offsets_req = offs
-        e32.load_padded(T=e64.from_layout(T64).clone() if offs else None)
-        if not offs:
-            e32.offsets = None
-            e32.T.copy_(T32)
+        # from the FP64 initial values: rounded to FP32, with their residual where kept
+        e32.load_padded(T=e64.from_layout(T64).clone())
         e32.step(dt, steps)
         torch.cuda.synchronize()
-        a = e32.from_layout(e32.T)[:, :, :nz].double()
-        if e32.offsets is not None:
-            a = a + torch.as_tensor(e32.offsets, device=a.device)[:, None, None]
+        a = e32.full_values()[:, :, :nz]
         r = {"max_rel_err": [float((a[t] - b[t])[wet].abs().max()) / float(b[t][wet].abs().max()) for t in range(K)],
              "sum_rel_err": [abs(float((a[t] * vol).sum()) - s0[t]) / abs(s0[t]) for t in range(K)],
              "sum_rel_err_fp32_geometry": [abs(float((a[t] * vol32).sum()) - s0_32[t]) / abs(s0_32[t])
@@ -455,11 +457,16 @@ def precision_report(m, e32, T32, e64, T64, dt, steps):
             r["offsets"] = [float(c) for c in e32.offsets]
         out[name] = r
     e32.plain_sums, e32._offsets_req = plain0, req0
+    e32.set_residual(res0)
     e32.offsets = None
     e32.T.copy_(T32)
-    # the default form's figures under the keys of earlier reports
-    out["max_rel_err"] = out["compensated"]["max_rel_err"]
-    out["sum_rel_err_fp32"] = out["compensated"]["sum_rel_err"]
+    if e32.Tlo is not None:
+        e32.load_padded(T=e64.from_layout(T64).clone())
+    # the timed form's figures under the keys of earlier reports
+    timed = "residual" if res0 else "compensated"
+    out["timed_form"] = timed
+    out["max_rel_err"] = out[timed]["max_rel_err"]
+    out["sum_rel_err_fp32"] = out[timed]["sum_rel_err"]
     out["sum_rel_err_fp64"] = out["fp64"]["sum_rel_err"]
     return out
 

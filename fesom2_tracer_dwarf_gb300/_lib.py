@@ -54,6 +54,7 @@ class StepDesc(ctypes.Structure):
         ("ab_order", ctypes.c_int),
         ("ab_eps", ctypes.c_double),
         ("fp32_plain_sums", ctypes.c_int),
+        ("Tlo", _vp),
     ]
 
 

@@ -54,10 +54,10 @@ def stage_candidates(stage: str, K: int, precision: str = "fp64", wsplit: bool =
         # the ratio kernel also has variants without shared memory (3; 4: fewer registers); the
         # LO stage a whole-column kernel (3: columns of at most 64 layers, not under w_split;
         # its block shape is fixed, so one candidate)
-        slices = SLICES + ((3, 4) if stage in ("ratio", "update") else ())
+        slices = SLICES + ((3, 4) if stage == "ratio" else ())
         cands = [{1 + slot: w, 4 + slot: ns} for w, ns in product(NODE_WARPS, slices)]
         if stage == "lo" and not wsplit:
-            cands.append({1 + slot: 0, 4 + slot: 3})
+            cands.append({1 + slot: 4, 4 + slot: 3})
         if stage == "lo" and wsplit:
             cands = [{**c, 8: solver} for c in cands for solver in (0, 1)]
         return cands
@@ -122,6 +122,7 @@ def tune(engine, dt: float = 1.0, reps: int = 5, cache_path: str | None = None, 
             return dict(hit, cached=True)
 
     saved = [engine.T.clone()] + ([engine.TA.clone()] if engine.TA is not None else [])
+    saved_lo = engine.Tlo.clone() if getattr(engine, "Tlo", None) is not None else None
     fct = engine.lim == "FCT"
     stages = [("hflux", _lib.STAGE_HFLUX)]
     stages += [("lo", _lib.STAGE_LO), ("ratio", _lib.STAGE_RATIO)] if fct else []
@@ -147,6 +148,8 @@ def tune(engine, dt: float = 1.0, reps: int = 5, cache_path: str | None = None, 
     engine.T.copy_(saved[0])
     if engine.TA is not None:
         engine.TA.copy_(saved[1])
+    if saved_lo is not None:
+        engine.Tlo.copy_(saved_lo)
     torch.cuda.synchronize(engine.device)
     result = {"cfg": cfg, "ms": best_ms}
     _MEMO[key] = result

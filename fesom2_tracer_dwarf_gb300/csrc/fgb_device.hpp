@@ -123,6 +123,7 @@ struct FastPtrs {
   float ab_old, ab_new;
   int wsplit_fused;  // w_split: the LO kernel also solves the implicit vertical step
   int comp;          // compensated flux-divergence and FCT +/- sums (fgb_step_desc.fp32_plain_sums == 0)
+  float* Tlo;        // optional (G,N,LZ,KV), stride gT: the rounding residual of each value of T
 };
 
 // Shared-memory shape of the w_split kernel (kf_vert_impl): a warp holds

@@ -774,7 +774,10 @@ __device__ __forceinline__ void vimpl_row(int k, int k0, int k1, float W0, float
 
 // ---------------------------------------------------------------------------
 // FCT stage 1: low-order solution and vertical antidiffusive flux
-// (lib/oce_adv_tra_driver.F90:91-235). The low-order edge flux
+// (lib/oce_adv_tra_driver.F90:91-235). The FP32 form stores the low-order
+// solution as its increment LO - T (0 outside the column): rounding it to
+// FP32 then costs a rounding of the small increment, not of the value, and
+// the later stages add T back, which they read anyway. The low-order edge flux
 // -(T1 (v + |v|) + T2 (v - |v|)) / 2 is exactly -v T_up with T_up the value
 // at the upwind node; this node adds -v T_up (role 0, the edge's first node)
 // or +v T_up (role 1), the same rounded product at both ends of the edge.
@@ -912,11 +915,11 @@ __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
         const unsigned k = kk[i];
         const int z = (int)k + 1;
         const V<KV> tn = tnk[i];
-        V<KV> l = acc[i];
+        V<KV> l = splat<KV>(0.f);  // the increment LO - T
         if (z >= nzmin && z <= nzmax - 1) {
           const float hn = hnv[i], hnn = hnnv[i], av = avv[i];
           const float ra = hn / hnn, rb = fdv(dt, av * hnn);  // ra IEEE: exactly 1 for an unchanged layer
-          l = fmas(add(l, sub(sFlo[k], sFlo[k + 1])), rb, muls(tn, ra));
+          l = fmas(add(acc[i], sub(sFlo[k], sFlo[k + 1])), rb, muls(tn, ra - 1.f));
         }
         if (WSPLIT && NS == 2 && a.wsplit_fused) lk[i] = l;
         else st<KV>(lo, n * LZ + k, l);
@@ -940,13 +943,13 @@ __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
             ac[r] = act[r] ? A_ : 0.f;
             bc[r] = act[r] ? B_ : 1.f;
             cc[r] = act[r] ? C_ : 0.f;
-            dv[r] = act[r] ? muls(lk[r], hnnv[r]) : splat<KV>(0.f);
+            dv[r] = act[r] ? muls(add(tnk[r], lk[r]), hnnv[r]) : splat<KV>(0.f);  // hnode_new LO
           }
           pcr_solve2<KV>(ac, bc, cc, dv, lane);
 #pragma unroll
           for (int r = 0; r < 2; ++r) {
             const unsigned k = base + lane + kW * r;
-            if (k < LZ) st<KV>(lo, n * LZ + k, act[r] ? dv[r] : lk[r]);
+            if (k < LZ) st<KV>(lo, n * LZ + k, act[r] ? sub(dv[r], tnk[r]) : lk[r]);
           }
         }
       }
@@ -1004,8 +1007,8 @@ __global__ void __launch_bounds__(128, (NS == 1 ? 10 : 7)) kf_ratio(DMesh m, Fas
         V<KV> lv[NS], tv[NS];
 #pragma unroll
         for (int i = 0; i < NS; ++i) {
-          lv[i] = ld<KV>(Lg, c.x * LZ + kk[i]);
           tv[i] = ld<KV>(Tg, c.x * LZ + kk[i]);
+          lv[i] = add(tv[i], ld<KV>(Lg, c.x * LZ + kk[i]));  // LO = T + (LO - T)
         }
 #pragma unroll
         for (int i = 0; i < NS; ++i) {
@@ -1090,7 +1093,7 @@ __global__ void __launch_bounds__(128, (NS == 1 ? 10 : 7)) kf_ratio(DMesh m, Fas
         V<KV> rp = splat<KV>(0.f), rm = rp;
         if (z >= nzmin && z <= nzmax - 1) {
           const float r = fdv(dt, g.areasvol[n * LZ + k]);
-          const V<KV> lv = ld<KV>(Lg, n * LZ + k);
+          const V<KV> lv = add(ld<KV>(Tg, n * LZ + k), ld<KV>(Lg, n * LZ + k));
           const bool edge = z == nzmax - 1 || z == nzmin;
 #pragma unroll
           for (int t = 0; t < KV; ++t) {
@@ -1154,7 +1157,7 @@ __global__ void __launch_bounds__(128, LEAN ? 8 : 7) kf_ratio64(DMesh m, FastPtr
       const float m0 = z[i] > minlev ? -1e3f : -INFINITY;
       mx[i] = splat<KV>(m0);
       mn[i] = splat<KV>(-m0);
-      lo[i] = ld<KV>(Lg, n * LZ + kk[i]);
+      lo[i] = add(ld<KV>(Tg, n * LZ + kk[i]), ld<KV>(Lg, n * LZ + kk[i]));  // LO = T + (LO - T)
     }
 #pragma unroll(LEAN ? 1 : 2)
     for (int j = 0; j < ncl; ++j) {
@@ -1162,8 +1165,8 @@ __global__ void __launch_bounds__(128, LEAN ? 8 : 7) kf_ratio64(DMesh m, FastPtr
       V<KV> lv[2], tv[2];
 #pragma unroll
       for (int i = 0; i < 2; ++i) {
-        lv[i] = ld<KV>(Lg, c * LZ + kk[i]);
         tv[i] = ld<KV>(Tg, c * LZ + kk[i]);
+        lv[i] = add(tv[i], ld<KV>(Lg, c * LZ + kk[i]));
       }
 #pragma unroll
       for (int i = 0; i < 2; ++i)
@@ -1345,11 +1348,13 @@ __device__ __forceinline__ void finish_node(const DMesh& m, const FastPtrs& a, i
 // divergence cancels between neighbours to the last bit of the sum; without
 // DEL the new value is then LO + T (1 - hnode/hnode_new) + S dt / (areasvol
 // hnode_new), the update of the reference in exact arithmetic.
-// UE: incident edges unrolled (their gathers in flight together); deeper
-// unrolling takes registers, so fewer warps are resident.
-template <int KV, int NS, bool DEL, bool COMP, int UE = 2>
-__global__ void __launch_bounds__(128, (NS == 1 ? (UE >= 8 ? 4 : UE >= 4 ? 6 : (COMP ? 8 : 9)) : 4))
-    kf_update(DMesh m, FastPtrs a) {
+// RES (without DEL): each value carries its rounding residual in a.Tlo; the
+// new value T + Tlo + increment is split exactly into its FP32 rounding and
+// the new residual (TwoSum), so increments below half an FP32 unit of T --
+// the rule, not the exception, where the flow is slow -- accumulate instead
+// of being rounded away.
+template <int KV, int NS, bool DEL, bool COMP, bool RES = false>
+__global__ void __launch_bounds__(128, (NS == 1 ? (COMP || RES ? 8 : 9) : 4)) kf_update(DMesh m, FastPtrs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
   const int n = blockIdx.x * (blockDim.x / kW) + wib;
@@ -1404,7 +1409,7 @@ __global__ void __launch_bounds__(128, (NS == 1 ? (UE >= 8 ? 4 : UE >= 4 ? 6 : (
     float* del = DEL ? a.del + gi * a.gN : nullptr;
     for (unsigned base = 0; base < LZ; base += kW * NS) {
       unsigned kk[NS];
-      V<KV> dh[NS], dc[NS], rpn[NS], rmn[NS], lo[NS], Tn[NS], d0[NS];
+      V<KV> dh[NS], dc[NS], rpn[NS], rmn[NS], lo[NS], Tn[NS], d0[NS], tl[NS];
       float av[NS], hnn[NS], hn[NS];
 #pragma unroll
       for (int i = 0; i < NS; ++i) {
@@ -1419,11 +1424,12 @@ __global__ void __launch_bounds__(128, (NS == 1 ? (UE >= 8 ? 4 : UE >= 4 ? 6 : (
         lo[i] = ld<KV>(Lg, n * LZ + kk[i]);
         Tn[i] = ld<KV>(Tg, n * LZ + kk[i]);
         d0[i] = DEL ? ld<KV>(del, n * LZ + kk[i]) : splat<KV>(0.f);
+        tl[i] = RES ? ld<KV>(a.Tlo + gi * a.gT, n * LZ + kk[i]) : splat<KV>(0.f);
         av[i] = g.areasvol[n * LZ + kk[i]];
         hnn[i] = g.hnode_new[n * LZ + kk[i]];
         hn[i] = g.hnode[n * LZ + kk[i]];
       }
-#pragma unroll UE
+#pragma unroll 2
       for (int j = 0; j < nb.deg; ++j) {
         const int2 q = nb.get(m, j);
         const unsigned ed = (unsigned)(q.x >> 1);
@@ -1457,27 +1463,39 @@ __global__ void __launch_bounds__(128, (NS == 1 ? (UE >= 8 ? 4 : UE >= 4 ? 6 : (
         const unsigned k = base + lane + kW * i;
         if (k >= LZ) continue;
         const int z = (int)k + 1;
-        V<KV> tnew = Tn[i], enew = d0[i];
+        V<KV> tnew = Tn[i], enew = d0[i], tlnew = tl[i];
         if (z >= nzmin && z <= nzmax - 1) {
           const float r = fdv(dt, av[i]);
           const float ra = hn[i] / hnn[i];  // IEEE: exactly 1 for an unchanged layer
+          // lo holds LO - T, so LO - T hnode / hnode_new = (LO - T) + T (1 - ra),
+          // exactly LO - T when the layer keeps its thickness
+          const V<KV> dlo = fmas(Tn[i], 1.f - ra, lo[i]);
+          V<KV> inc;  // the new value minus T
           if (COMP && !DEL) {
             // S = horizontal + vertical antidiffusive divergence, compensated
             two_sum(dh[i], dc[i], sLv[k]);
             two_sum(dh[i], dc[i], sub(splat<KV>(0.f), sLv[k + 1]));
             const float q = fdv(dt, av[i] * hnn[i]);
-            const V<KV> base = fmas(Tn[i], 1.f - ra, lo[i]);  // T (1 - ra) is exactly 0 when ra = 1
-            tnew = fmas(dh[i], q, fmas(dc[i], q, base));
+            inc = fmas(dh[i], q, fmas(dc[i], q, dlo));
           } else {
             if (COMP) dh[i] = add(dh[i], dc[i]);
-            // -T hnode + LO hnode_new as hnode_new (LO - T hnode / hnode_new): exactly
-            // zero when LO equals T and the layer keeps its thickness
-            const V<KV> dv = fmas(sub(lo[i], muls(Tn[i], ra)), hnn[i], muls(sub(sLv[k], sLv[k + 1]), r));
+            // -T hnode + LO hnode_new as hnode_new (LO - T hnode / hnode_new)
+            const V<KV> dv = fmas(dlo, hnn[i], muls(sub(sLv[k], sLv[k + 1]), r));
             enew = add(add(d0[i], muls(dh[i], r)), dv);
-            tnew = fmas(enew, fdv(1.f, hnn[i]), Tn[i]);
+            inc = muls(enew, fdv(1.f, hnn[i]));
+          }
+          if (RES) {
+            // T + (Tlo + inc) = tnew + tlnew exactly
+            const V<KV> b = add(tl[i], inc);
+            tnew = add(Tn[i], b);
+            const V<KV> bp = sub(tnew, Tn[i]);
+            tlnew = add(sub(Tn[i], sub(tnew, bp)), sub(b, bp));
+          } else {
+            tnew = add(Tn[i], inc);
           }
         }
         st<KV>(Tg, n * LZ + k, tnew);
+        if (RES) st<KV>(a.Tlo + gi * a.gT, n * LZ + k, tlnew);
         if (DEL) st<KV>(del, n * LZ + k, enew);
         if (a.TAout)
           st<KV>(a.TAout + gi * a.gTA, n * LZ + k, a.ab2 ? fmas(Tn[i], a.ab_old, muls(tnew, a.ab_new)) : tnew);
@@ -1626,7 +1644,8 @@ __global__ void __launch_bounds__(kVimplWarpsF * kW) kf_vert_impl(DMesh m, FastP
     for (int i = lane; i < nn * LZ; i += kW) {
       const int jj = i / LZ, k = i - jj * LZ;
       const unsigned iz = (unsigned)(n0 + jj) * LZ + k;
-      *reinterpret_cast<V<KV>*>(sY + k * S::RS + jj * KV) = muls(ld<KV>(lo, iz), g.hnode_new[iz]);
+      *reinterpret_cast<V<KV>*>(sY + k * S::RS + jj * KV) =
+          muls(add(ld<KV>(a.T + gi * a.gT, iz), ld<KV>(lo, iz)), g.hnode_new[iz]);  // hnode_new (T + (LO - T))
     }
     __syncwarp();
     if (own) {
@@ -1657,7 +1676,8 @@ __global__ void __launch_bounds__(kVimplWarpsF * kW) kf_vert_impl(DMesh m, FastP
     for (int i = lane; i < nn * LZ; i += kW) {
       const int jj = i / LZ, k = i - jj * LZ, n = n0 + jj;
       if (k >= m.ulev[n] - 1 && k <= m.nlev[n] - 2)
-        st<KV>(lo, (unsigned)n * LZ + k, *reinterpret_cast<const V<KV>*>(sY + k * S::RS + jj * KV));
+        st<KV>(lo, (unsigned)n * LZ + k,
+               sub(*reinterpret_cast<const V<KV>*>(sY + k * S::RS + jj * KV), ld<KV>(a.T + gi * a.gT, (unsigned)n * LZ + k)));
     }
   }
 }
@@ -1703,11 +1723,14 @@ __global__ void __launch_bounds__(256) kf_vert_pcr(DMesh m, FastPtrs a) {
     V<KV> dv[2];
 #pragma unroll
     for (int r = 0; r < 2; ++r)
-      dv[r] = act[r] ? muls(ld<KV>(lo, (unsigned)n * LZ + lane + kW * r), hn[r]) : splat<KV>(0.f);
+      dv[r] = act[r] ? muls(add(ld<KV>(a.T + gi * a.gT, (unsigned)n * LZ + lane + kW * r),
+                                ld<KV>(lo, (unsigned)n * LZ + lane + kW * r)), hn[r])
+                     : splat<KV>(0.f);  // hnode_new (T + (LO - T))
     pcr_solve2<KV>(av, bv, cv, dv, lane);
 #pragma unroll
     for (int r = 0; r < 2; ++r)
-      if (act[r]) st<KV>(lo, (unsigned)n * LZ + lane + kW * r, dv[r]);
+      if (act[r])
+        st<KV>(lo, (unsigned)n * LZ + lane + kW * r, sub(dv[r], ld<KV>(a.T + gi * a.gT, (unsigned)n * LZ + lane + kW * r)));
   }
 }
 

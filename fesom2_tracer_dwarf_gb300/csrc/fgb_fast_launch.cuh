@@ -77,20 +77,23 @@ void launch_ratio_f(const DMesh& m, const FastPtrs& a, int nw, cudaStream_t s) {
   else launch_ratio_fc<KV, NS, false>(m, a, nw, s);
 }
 
-template <int KV, int NS, bool DEL, bool COMP, int UE>
+template <int KV, int NS, bool DEL, bool COMP, bool RES>
 void launch_update_fc(const DMesh& m, const FastPtrs& a, int nw, cudaStream_t s) {
   const size_t sm = nw * warp_bytes<KV>(0, kUpdVec, m.LW);
-  allow_smem_f(kf_update<KV, NS, DEL, COMP, UE>, sm);
-  kf_update<KV, NS, DEL, COMP, UE><<<(m.N + nw - 1) / nw, nw * kW, sm, s>>>(m, a);
+  allow_smem_f(kf_update<KV, NS, DEL, COMP, RES>, sm);
+  kf_update<KV, NS, DEL, COMP, RES><<<(m.N + nw - 1) / nw, nw * kW, sm, s>>>(m, a);
 }
-template <int KV, int NS, int UE = 2>
+template <int KV, int NS>
 void launch_update_f(const DMesh& m, const FastPtrs& a, int nw, cudaStream_t s) {
-  if (a.del) {
-    if (a.comp) launch_update_fc<KV, NS, true, true, UE>(m, a, nw, s);
-    else launch_update_fc<KV, NS, true, false, UE>(m, a, nw, s);
+  if (a.del) {  // the reference C interface: a persistent del_ttf, no residual
+    if (a.comp) launch_update_fc<KV, NS, true, true, false>(m, a, nw, s);
+    else launch_update_fc<KV, NS, true, false, false>(m, a, nw, s);
+  } else if (a.Tlo) {
+    if (a.comp) launch_update_fc<KV, NS, false, true, true>(m, a, nw, s);
+    else launch_update_fc<KV, NS, false, false, true>(m, a, nw, s);
   } else {
-    if (a.comp) launch_update_fc<KV, NS, false, true, UE>(m, a, nw, s);
-    else launch_update_fc<KV, NS, false, false, UE>(m, a, nw, s);
+    if (a.comp) launch_update_fc<KV, NS, false, true, false>(m, a, nw, s);
+    else launch_update_fc<KV, NS, false, false, false>(m, a, nw, s);
   }
 }
 
@@ -189,10 +192,7 @@ int launch_fast(const DMesh& m, const FastPtrs& a, const LaunchArgs& L, cudaStre
       ++launches;
     }
     if (L.mask & FGB_STAGE_UPDATE) {
-      // 1: one layer per lane per pass, 2: two; 3 and 4: one, with 4 and 8 edges unrolled
       if (L.ns_upd == 2) launch_update_f<KV, 2>(m, a, L.nw_upd, s);
-      else if (L.ns_upd == 3) launch_update_f<KV, 1, 4>(m, a, L.nw_upd, s);
-      else if (L.ns_upd == 4) launch_update_f<KV, 1, 8>(m, a, L.nw_upd, s);
       else launch_update_f<KV, 1>(m, a, L.nw_upd, s);
       ++launches;
     }

@@ -11,7 +11,8 @@
 // value of an interface takes four reciprocals (the seven quotients of the
 // reference share denominators), a slope two, and the low-order factors
 // T hnode / hnode_new and dt / (areasvol hnode_new) one each. Stencils read
-// the column from shared memory, one round per phase.
+// the column from shared memory, one round per phase. The LO workspace holds
+// the increment LO - T (the FP32 form's convention, see kf_lo).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -276,8 +277,10 @@ __global__ void __launch_bounds__(kLo64Warps * kW, 7) kf_lo64(DMesh m, FastPtrs 
     for (int s = 0; s < 2; ++s) {
       if (!lay[s]) continue;
       const int z = k[s] + 1;
-      V<KV> l = COMP ? add(acc[s], accc[s]) : acc[s];
-      if (z >= nzmin && z <= nzmax - 1) l = fmas(add(l, sub(flo[s], sF[k[s] + 1])), rb[s], muls(t[s], ra[s]));
+      // the increment LO - T = (fluxes) dt / (areasvol hnode_new) + T (hnode / hnode_new - 1)
+      V<KV> l = splat<KV>(0.f);
+      if (z >= nzmin && z <= nzmax - 1)
+        l = fmas(add(COMP ? add(acc[s], accc[s]) : acc[s], sub(flo[s], sF[k[s] + 1])), rb[s], muls(t[s], ra[s] - 1.f));
       st<KV>(lo, (unsigned)n * LZ + k[s], l);
     }
   }

@@ -47,7 +47,7 @@ int launch_stages_f32(const DMesh& m, const fgb_step_desc& d, int mask, cudaStre
   }
   const uintptr_t al = 4u * KV;
   auto misaligned = [&](const void* p) { return p && (reinterpret_cast<uintptr_t>(p) % al) != 0; };
-  if (misaligned(d.T) || misaligned(d.TA) || misaligned(d.TAout) || misaligned(d.del) ||
+  if (misaligned(d.T) || misaligned(d.TA) || misaligned(d.TAout) || misaligned(d.del) || misaligned(d.Tlo) ||
       reinterpret_cast<uintptr_t>(d.vel) % 8 != 0 || d.strideT % KV != 0 || (d.TA && d.strideTA % KV != 0)) {
     *err = "FP32 tracer arrays must be aligned to their group (4 * tracer_vec bytes, strides multiples of tracer_vec)";
     return -1;
@@ -84,6 +84,7 @@ int launch_stages_f32(const DMesh& m, const fgb_step_desc& d, int mask, cudaStre
   a.pv = (float)d.pv;
   a.wsplit_fused = 0;  // set per launch of the LO kernel
   a.comp = d.fp32_plain_sums ? 0 : 1;
+  a.Tlo = d.del ? nullptr : static_cast<float*>(d.Tlo);
   a.ab2 = d.ab_order == 2;
   a.ab_old = (float)(-(0.5 + d.ab_eps));
   a.ab_new = (float)(1.5 + d.ab_eps);
@@ -102,8 +103,7 @@ int launch_stages_f32(const DMesh& m, const fgb_step_desc& d, int mask, cudaStre
   // ratio: 1 or 2 layers per lane with shared-memory staging, or 3 (the default)
   // the whole column per warp without shared memory
   L.ns_ratio = (d.cfg[5] >= 1 && d.cfg[5] <= 4) ? d.cfg[5] : 0;
-  // update: 1 or 2 layers per lane per pass; 3, 4: one layer, 4 or 8 edges unrolled
-  L.ns_upd = (d.cfg[6] >= 1 && d.cfg[6] <= 4) ? d.cfg[6] : 1;
+  L.ns_upd = ns(d.cfg[6], 1);
   L.vimpl_thomas = d.cfg[8] == 1;
   // the tiled edge kernel stages rows with 16-byte asynchronous copies
   auto al16 = [](const void* p) { return p == nullptr || reinterpret_cast<uintptr_t>(p) % 16 == 0; };

@@ -69,7 +69,7 @@ class TracerAdvection:
     def __init__(self, mesh: Mesh, ntracers: int, precision: str = "fp64", hor: str = "UPW1",
                  ver: str = "UPW1", lim: str = "NONE", ph: float = 1.0, pv: float = 1.0,
                  copy_ab: bool = False, device: str = "cuda", tracer_vec: int | None = None,
-                 ab2_eps: float | None = None, offsets=None, plain_sums: bool = False):
+                 ab2_eps: float | None = None, offsets=None, plain_sums: bool = False, residual: bool = False):
         _require_cuda()
         if ab2_eps is not None and copy_ab:
             raise ValueError("copy_ab and ab2_eps are two choices of the valuesAB time level; give one")
@@ -89,6 +89,8 @@ class TracerAdvection:
         self.ab2_eps = None if ab2_eps is None else float(ab2_eps)
         # FP32 form: plain FP32 sums instead of the compensated flux-divergence and FCT +/- sums
         self.plain_sums = bool(plain_sums)
+        # FP32 form with the FCT limiter: each value carries its FP32 rounding residual (self.Tlo)
+        self.residual = bool(residual) and precision == "fp32" and lim == "FCT"
         if isinstance(offsets, str):
             if offsets not in ("mean", "auto"):
                 raise ValueError('offsets must be None, "mean", "auto" or one value per tracer')
@@ -100,6 +102,7 @@ class TracerAdvection:
         m.upload()
         z = lambda *s: torch.zeros(*s, dtype=self.dtype, device=self.device)
         self.T = z(*self.layout_shape)
+        self.Tlo = z(*self.layout_shape) if self.residual else None
         self.TA = None if copy_ab else z(*self.layout_shape)
         self.vel = z(m.M, m.LZ, 2)
         self.w = z(m.N, m.LW)
@@ -115,6 +118,13 @@ class TracerAdvection:
         self._stats_out = torch.zeros(self.K, 4, dtype=torch.float64, device=self.device)
         self.launches = 0
         self.cfg = [0] * _lib.NCFG  # launch configuration, see set_launch
+
+    def set_residual(self, on: bool):
+        """FP32 form with the FCT limiter: keep (allocate, zero) or drop the
+        per-value rounding residual. Set the tracers afterwards to fill it."""
+        on = bool(on) and self.precision == "fp32" and self.lim == "FCT"
+        self.residual = on
+        self.Tlo = torch.zeros_like(self.T) if on else None
 
     def set_launch(self, cfg):
         """Launch configuration (fgb_step_desc.cfg): a list of up to 12 ints or a
@@ -172,13 +182,16 @@ class TracerAdvection:
         else:
             self.offsets = req
 
-    def _shifted(self, vals, ld):
-        """(K, N, nz) float64 values -> (K, N, ld) engine dtype on the host, minus the offsets."""
+    def _shifted(self, vals, ld, residual=False):
+        """(K, N, nz) float64 values -> (K, N, ld) engine dtype on the host, minus the offsets
+        (residual=True: the remainder those values leave after rounding to the engine dtype)."""
         m = self.mesh
         t = torch.as_tensor(np.asarray(vals) if not torch.is_tensor(vals) else vals.cpu(), dtype=torch.float64)
         t = t.reshape(self.K, m.N, -1)
         if self.offsets is not None:
             t = t - torch.as_tensor(self.offsets, dtype=torch.float64)[:, None, None]
+        if residual:
+            t = t - t.to(self.dtype).double()
         out = torch.zeros(self.K, m.N, ld, dtype=self.dtype)
         out[..., : t.shape[-1]] = t.to(self.dtype)
         return out.to(self.device)
@@ -189,6 +202,8 @@ class TracerAdvection:
         self._resolve_offsets(values if torch.is_tensor(values) else np.asarray(values, dtype=np.float64))
         v = self.to_layout(self._shifted(values, m.LZ))
         self.T.copy_(v)
+        if self.Tlo is not None:
+            self.Tlo.copy_(self.to_layout(self._shifted(values, m.LZ, residual=True)))
         if self.TA is not None:
             self.TA.copy_(self.to_layout(self._shifted(values_ab, m.LZ)) if values_ab is not None else v)
 
@@ -219,6 +234,8 @@ class TracerAdvection:
             if self.offsets is not None:
                 T = T.double() - torch.as_tensor(self.offsets, device=T.device)[:, None, None]
             self.T.copy_(self.to_layout(T.to(self.dtype)))
+            if self.Tlo is not None:  # the remainder of wider values after rounding (0 for FP32 input)
+                self.Tlo.copy_(self.to_layout((T.double() - T.to(self.dtype).double()).to(self.dtype)))
         if TA is not None and self.TA is not None:
             if self.offsets is not None:
                 TA = TA.double() - torch.as_tensor(self.offsets, device=TA.device)[:, None, None]
@@ -257,6 +274,7 @@ class TracerAdvection:
         d.workspace = self.workspace.data_ptr()
         d.workspace_bytes = self.workspace.numel()
         d.fp32_plain_sums = int(self.plain_sums)
+        d.Tlo = None if self.Tlo is None else self.Tlo.data_ptr()
         for i, c in enumerate(self.cfg):
             d.cfg[i] = c
         return d
@@ -287,6 +305,8 @@ class TracerAdvection:
         before reading ``host_out``."""
         if self.TA is not None:
             raise ValueError("run_host needs copy_ab=True (valuesAB follows the values)")
+        # host batches are FP32 values stepped from the host: they carry no rounding residual
+        saved_tlo, self.Tlo = self.Tlo, None
         nb = len(host_in)
         if len(host_out) != nb:
             raise ValueError("host_in and host_out need one tensor per batch")
@@ -339,6 +359,7 @@ class TracerAdvection:
         for b in range(3):
             for c in range(nc):
                 main.wait_event(free[b][c])
+        self.Tlo = saved_tlo
         return host_out
 
     def capture(self, dt: float, nsteps: int = 1):
@@ -356,18 +377,33 @@ class TracerAdvection:
         return g
 
     # ---- outputs -----------------------------------------------------------
+    def full_values(self):
+        """(K, N, LZ) float64 tensor on the device: the stored values plus the
+        rounding residuals (residual=True) plus the anomaly offsets."""
+        v = self.from_layout(self.T).double()
+        if self.Tlo is not None:
+            v = v + self.from_layout(self.Tlo).double()
+        if self.offsets is not None:
+            v = v + torch.as_tensor(self.offsets, device=v.device)[:, None, None]
+        return v
+
     def values(self) -> np.ndarray:
         """(K, N, nz) tracer values as float64."""
-        m = self.mesh
-        v = self.from_layout(self.T)[:, :, : m.nz].double().cpu().numpy()
-        if self.offsets is not None:
-            v += self.offsets[:, None, None]
-        return v
+        return self.full_values()[:, :, : self.mesh.nz].cpu().numpy()
 
     def workspace_view(self, name: str):
         """One workspace array per tracer: vf (E,LZ), adfh (K,E,LZ), lo (K,N,LZ),
         adfv (K,N,LW), rp / rm (K,N,LZ). Views of the workspace in the FP64
-        form; copies when the FP32 form groups tracers."""
+        form; copies when the FP32 form groups tracers. The FP32 form stores the
+        low-order solution as its increment LO - T: "lo" adds the current T back
+        (read it before the update stage changes T), "lo_increment" is the
+        stored increment."""
+        if name == "lo" and self.precision == "fp32":
+            return self.workspace_view("lo_increment") + self.from_layout(self.T)
+        if name == "lo_increment":
+            if self.precision != "fp32":
+                raise ValueError("only the FP32 form stores the LO increment")
+            name = "lo"
         m = self.mesh
         L = _lib.load()
         offs = (ctypes.c_longlong * 7)()

@@ -262,6 +262,13 @@ typedef struct {
    * so that the edge fluxes cancel between neighbouring nodes to the last bit
    * of the sum; 1 plain FP32 sums. The FP64 form ignores it. */
   int fp32_plain_sums;
+  /* FP32 form, optional (NULL: off): the rounding residual of every tracer
+   * value, an array of T's layout and strideT. The value of a cell is
+   * T + Tlo; the update stage forms T + Tlo + increment and stores its FP32
+   * rounding in T and the (exact) remainder in Tlo, so that increments below
+   * half an FP32 unit of T are kept. Ignored with del (the reference C
+   * interface's persistent del_ttf) and by the FP64 forms. */
+  void* Tlo;
 } fgb_step_desc;
 
 /* Full step: vflux, hflux, and the FCT (lo, ratio, update) or plain update. */

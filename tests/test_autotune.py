@@ -25,7 +25,7 @@ def test_candidates_cover_allowed_values():
     lo32 = autotune.stage_candidates("lo", 4, "fp32")
     lo32s = autotune.stage_candidates("lo", 4, "fp32", wsplit=True)
     # the whole-column LO kernel is a candidate only without w_split
-    assert {1: 0, 4: 3} in lo32 and all(c.get(4) != 3 for c in lo32s)
+    assert {1: 4, 4: 3} in lo32 and all(c.get(4) != 3 for c in lo32s)
     assert len(lo32s) == 2 * (len(lo32) - 1) and {1: 2, 4: 1, 8: 1} in lo32s and {1: 2, 4: 1, 8: 0} in lo32s
 
 
