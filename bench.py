@@ -390,7 +390,12 @@ def build_case(cfg, precision, device, seed=20260301):
     return m, eng, eng.T.clone()
 
 
-def precision_report(m, e32, T32, e64, T64, dt, steps):
+REPORT_VARIANTS = (("residual", False, True, None), ("residual_plain_sums", True, True, None),
+                   ("compensated", False, False, None), ("plain_sums", True, False, None),
+                   ("anomaly", False, False, "auto"))
+
+
+def precision_report(m, e32, T32, e64, T64, dt, steps, variants=REPORT_VARIANTS):
     """The FP32 form against the plain FP64 form from the same initial values
     after `steps` steps. Per tracer: the max-norm error relative to max |T|,
     the relative change of the volume integral sum(T hnode_new areasvol) --
@@ -435,9 +440,6 @@ def precision_report(m, e32, T32, e64, T64, dt, steps):
                                     "violations": [extrema(b[t], t)[0] for t in range(K)],
                                     "max_excursion": [extrema(b[t], t)[1] for t in range(K)]}}
     plain0, req0, res0 = e32.plain_sums, e32._offsets_req, e32.residual
-    variants = (("residual", False, True, None), ("residual_plain_sums", True, True, None),
-                ("compensated", False, False, None), ("plain_sums", True, False, None),
-                ("anomaly", False, False, "auto"))
     for name, plain, res, offs in variants:
         e32.plain_sums = plain
         e32.set_residual(res)
@@ -463,7 +465,7 @@ def precision_report(m, e32, T32, e64, T64, dt, steps):
     if e32.Tlo is not None:
         e32.load_padded(T=e64.from_layout(T64).clone())
     # the timed form's figures under the keys of earlier reports
-    timed = "residual" if res0 else "compensated"
+    timed = variants[0][0] if res0 else "compensated"
     out["timed_form"] = timed
     out["max_rel_err"] = out[timed]["max_rel_err"]
     out["sum_rel_err_fp32"] = out[timed]["sum_rel_err"]
@@ -835,11 +837,16 @@ def run_profile(args):
     m, eng, _ = build_case(cfg, args.precision or cfg["precision"], "cuda:0")
     if args.launch_cfg:
         eng.set_launch([int(x) for x in args.launch_cfg.split(",")])
+    if args.plain_sums is not None:
+        eng.plain_sums = int(args.plain_sums)
+    if args.residual is not None:
+        eng.set_residual(bool(args.residual))
     torch.cuda.synchronize()
     eng.step(cfg["dt"], args.profile)
     torch.cuda.synchronize()
     print(json.dumps({"workload": args.workload, "form": eng.precision, "steps": args.profile,
-                      "launch_cfg": eng.cfg, "launches": eng.launches}))
+                      "launch_cfg": eng.cfg, "plain_sums": eng.plain_sums, "residual": eng.residual,
+                      "launches": eng.launches}))
 
 
 def main():
@@ -861,6 +868,9 @@ def main():
                     help="with --profile: the form to run (default: the workload's)")
     ap.add_argument("--launch-cfg", default=None,
                     help="with --profile: launch configuration, comma-separated (default: the library's)")
+    ap.add_argument("--plain-sums", type=int, default=None,
+                    help="with --profile: FP32 plain-sum bit mask (1 LO, 2 update, 4 FCT sums; default 0)")
+    ap.add_argument("--residual", type=int, default=None, help="with --profile: 1 keeps the FP32 rounding residual")
     args = ap.parse_args()
     if args.profile:
         run_profile(args)

@@ -122,7 +122,7 @@ struct FastPtrs {
   int ab2;  // TAout = ab_old * T_old + ab_new * T_new (else T_new)
   float ab_old, ab_new;
   int wsplit_fused;  // w_split: the LO kernel also solves the implicit vertical step
-  int comp;          // compensated flux-divergence and FCT +/- sums (fgb_step_desc.fp32_plain_sums == 0)
+  int comp;          // compensated sums: bit 1 LO fluxes, 2 update divergence, 4 FCT +/- sums (~fp32_plain_sums)
   float* Tlo;        // optional (G,N,LZ,KV), stride gT: the rounding residual of each value of T
 };
 

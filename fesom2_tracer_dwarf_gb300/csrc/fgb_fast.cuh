@@ -192,24 +192,43 @@ static __global__ void __launch_bounds__(256) kf_vflux(DMesh m, const float* __r
   }
   const unsigned LZ = m.LZ;
   const float2* __restrict__ uv = reinterpret_cast<const float2*>(vel);
-  for (int i = 0; i < cnt; ++i) {
-    const int ei = __shfl_sync(0xffffffffu, e, i);
-    const int e1 = __shfl_sync(0xffffffffu, el1, i), e2 = __shfl_sync(0xffffffffu, el2, i);
-    const int l1 = __shfl_sync(0xffffffffu, nl1, i), l2 = __shfl_sync(0xffffffffu, nl2, i);
-    const float dX1 = __shfl_sync(0xffffffffu, cr.x, i), dY1 = __shfl_sync(0xffffffffu, cr.y, i);
-    const float dX2 = __shfl_sync(0xffffffffu, cr.z, i), dY2 = __shfl_sync(0xffffffffu, cr.w, i);
+  // two edges per round: the element loads of both are in flight together
+  for (int i0 = 0; i0 < cnt; i0 += 2) {
+    const int i1 = min(i0 + 1, cnt - 1);  // a repeat of the last edge when cnt is odd (same value stored)
+    int ei[2], e1[2], e2[2], l1[2], l2[2];
+    float dX1[2], dY1[2], dX2[2], dY2[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int i = q ? i1 : i0;
+      ei[q] = __shfl_sync(0xffffffffu, e, i);
+      e1[q] = __shfl_sync(0xffffffffu, el1, i);
+      e2[q] = __shfl_sync(0xffffffffu, el2, i);
+      l1[q] = __shfl_sync(0xffffffffu, nl1, i);
+      l2[q] = __shfl_sync(0xffffffffu, nl2, i);
+      dX1[q] = __shfl_sync(0xffffffffu, cr.x, i);
+      dY1[q] = __shfl_sync(0xffffffffu, cr.y, i);
+      dX2[q] = __shfl_sync(0xffffffffu, cr.z, i);
+      dY2[q] = __shfl_sync(0xffffffffu, cr.w, i);
+    }
     for (unsigned k = lane; k < LZ; k += kW) {
       const int z = (int)k + 1;
-      float v = 0.f;
-      if (z <= l1) {
-        const float2 u = uv[e1 * LZ + k];
-        v = (-(u.y * dX1) + u.x * dY1) * g.helem[e1 * LZ + k];
+      float2 u1[2], u2[2];
+      float h1[2], h2[2];
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const bool a1 = z <= l1[q], a2 = z <= l2[q];
+        u1[q] = a1 ? uv[e1[q] * LZ + k] : make_float2(0.f, 0.f);
+        h1[q] = a1 ? g.helem[e1[q] * LZ + k] : 0.f;
+        u2[q] = a2 ? uv[e2[q] * LZ + k] : make_float2(0.f, 0.f);
+        h2[q] = a2 ? g.helem[e2[q] * LZ + k] : 0.f;
       }
-      if (z <= l2) {
-        const float2 u = uv[e2 * LZ + k];
-        v = v + (u.y * dX2 - u.x * dY2) * g.helem[e2 * LZ + k];
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        float v = 0.f;
+        if (z <= l1[q]) v = (-(u1[q].y * dX1[q]) + u1[q].x * dY1[q]) * h1[q];
+        if (z <= l2[q]) v = v + (u2[q].y * dX2[q] - u2[q].x * dY2[q]) * h2[q];
+        vf[ei[q] * LZ + k] = v;
       }
-      vf[ei * LZ + k] = v;
     }
   }
 }

@@ -73,7 +73,7 @@ void launch_ratio_fc(const DMesh& m, const FastPtrs& a, int nw, cudaStream_t s) 
 }
 template <int KV, int NS>
 void launch_ratio_f(const DMesh& m, const FastPtrs& a, int nw, cudaStream_t s) {
-  if (a.comp) launch_ratio_fc<KV, NS, true>(m, a, nw, s);
+  if (a.comp & 4) launch_ratio_fc<KV, NS, true>(m, a, nw, s);
   else launch_ratio_fc<KV, NS, false>(m, a, nw, s);
 }
 
@@ -86,13 +86,13 @@ void launch_update_fc(const DMesh& m, const FastPtrs& a, int nw, cudaStream_t s)
 template <int KV, int NS>
 void launch_update_f(const DMesh& m, const FastPtrs& a, int nw, cudaStream_t s) {
   if (a.del) {  // the reference C interface: a persistent del_ttf, no residual
-    if (a.comp) launch_update_fc<KV, NS, true, true, false>(m, a, nw, s);
+    if (a.comp & 2) launch_update_fc<KV, NS, true, true, false>(m, a, nw, s);
     else launch_update_fc<KV, NS, true, false, false>(m, a, nw, s);
   } else if (a.Tlo) {
-    if (a.comp) launch_update_fc<KV, NS, false, true, true>(m, a, nw, s);
+    if (a.comp & 2) launch_update_fc<KV, NS, false, true, true>(m, a, nw, s);
     else launch_update_fc<KV, NS, false, false, true>(m, a, nw, s);
   } else {
-    if (a.comp) launch_update_fc<KV, NS, false, true, false>(m, a, nw, s);
+    if (a.comp & 2) launch_update_fc<KV, NS, false, true, false>(m, a, nw, s);
     else launch_update_fc<KV, NS, false, false, false>(m, a, nw, s);
   }
 }
@@ -101,7 +101,7 @@ template <int KV, bool LEAN>
 void launch_ratio64(const DMesh& m, const FastPtrs& a, int nw, cudaStream_t s) {
   const unsigned grid = (m.N + nw - 1) / nw;
   const size_t sm = nw * ratio64_warp_bytes(KV);
-  if (a.comp) kf_ratio64<KV, LEAN, true><<<grid, nw * kW, sm, s>>>(m, a);
+  if (a.comp & 4) kf_ratio64<KV, LEAN, true><<<grid, nw * kW, sm, s>>>(m, a);
   else kf_ratio64<KV, LEAN, false><<<grid, nw * kW, sm, s>>>(m, a);
 }
 
@@ -113,7 +113,7 @@ void launch_lo64c(const DMesh& m, const FastPtrs& a, cudaStream_t s) {
 }
 template <int KV, int VER, bool TASEP, bool WESEP>
 void launch_lo64(const DMesh& m, const FastPtrs& a, cudaStream_t s) {
-  if (a.comp) launch_lo64c<KV, VER, TASEP, WESEP, true>(m, a, s);
+  if (a.comp & 1) launch_lo64c<KV, VER, TASEP, WESEP, true>(m, a, s);
   else launch_lo64c<KV, VER, TASEP, WESEP, false>(m, a, s);
 }
 

@@ -83,7 +83,7 @@ int launch_stages_f32(const DMesh& m, const fgb_step_desc& d, int mask, cudaStre
   a.ph = (float)d.ph;
   a.pv = (float)d.pv;
   a.wsplit_fused = 0;  // set per launch of the LO kernel
-  a.comp = d.fp32_plain_sums ? 0 : 1;
+  a.comp = ~d.fp32_plain_sums & 7;
   a.Tlo = d.del ? nullptr : static_cast<float*>(d.Tlo);
   a.ab2 = d.ab_order == 2;
   a.ab_old = (float)(-(0.5 + d.ab_eps));

@@ -87,8 +87,9 @@ class TracerAdvection:
         self.set_schemes(hor, ver, lim, ph, pv)
         self.copy_ab = copy_ab
         self.ab2_eps = None if ab2_eps is None else float(ab2_eps)
-        # FP32 form: plain FP32 sums instead of the compensated flux-divergence and FCT +/- sums
-        self.plain_sums = bool(plain_sums)
+        # FP32 form: plain FP32 sums instead of compensated ones (fgb_step_desc.fp32_plain_sums:
+        # True = all, False = none, or the bit mask 1 LO fluxes, 2 update divergence, 4 FCT +/- sums)
+        self.plain_sums = plain_sums
         # FP32 form with the FCT limiter: each value carries its FP32 rounding residual (self.Tlo)
         self.residual = bool(residual) and precision == "fp32" and lim == "FCT"
         if isinstance(offsets, str):
@@ -273,7 +274,8 @@ class TracerAdvection:
         d.del_ = None
         d.workspace = self.workspace.data_ptr()
         d.workspace_bytes = self.workspace.numel()
-        d.fp32_plain_sums = int(self.plain_sums)
+        ps = self.plain_sums
+        d.fp32_plain_sums = 7 if ps is True else (0 if ps is False or ps is None else int(ps))
         d.Tlo = None if self.Tlo is None else self.Tlo.data_ptr()
         for i, c in enumerate(self.cfg):
             d.cfg[i] = c

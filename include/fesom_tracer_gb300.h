@@ -256,11 +256,14 @@ typedef struct {
    * runs after every stage that reads TA. */
   int ab_order;
   double ab_eps;
-  /* FP32 form: 0 (default) forms the flux divergence of the update and the
-   * FCT +/- sums of the limiter as compensated sums (FP32 pairs with
-   * error-free additions, the same rounded product at both ends of an edge),
-   * so that the edge fluxes cancel between neighbouring nodes to the last bit
-   * of the sum; 1 plain FP32 sums. The FP64 form ignores it. */
+  /* FP32 form: which sums are plain FP32 sums instead of compensated ones
+   * (FP32 pairs with error-free additions, of one rounded product per edge
+   * that is the same number at both ends, so the edge fluxes cancel between
+   * neighbouring nodes to the last bit of the sum). Bit mask, 0 (default): all
+   * compensated. 1: the low-order fluxes of the LO stage; 2: the flux
+   * divergence of the update; 4: the FCT +/- sums of the limiter (these only
+   * scale each edge's flux, the same factor at both ends, so they never
+   * affect conservation); 7: all plain. The FP64 forms ignore it. */
   int fp32_plain_sums;
   /* FP32 form, optional (NULL: off): the rounding residual of every tracer
    * value, an array of T's layout and strideT. The value of a cell is
