@@ -1155,13 +1155,18 @@ __global__ void __launch_bounds__(128, LEAN ? 8 : 7) kf_ratio64(DMesh m, FastPtr
   const int c0 = m.cl_ptr[n], ncl = m.cl_ptr[n + 1] - c0, minlev = m.cl_minlev[n];
   const int nzmin = m.ulev[n], nzmax = m.nlev[n];
   const float dt = a.dt;
+  // layers 32..63 are gathered only when the column reaches them; otherwise
+  // their limiting factors are stored as zeros (neighbours read them)
+  const bool s1 = nzmax - 2 >= kW;
   unsigned kk[2];
   int z[2];
+  bool live[2];
 #pragma unroll
   for (int i = 0; i < 2; ++i) {
     const unsigned k = lane + kW * i;
     kk[i] = k < LZ ? k : LZ - 1;
     z[i] = (int)k + 1;
+    live[i] = i == 0 || s1;
   }
   for (int gi = 0; gi < a.G; ++gi) {
     const float* __restrict__ Tg = a.T + gi * a.gT;
@@ -1176,7 +1181,7 @@ __global__ void __launch_bounds__(128, LEAN ? 8 : 7) kf_ratio64(DMesh m, FastPtr
       const float m0 = z[i] > minlev ? -1e3f : -INFINITY;
       mx[i] = splat<KV>(m0);
       mn[i] = splat<KV>(-m0);
-      lo[i] = add(ld<KV>(Tg, n * LZ + kk[i]), ld<KV>(Lg, n * LZ + kk[i]));  // LO = T + (LO - T)
+      lo[i] = live[i] ? add(ld<KV>(Tg, n * LZ + kk[i]), ld<KV>(Lg, n * LZ + kk[i])) : splat<KV>(0.f);  // LO = T + (LO - T)
     }
 #pragma unroll(LEAN ? 1 : 2)
     for (int j = 0; j < ncl; ++j) {
@@ -1184,8 +1189,8 @@ __global__ void __launch_bounds__(128, LEAN ? 8 : 7) kf_ratio64(DMesh m, FastPtr
       V<KV> lv[2], tv[2];
 #pragma unroll
       for (int i = 0; i < 2; ++i) {
-        tv[i] = ld<KV>(Tg, c * LZ + kk[i]);
-        lv[i] = add(tv[i], ld<KV>(Lg, c * LZ + kk[i]));
+        tv[i] = live[i] ? ld<KV>(Tg, c * LZ + kk[i]) : splat<KV>(0.f);
+        lv[i] = live[i] ? add(tv[i], ld<KV>(Lg, c * LZ + kk[i])) : tv[i];
       }
 #pragma unroll
       for (int i = 0; i < 2; ++i)
@@ -1232,7 +1237,8 @@ __global__ void __launch_bounds__(128, LEAN ? 8 : 7) kf_ratio64(DMesh m, FastPtr
     V<KV> pl[2], mi[2], plc[2], mic[2];
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
-      const V<KV> ad0 = ld<KV>(adfv, n * LW + kk[i]), ad1 = ld<KV>(adfv, n * LW + kk[i] + 1);
+      const V<KV> ad0 = live[i] ? ld<KV>(adfv, n * LW + kk[i]) : splat<KV>(0.f);
+      const V<KV> ad1 = live[i] ? ld<KV>(adfv, n * LW + kk[i] + 1) : splat<KV>(0.f);
 #pragma unroll
       for (int t = 0; t < KV; ++t) {
         pl[i].v[t] = fmaxf(0.f, ad0.v[t]) + fmaxf(0.f, -ad1.v[t]);
@@ -1248,7 +1254,7 @@ __global__ void __launch_bounds__(128, LEAN ? 8 : 7) kf_ratio64(DMesh m, FastPtr
       const float sg = (code & 1) ? -1.f : 1.f;
       V<KV> f[2];
 #pragma unroll
-      for (int i = 0; i < 2; ++i) f[i] = ld<KV>(Fg, ed * LZ + kk[i]);
+      for (int i = 0; i < 2; ++i) f[i] = live[i] ? ld<KV>(Fg, ed * LZ + kk[i]) : splat<KV>(0.f);
 #pragma unroll
       for (int i = 0; i < 2; ++i) {
         if (COMP) {
@@ -1397,9 +1403,10 @@ __global__ void __launch_bounds__(128, (NS == 1 ? (COMP || RES ? 8 : 9) : 4)) kf
       for (int c = 0; c < 3; ++c) {
         const int k = c0 + lane + kW * c;
         const int kr = k < nz ? k : nz - 1, kv = k < nl ? k : nl - 1;
-        rp[c] = ld<KV>(Rg, 2 * (n * LZ + kr));
-        rm[c] = ld<KV>(Rg, 2 * (n * LZ + kr) + 1);
-        fv[c] = ld<KV>(adfv, n * LW + kv);
+        const bool need = k <= nzmax - 1;  // layers and interfaces of the column (to its bottom)
+        rp[c] = need ? ld<KV>(Rg, 2 * (n * LZ + kr)) : splat<KV>(0.f);
+        rm[c] = need ? ld<KV>(Rg, 2 * (n * LZ + kr) + 1) : splat<KV>(0.f);
+        fv[c] = need ? ld<KV>(adfv, n * LW + kv) : splat<KV>(0.f);
       }
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
@@ -1426,7 +1433,9 @@ __global__ void __launch_bounds__(128, (NS == 1 ? (COMP || RES ? 8 : 9) : 4)) kf
     const float* __restrict__ Lg = a.lo + gi * a.gN;
     float* __restrict__ Tg = a.T + gi * a.gT;
     float* del = DEL ? a.del + gi * a.gN : nullptr;
-    for (unsigned base = 0; base < LZ; base += kW * NS) {
+    // passes below the column's deepest layer change nothing: skipped
+    const unsigned lz_col = min(LZ, (unsigned)max(nzmax - 1, 1));
+    for (unsigned base = 0; base < lz_col; base += kW * NS) {
       unsigned kk[NS];
       V<KV> dh[NS], dc[NS], rpn[NS], rmn[NS], lo[NS], Tn[NS], d0[NS], tl[NS];
       float av[NS], hnn[NS], hn[NS];

@@ -58,6 +58,11 @@ __global__ void __launch_bounds__(kLo64Warps * kW, 7) kf_lo64(DMesh m, FastPtrs 
   const bool nb_staged = deg <= kMaxDegF;
   if (nb_staged && lane < deg) sNb[lane] = make_int2(m.ne_code[e0 + lane], m.ne_other[e0 + lane]);
   const float dt = a.dt;
+  // The second slice (layers 32..63) is skipped when the column ends above it
+  // (its deepest layer, 0-based nzmax - 2, is above layer 32): no loads, no
+  // arithmetic; its interface fluxes are zero (still written: the bottom
+  // interface is read by the update) and its LO increments are never read.
+  const bool s1 = nzmax - 2 >= kW;
   // per slice: layer / interface index, geometry and velocity (tracer independent)
   int k[2];
   bool lay[2], itf[2];
@@ -65,8 +70,8 @@ __global__ void __launch_bounds__(kLo64Warps * kW, 7) kf_lo64(DMesh m, FastPtrs 
 #pragma unroll
   for (int s = 0; s < 2; ++s) {
     k[s] = lane + kW * s;
-    lay[s] = k[s] < LZ;
-    itf[s] = k[s] < LW;
+    lay[s] = k[s] < LZ && (s == 0 || s1);
+    itf[s] = k[s] < LW && (s == 0 || s1);
     const unsigned iz = (unsigned)n * LZ + k[s], iw = (unsigned)n * LW + k[s];
     hn[s] = lay[s] ? g.hnode[iz] : 1.f;
     hnn[s] = lay[s] ? g.hnode_new[iz] : 1.f;
@@ -257,8 +262,8 @@ __global__ void __launch_bounds__(kLo64Warps * kW, 7) kf_lo64(DMesh m, FastPtrs 
       V<KV> to[2];
 #pragma unroll
       for (int s = 0; s < 2; ++s) {
-        v[s] = a.vf[ed * LZ + kc[s]];
-        to[s] = ld<KV>(Tg, (unsigned)q.y * LZ + kc[s]);
+        v[s] = lay[s] ? a.vf[ed * LZ + kc[s]] : 0.f;
+        to[s] = lay[s] ? ld<KV>(Tg, (unsigned)q.y * LZ + kc[s]) : splat<KV>(0.f);
       }
 #pragma unroll
       for (int s = 0; s < 2; ++s) {

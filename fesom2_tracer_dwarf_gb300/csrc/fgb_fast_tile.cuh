@@ -54,9 +54,13 @@ __global__ void __launch_bounds__(kTileThreads) kf_hflux_tile(DMesh m, FastPtrs 
   const int t = blockIdx.x;
   const int p0 = m.tile_ptr[t], ne = m.tile_ptr[t + 1] - p0;
   const int q0 = m.tile_nptr[t], nn = m.tile_nptr[t + 1] - q0;
+  __shared__ int s_hi;  // the deepest layer of the tile's edges
+  if (tid == 0) s_hi = 0;
+  __syncthreads();
   for (int i = tid; i < ne; i += kTileThreads) {
     fill_edge<HOR>(m, p0 + i, recs[i]);
     *reinterpret_cast<uint2*>(slots + 8 * i) = *reinterpret_cast<const uint2*>(m.tile_slots + 8 * (size_t)(p0 + i));
+    atomicMax(&s_hi, recs[i].hi);
   }
   for (int i = tid; i < nn; i += kTileThreads) nodes[i] = m.tile_nodes[q0 + i];
   const unsigned LZ = m.LZ;
@@ -69,6 +73,12 @@ __global__ void __launch_bounds__(kTileThreads) kf_hflux_tile(DMesh m, FastPtrs 
     for (unsigned k0 = 0; k0 < LZ; k0 += kTileChunk) {
       const int rows = (int)min((unsigned)kTileChunk, LZ - k0);
       __syncthreads();  // the previous pass has read the rows (first pass: records filled)
+      if ((int)k0 >= s_hi) {
+        // below every edge of the tile: the fluxes are zero (the node kernels read them)
+        if (lane < rows)
+          for (int j = warp; j < ne; j += kTileThreads / kW) st<KV>(out, (unsigned)recs[j].e * LZ + k0 + lane, splat<KV>(0.f));
+        continue;
+      }
       // Stage the pass with 16-byte asynchronous copies: a node's rows of the
       // pass are rows * KV floats from (node * LZ + k0) * KV, a multiple of 16
       // bytes from a 16-byte boundary (LZ, k0 and rows are multiples of 4).
