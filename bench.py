@@ -465,7 +465,8 @@ def precision_report(m, e32, T32, e64, T64, dt, steps, variants=REPORT_VARIANTS)
     if e32.Tlo is not None:
         e32.load_padded(T=e64.from_layout(T64).clone())
     # the timed form's figures under the keys of earlier reports
-    timed = variants[0][0] if res0 else "compensated"
+    # the variant the engine itself runs (its sums and residual), else the first
+    timed = next((v[0] for v in variants if (v[1] is plain0 or v[1] == plain0) and v[2] == res0), variants[0][0])
     out["timed_form"] = timed
     out["max_rel_err"] = out[timed]["max_rel_err"]
     out["sum_rel_err_fp32"] = out[timed]["sum_rel_err"]
