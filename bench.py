@@ -3,10 +3,14 @@
 
 Default workload: the precision form at scale -- 2048x2048 nodes doubly
 periodic (dx = 1 km), 64 layers stretched 5 m -> 250 m, 4 tracers (T, S, two
-passive blobs), MUSCL horizontal + PPM vertical + FCT, FP32 form; the plain
-FP64 path is timed on the same workload beside it. A step is one
-do_oce_adv_tra for every tracer plus the tendency update, inputs resident in
-HBM (they are far larger than the 129 MB L2, so no flush is needed).
+passive blobs), MUSCL horizontal + PPM vertical + FCT, FP32 form with each
+value's FP32 rounding residual carried by the update; the plain FP64 path
+(fast and bit-exact forms) is timed on the same workload beside it, and a
+100-step FP32-vs-FP64 precision report follows. A step is one do_oce_adv_tra
+for every tracer plus the tendency update, inputs resident in HBM (they are
+far larger than the 129 MB L2, so no flush is needed). The batching form
+(batch_16: 16 meshes in one union, CUDA graphs of 50 steps, against per-mesh
+sequential FP64 steps) is the line's second figure, under "batch_16".
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME]
   python bench.py --impl reference ...   # the CPU implementation of the path
@@ -38,8 +42,11 @@ UNIT = "tracer-cell updates/s"
 
 WORKLOADS = {
     # The precision form at scale: 2048^2 x 64 doubly periodic, 4 tracers (default).
+    # The FP32 form with each value's rounding residual (the precision form that meets the
+    # conservation target) and the LO fluxes summed with compensation.
     "precision_2048": dict(kind="flat", nx=2049, L=2048e3, nz=64, K=4, hor="MUSCL", ver="PPM", lim="FCT",
-                           dt=400.0, precision="fp32", compare_fp64=True, report_steps=100),
+                           dt=400.0, precision="fp32", compare_fp64=True, report_steps=100, residual=True,
+                           batch="batch_16"),
     # The default workload with w_split: w = we + wi, we clipped at a quarter of
     # max |w|; the LO stage adds the implicit vertical solve with wi.
     "wsplit_2048": dict(kind="flat", nx=2049, L=2048e3, nz=64, K=4, hor="MUSCL", ver="PPM", lim="FCT",
@@ -167,7 +174,7 @@ class ClockSampler:
 # library's kernels as written below; intermediates the kernels add (the
 # edge volume fluxes, repeated geometry reads) are not algorithmic.
 # ---------------------------------------------------------------------------
-def stage_bytes(m, K, s, ver, fct=True, copy_ab=True, wsplit=False):
+def stage_bytes(m, K, s, ver, fct=True, copy_ab=True, wsplit=False, residual=False):
     cells = m.N * m.nz  # node-layers; x K tracer-cells
     ta = 0 if copy_ab else 1
     e = 3
@@ -180,6 +187,8 @@ def stage_bytes(m, K, s, ver, fct=True, copy_ab=True, wsplit=False):
             b["lo"] += cells * s * 2                                # w_e, w_i (the implicit solve on LO in place)
         b["ratio"] = cells * s * K * (1 + 1 + e + 1 + 2)           # LO, T, adf_h, adf_v -> R+, R-
         b["update"] = cells * s * K * (e + 2 + 1 + 1 + 2)          # adf_h, R+-, adf_v, LO, T -> T
+        if residual:
+            b["update"] += cells * s * K * 2                        # the rounding residual, read and written
     else:
         b["hflux"] = cells * s * K * (1 + ta)                      # T (+T_AB)
         b["update"] = cells * s * (4 + qr + K * 1)                 # w_e, area, hnode_new, areasvol -> T
@@ -344,7 +353,8 @@ def build_case(cfg, precision, device, seed=20260301):
     if cfg["kind"] == "flat":
         m, vel, w, T0 = _flat_part(cfg["nx"] - 1, cfg["nz"], precision, device, cfg["dt"], 0.4, cfg["K"], seed)
         eng = TracerAdvection(m, cfg["K"], precision, *sch, copy_ab=True, device=device,
-                              tracer_vec=cfg.get("tracer_vec") if precision == "fp32" else None)
+                              tracer_vec=cfg.get("tracer_vec") if precision == "fp32" else None,
+                              residual=bool(cfg.get("residual")) and precision == "fp32")
         eng.load_padded(T=T0, vel=vel, w=w)
         if cfg.get("wsplit"):
             c = float(w.abs().max()) * cfg["wsplit"]
@@ -390,9 +400,10 @@ def build_case(cfg, precision, device, seed=20260301):
     return m, eng, eng.T.clone()
 
 
-REPORT_VARIANTS = (("residual", False, True, None), ("residual_plain_sums", True, True, None),
-                   ("compensated", False, False, None), ("plain_sums", True, False, None),
-                   ("anomaly", False, False, "auto"))
+# (name, plain-sum mask or None for the engine's default, residual, anomaly offsets)
+REPORT_VARIANTS = (("residual", None, True, None), ("residual_all_compensated", False, True, None),
+                   ("residual_plain_sums", True, True, None), ("plain", None, False, None),
+                   ("compensated", False, False, None), ("anomaly", None, False, "auto"))
 
 
 def precision_report(m, e32, T32, e64, T64, dt, steps, variants=REPORT_VARIANTS):
@@ -404,11 +415,12 @@ def precision_report(m, e32, T32, e64, T64, dt, steps, variants=REPORT_VARIANTS)
     violations (wet cells outside the initial [min, max], and the largest
     excursion relative to the initial range). The FP32 form runs several ways,
     which separates the error sources: "residual" (each value carries its FP32
-    rounding residual, compensated flux-divergence and FCT +/- sums),
-    "residual_plain_sums" (the same with plain FP32 sums), "compensated" (no
-    residual: FP32 storage rounding), "plain_sums" (neither) and "anomaly"
-    (compensated sums, no residual, each tracer stored as T - c about its
-    initial mean where that shrinks the stored values, offsets="auto")."""
+    rounding residual; the low-order fluxes summed with compensation, the
+    engine's default with the residual), "residual_all_compensated" (every sum
+    compensated), "residual_plain_sums" (none), "plain" (no residual, plain
+    sums: FP32 storage rounding), "compensated" (no residual, every sum
+    compensated) and "anomaly" (no residual, each tracer stored as T - c about
+    its initial mean where that shrinks the stored values, offsets="auto")."""
     import torch
 
     e64.T.copy_(T64)
@@ -466,7 +478,7 @@ def precision_report(m, e32, T32, e64, T64, dt, steps, variants=REPORT_VARIANTS)
         e32.load_padded(T=e64.from_layout(T64).clone())
     # the timed form's figures under the keys of earlier reports
     # the variant the engine itself runs (its sums and residual), else the first
-    timed = next((v[0] for v in variants if (v[1] is plain0 or v[1] == plain0) and v[2] == res0), variants[0][0])
+    timed = next((v[0] for v in variants if v[1] is plain0 and v[2] == res0), variants[0][0])
     out["timed_form"] = timed
     out["max_rel_err"] = out[timed]["max_rel_err"]
     out["sum_rel_err_fp32"] = out[timed]["sum_rel_err"]
@@ -530,6 +542,10 @@ def time_e2e(eng, T0, dt, steps, dist_barrier):
     host_in = torch.empty(T0.shape, dtype=T0.dtype, pin_memory=True)
     host_in.copy_(T0.cpu())
     host_out = torch.empty_like(host_in).pin_memory()
+    if eng.Tlo is not None:  # the residual form: each batch is the pair (values, residuals)
+        lo = torch.empty_like(host_in).pin_memory()
+        lo.copy_(eng.Tlo.cpu())
+        host_in, host_out = (host_in, lo), (host_out, torch.empty_like(lo).pin_memory())
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     # warm-up, and the number of copy streams per direction that runs the
     # batches fastest on this machine (host-device copy rates vary by host)
@@ -553,7 +569,8 @@ def time_e2e(eng, T0, dt, steps, dist_barrier):
     torch.cuda.synchronize()
     dist_barrier()
     eng.T.copy_(T0)
-    nbytes = host_in.numel() * host_in.element_size()
+    halves = host_in if isinstance(host_in, tuple) else (host_in,)
+    nbytes = sum(h.numel() * h.element_size() for h in halves)
     return start.elapsed_time(end), nbytes, nbytes, nc
 
 
@@ -646,6 +663,65 @@ def time_graph(eng, T0, dt, graph_steps, replays, warmup, dist_barrier):
     return start.elapsed_time(end), launches_per_replay
 
 
+def sequential_fp64(cfg, n64, device, dist, cells):
+    """Per-mesh sequential plain FP64 steps of a batching workload (eager
+    launches, one mesh after another): the denominator of the batching form."""
+    import torch
+
+    from fesom2_tracer_dwarf_gb300.engine import TracerAdvection
+
+    tot64, l64 = 0.0, 0
+    for i, (n, nz, cfl) in enumerate(batch_parts(cfg)):
+        p, v, w, T = _flat_part(n, nz, "fp64", device, cfg["dt"], cfl, cfg["K"], 20260301 + i)
+        e = TracerAdvection(p, cfg["K"], "fp64", cfg["hor"], cfg["ver"], cfg["lim"], copy_ab=True, device=device)
+        e.load_padded(T=T, vel=v, w=w)
+        e.step(cfg["dt"])
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        l0 = e.launches
+        t0.record()
+        e.step(cfg["dt"], n64)
+        t1.record()
+        torch.cuda.synchronize()
+        tot64 += t0.elapsed_time(t1)
+        l64 += e.launches - l0
+        del e, p, v, w, T
+    ms64 = tot64 / n64
+    return {"value": job_rate(ms64, cells, dist, device)[1], "ms_per_step": ms64, "steps": n64,
+            "mode": "per-mesh sequential eager launches", "gpu_launches": l64}
+
+
+def run_batch_form(name, args, device, dist, barrier, local):
+    """The batching form as a second figure of a run: the union of the
+    workload's meshes stepped by CUDA graphs of graph_steps steps (one launch
+    per stage over every mesh), its own clocks, and the per-mesh sequential
+    plain FP64 steps it replaces."""
+    from fesom2_tracer_dwarf_gb300 import autotune
+
+    cfg = WORKLOADS[name]
+    m, eng, T0 = build_case(cfg, cfg["precision"], device)
+    cells = m.wet_cells() * cfg["K"]
+    tuned = None if args.no_tune else autotune.tune(eng, cfg["dt"], reps=3)
+    replays = max(1, args.batch_steps // cfg["graph_steps"])
+    with ClockSampler(local) as clk:
+        total_ms, per_replay = time_graph(eng, T0, cfg["dt"], cfg["graph_steps"], replays, args.warmup, barrier)
+    nsteps = replays * cfg["graph_steps"]
+    ms = total_ms / nsteps
+    t_max, value = job_rate(ms, cells, dist, device)
+    out = {"workload": name, "config": workload_config(name, cfg, dist.get_world_size() if dist else 1),
+           "form": cfg["precision"], "value": value, "unit": UNIT, "ms_per_step": t_max, "steps": nsteps,
+           "cuda_graph_steps": cfg["graph_steps"], "tracer_cells_per_step": cells,
+           "launch_cfg": tuned["cfg"] if tuned else "default", "gpu_launches": per_replay * replays,
+           "clocks": clk.summary()}
+    del eng, m, T0
+    if not args.no_fp64:
+        n64 = max(1, min(nsteps, args.fp64_steps))
+        out["fp64"] = sequential_fp64(cfg, n64, device, dist, cells)
+        out["over_fp64"] = value / out["fp64"]["value"]
+    return out
+
+
 def run_gpu(args):
     import torch
 
@@ -689,7 +765,7 @@ def run_gpu(args):
     s = 4 if cfg["precision"] == "fp32" else 8
     wet_frac = m.wet_cells() / (m.N * m.nz)
     sb = {k: v * wet_frac for k, v in stage_bytes(m, K, s, cfg["ver"], fct=cfg["lim"] == "FCT",
-                                                  wsplit=bool(cfg.get("wsplit"))).items()}
+                                                  wsplit=bool(cfg.get("wsplit")), residual=eng.residual).items()}
     peak, peak_kind = load_peaks()
     step_bytes = sum(sb.values())
     if per is None:  # graph: per-stage times of one eager step for the roofline split
@@ -749,31 +825,11 @@ def run_gpu(args):
             result["precision_report"] = precision_report(m, eng, T0, e64, T64, cfg["dt"], cfg["report_steps"])
         del e64
     elif cfg.get("compare_fp64") == "sequential" and not args.no_fp64:
-        # per-mesh sequential plain FP64 steps (eager launches, one mesh after another)
-        from fesom2_tracer_dwarf_gb300.engine import TracerAdvection
-
         n64 = max(1, min(args.steps, args.fp64_steps))
-        tot64, l64 = 0.0, 0
-        for i, (n, nz, cfl) in enumerate(batch_parts(cfg)):
-            p, v, w, T = _flat_part(n, nz, "fp64", device, cfg["dt"], cfl, K, 20260301 + i)
-            e = TracerAdvection(p, K, "fp64", cfg["hor"], cfg["ver"], cfg["lim"], copy_ab=True, device=device)
-            e.load_padded(T=T, vel=v, w=w)
-            e.step(cfg["dt"])
-            torch.cuda.synchronize()
-            t0 = torch.cuda.Event(enable_timing=True)
-            t1 = torch.cuda.Event(enable_timing=True)
-            l0 = e.launches
-            t0.record()
-            e.step(cfg["dt"], n64)
-            t1.record()
-            torch.cuda.synchronize()
-            tot64 += t0.elapsed_time(t1)
-            l64 += e.launches - l0
-            del e, p, v, w, T
-        ms64 = tot64 / n64
-        result["fp64"] = {"value": job_rate(ms64, cells, dist, device)[1], "ms_per_step": ms64, "steps": n64,
-                          "mode": "per-mesh sequential eager launches", "gpu_launches": l64}
+        result["fp64"] = sequential_fp64(cfg, n64, device, dist, cells)
         result["fp32_over_fp64"] = value / result["fp64"]["value"]
+    if cfg.get("batch") and not args.no_batch:
+        result[cfg["batch"]] = run_batch_form(cfg["batch"], args, device, dist, barrier, local)
     if cfg["kind"] == "files":
         lev = m.get("nlevels_nod2D") - 1
         result["mesh_layers"] = {"min": int(lev.min()), "max": int(lev.max()), "mean": float(lev.mean())}
@@ -862,15 +918,19 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-report", action="store_true", help="skip the FP32-vs-FP64 precision report")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batching form's second figure")
+    ap.add_argument("--batch-steps", type=int, default=100,
+                    help="steps of the batching form's second figure (whole CUDA graphs)")
     ap.add_argument("--no-tune", action="store_true", help="use the default launch configuration")
     ap.add_argument("--profile", type=int, default=0, metavar="N",
                     help="build the workload, run N plain steps (for a profiler) and exit")
-    ap.add_argument("--precision", choices=["fp32", "fp64"], default=None,
+    ap.add_argument("--precision", choices=["fp32", "fp64", "fp64fast"], default=None,
                     help="with --profile: the form to run (default: the workload's)")
     ap.add_argument("--launch-cfg", default=None,
                     help="with --profile: launch configuration, comma-separated (default: the library's)")
     ap.add_argument("--plain-sums", type=int, default=None,
-                    help="with --profile: FP32 plain-sum bit mask (1 LO, 2 update, 4 FCT sums; default 0)")
+                    help="with --profile: FP32 plain-sum bit mask (1 LO, 2 update, 4 FCT sums; default: "
+                         "6 with the residual, 7 without)")
     ap.add_argument("--residual", type=int, default=None, help="with --profile: 1 keeps the FP32 rounding residual")
     args = ap.parse_args()
     if args.profile:

@@ -69,7 +69,7 @@ class TracerAdvection:
     def __init__(self, mesh: Mesh, ntracers: int, precision: str = "fp64", hor: str = "UPW1",
                  ver: str = "UPW1", lim: str = "NONE", ph: float = 1.0, pv: float = 1.0,
                  copy_ab: bool = False, device: str = "cuda", tracer_vec: int | None = None,
-                 ab2_eps: float | None = None, offsets=None, plain_sums: bool = False, residual: bool = False):
+                 ab2_eps: float | None = None, offsets=None, plain_sums=None, residual: bool = False):
         _require_cuda()
         if ab2_eps is not None and copy_ab:
             raise ValueError("copy_ab and ab2_eps are two choices of the valuesAB time level; give one")
@@ -88,7 +88,9 @@ class TracerAdvection:
         self.copy_ab = copy_ab
         self.ab2_eps = None if ab2_eps is None else float(ab2_eps)
         # FP32 form: plain FP32 sums instead of compensated ones (fgb_step_desc.fp32_plain_sums:
-        # True = all, False = none, or the bit mask 1 LO fluxes, 2 update divergence, 4 FCT +/- sums)
+        # True = all, False = none, or the bit mask 1 LO fluxes, 2 update divergence, 4 FCT +/- sums).
+        # None: by the form -- with the residual only the LO fluxes are compensated (the piece that keeps
+        # the tracer sum to 1e-12), without it none (FP32 storage rounding dominates the sum's error)
         self.plain_sums = plain_sums
         # FP32 form with the FCT limiter: each value carries its FP32 rounding residual (self.Tlo)
         self.residual = bool(residual) and precision == "fp32" and lim == "FCT"
@@ -126,6 +128,7 @@ class TracerAdvection:
         on = bool(on) and self.precision == "fp32" and self.lim == "FCT"
         self.residual = on
         self.Tlo = torch.zeros_like(self.T) if on else None
+        self._host_lo = None  # run_host's residual buffers follow the new one
 
     def set_launch(self, cfg):
         """Launch configuration (fgb_step_desc.cfg): a list of up to 12 ints or a
@@ -275,7 +278,9 @@ class TracerAdvection:
         d.workspace = self.workspace.data_ptr()
         d.workspace_bytes = self.workspace.numel()
         ps = self.plain_sums
-        d.fp32_plain_sums = 7 if ps is True else (0 if ps is False or ps is None else int(ps))
+        if ps is None:
+            ps = 6 if self.Tlo is not None else 7
+        d.fp32_plain_sums = 7 if ps is True else (0 if ps is False else int(ps))
         d.Tlo = None if self.Tlo is None else self.Tlo.data_ptr()
         for i, c in enumerate(self.cfg):
             d.cfg[i] = c
@@ -294,7 +299,11 @@ class TracerAdvection:
         memory: batch i is copied to the device from ``host_in[i]``, advanced
         ``nsteps`` steps, and copied back into ``host_out[i]`` (tensors of
         ``layout_shape`` and the engine's dtype, pinned for asynchronous
-        copies; one tensor may serve several batches).
+        copies; one tensor may serve several batches). An engine that keeps
+        the FP32 rounding residual (residual=True) takes and returns each
+        batch as a pair (values, residuals) of such tensors, the two halves of
+        the FP64 field; a single tensor is then a batch of FP32 values, whose
+        residual starts at zero and is not returned.
 
         Three device buffers take turns as the field being stepped, the next
         batch arriving and the previous batch leaving, so the host-to-device
@@ -307,20 +316,31 @@ class TracerAdvection:
         before reading ``host_out``."""
         if self.TA is not None:
             raise ValueError("run_host needs copy_ab=True (valuesAB follows the values)")
-        # host batches are FP32 values stepped from the host: they carry no rounding residual
-        saved_tlo, self.Tlo = self.Tlo, None
         nb = len(host_in)
         if len(host_out) != nb:
             raise ValueError("host_in and host_out need one tensor per batch")
+
+        def halves(x):
+            x = tuple(x) if isinstance(x, (tuple, list)) else (x,)
+            if len(x) not in (1, 2) or (len(x) == 2 and self.Tlo is None):
+                raise ValueError("a batch is one tensor, or a (values, residuals) pair with residual=True")
+            return x
+
+        host_in = [halves(x) for x in host_in]
+        host_out = [halves(x) for x in host_out]
         nc = max(1, int(copy_streams))
         main = torch.cuda.current_stream(self.device)
+        if not hasattr(self, "_host_bufs"):
+            self._host_bufs = [self.T] + [torch.empty_like(self.T) for _ in range(2)]
+        if self.Tlo is not None and getattr(self, "_host_lo", None) is None:
+            self._host_lo = [self.Tlo] + [torch.empty_like(self.Tlo) for _ in range(2)]
         if getattr(self, "_host_nc", None) != nc:
-            if not hasattr(self, "_host_bufs"):
-                self._host_bufs = [self.T] + [torch.empty_like(self.T) for _ in range(2)]
             self._h2d = [torch.cuda.Stream(self.device) for _ in range(nc)]
             self._d2h = [torch.cuda.Stream(self.device) for _ in range(nc)]
             self._host_nc = nc
         bufs = self._host_bufs
+        lo = self._host_lo if self.Tlo is not None else None
+        saved_t, saved_lo = self.T, self.Tlo
         numel = bufs[0].numel()
         bounds = [(c * numel) // nc for c in range(nc + 1)]
         free = [[torch.cuda.Event() for _ in range(nc)] for _ in range(3)]     # chunk no longer read by D2H
@@ -330,38 +350,51 @@ class TracerAdvection:
             for c in range(nc):
                 free[b][c].record(main)
 
+        def device_halves(b):
+            return (bufs[b],) if lo is None else (bufs[b], lo[b])
+
         def load(i):
             b = i % 3
-            src, dst = host_in[i].view(-1), bufs[b].view(-1)
+            pairs = list(zip(host_in[i], device_halves(b)))
             for c in range(nc):
                 st = self._h2d[c]
                 with torch.cuda.stream(st):
                     st.wait_event(free[b][c])
-                    dst[bounds[c]:bounds[c + 1]].copy_(src[bounds[c]:bounds[c + 1]], non_blocking=True)
+                    for src, dst in pairs:
+                        dst.view(-1)[bounds[c]:bounds[c + 1]].copy_(src.view(-1)[bounds[c]:bounds[c + 1]],
+                                                                   non_blocking=True)
                     arrived[b][c].record(st)
 
-        if nb:
-            load(0)
-        for i in range(nb):
-            b = i % 3
-            if i + 1 < nb:
-                load(i + 1)
-            for c in range(nc):
-                main.wait_event(arrived[b][c])
-            self.T = bufs[b]
-            self.step(dt, nsteps)
-            stepped[b].record(main)
-            src, dst = bufs[b].view(-1), host_out[i].view(-1)
-            for c in range(nc):
-                st = self._d2h[c]
-                with torch.cuda.stream(st):
-                    st.wait_event(stepped[b])
-                    dst[bounds[c]:bounds[c + 1]].copy_(src[bounds[c]:bounds[c + 1]], non_blocking=True)
-                    free[b][c].record(st)
-        for b in range(3):
-            for c in range(nc):
-                main.wait_event(free[b][c])
-        self.Tlo = saved_tlo
+        try:
+            if nb:
+                load(0)
+            for i in range(nb):
+                b = i % 3
+                if i + 1 < nb:
+                    load(i + 1)
+                for c in range(nc):
+                    main.wait_event(arrived[b][c])
+                self.T = bufs[b]
+                if lo is not None:
+                    self.Tlo = lo[b]
+                    if len(host_in[i]) == 1:  # FP32 values: no residual yet
+                        self.Tlo.zero_()
+                self.step(dt, nsteps)
+                stepped[b].record(main)
+                pairs = list(zip(device_halves(b), host_out[i]))
+                for c in range(nc):
+                    st = self._d2h[c]
+                    with torch.cuda.stream(st):
+                        st.wait_event(stepped[b])
+                        for src, dst in pairs:
+                            dst.view(-1)[bounds[c]:bounds[c + 1]].copy_(src.view(-1)[bounds[c]:bounds[c + 1]],
+                                                                       non_blocking=True)
+                        free[b][c].record(st)
+            for b in range(3):
+                for c in range(nc):
+                    main.wait_event(free[b][c])
+        finally:
+            self.T, self.Tlo = saved_t, saved_lo
         return host_out
 
     def capture(self, dt: float, nsteps: int = 1):

@@ -265,3 +265,39 @@ def test_run_host_batches(pkg, oracle_mod):
     torch.cuda.synchronize()
     for got, exp in zip(host_out, expect):
         assert torch.equal(got, exp)
+
+
+def test_run_host_batches_with_residual(pkg, oracle_mod):
+    """run_host on an engine that keeps the FP32 rounding residual: batches
+    given as (values, residuals) pairs come back as the pair that stepping
+    each batch on the device gives, bit for bit; a batch given as one tensor
+    starts with a zero residual."""
+    mesh_mod, engine, synthetic = pkg
+    m = mesh_mod.Mesh(**MESHES["periodic"])
+    rng = np.random.default_rng(81)
+    vel, w = synthetic.random_flow(m, rng)
+    eng = engine.TracerAdvection(m, 4, "fp32", "MUSCL", "PPM", "FCT", copy_ab=True, residual=True)
+    eng.set_velocity(vel, w)
+    fields = [synthetic.random_field(m, rng, 4) for _ in range(4)]
+    expect, host_in = [], []
+    for f in fields:
+        eng.set_tracers(f)
+        host_in.append((eng.T.cpu().pin_memory(), eng.Tlo.cpu().pin_memory()))
+        eng.step(300.0, 2)
+        expect.append((eng.T.cpu().clone(), eng.Tlo.cpu().clone()))
+    assert any(float(lo.abs().max()) > 0 for _, lo in host_in)
+    host_out = [(torch.empty_like(a).pin_memory(), torch.empty_like(b).pin_memory()) for a, b in host_in]
+    eng.run_host(host_in, host_out, 300.0, nsteps=2)
+    torch.cuda.synchronize()
+    for (gt, gl), (et, el) in zip(host_out, expect):
+        assert torch.equal(gt, et) and torch.equal(gl, el)
+    # one tensor: the values alone, residual zero at the start of the batch
+    eng.set_tracers(fields[0])
+    vals = eng.T.cpu().pin_memory()
+    eng.Tlo.zero_()
+    eng.step(300.0)
+    exp = eng.T.cpu().clone()
+    out = torch.empty_like(vals).pin_memory()
+    eng.run_host([vals], [out], 300.0)
+    torch.cuda.synchronize()
+    assert torch.equal(out, exp)
