@@ -697,6 +697,8 @@ def run_batch_form(name, args, device, dist, barrier, local):
     workload's meshes stepped by CUDA graphs of graph_steps steps (one launch
     per stage over every mesh), its own clocks, and the per-mesh sequential
     plain FP64 steps it replaces."""
+    import torch
+
     from fesom2_tracer_dwarf_gb300 import autotune
 
     cfg = WORKLOADS[name]
@@ -715,6 +717,7 @@ def run_batch_form(name, args, device, dist, barrier, local):
            "launch_cfg": tuned["cfg"] if tuned else "default", "gpu_launches": per_replay * replays,
            "clocks": clk.summary()}
     del eng, m, T0
+    torch.cuda.empty_cache()
     if not args.no_fp64:
         n64 = max(1, min(nsteps, args.fp64_steps))
         out["fp64"] = sequential_fp64(cfg, n64, device, dist, cells)
@@ -819,16 +822,19 @@ def run_gpu(args):
                            "gpu_launches": l64}
             if key == "fp64":
                 del e64, m64, T64
+                torch.cuda.empty_cache()  # the mesh and workspace allocations are the library's own
         result["fp32_over_fp64"] = value / result["fp64"]["value"]
         result["fp32_over_fp64_exact"] = value / result["fp64_exact"]["value"]
         if cfg.get("report_steps") and not args.no_report:
             result["precision_report"] = precision_report(m, eng, T0, e64, T64, cfg["dt"], cfg["report_steps"])
-        del e64
+        del e64, m64, T64
+        torch.cuda.empty_cache()
     elif cfg.get("compare_fp64") == "sequential" and not args.no_fp64:
         n64 = max(1, min(args.steps, args.fp64_steps))
         result["fp64"] = sequential_fp64(cfg, n64, device, dist, cells)
         result["fp32_over_fp64"] = value / result["fp64"]["value"]
     if cfg.get("batch") and not args.no_batch:
+        torch.cuda.empty_cache()
         result[cfg["batch"]] = run_batch_form(cfg["batch"], args, device, dist, barrier, local)
     if cfg["kind"] == "files":
         lev = m.get("nlevels_nod2D") - 1

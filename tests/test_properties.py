@@ -7,6 +7,14 @@ meshes, CPU) and on the GPU (up to the full benchmark meshes).
 - the volume integral sum(T * hnode_new * areasvol) over wet cells is
   conserved on closed-wall and ragged basins;
 - FCT creates no new extrema under a solenoidal flow at CFL <= 0.5.
+
+The FP32 form's bars, over 3-5 steps: the volume integral to 1e-9 (closed
+basins) and 1e-10 (the 2048^2 mesh) with FP32 storage, to 1e-11 and 1e-13
+when each value carries its FP32 rounding residual; within 2e-6 of the FP64
+form in the max-norm; no excursion beyond 1e-6 of the initial range. (Largest
+figures measured on a GB300: 2.2e-10, 1.1e-11, 1.4e-12, 2.1e-14, 3.4e-7.) The
+sum is taken with FP64 volumes, which the FP32 kernels round: on the 129^2
+basin that rounding alone is of order 1e-12.
 """
 import itertools
 
@@ -144,7 +152,7 @@ def test_gpu_uniform_stays_uniform(precision, hor, ver, lim):
     T = np.full((4, m.N, m.nz), 7.25)
     e = _engine(m, 4, precision, (hor, ver, lim), vel, w, T)
     e.step(300.0, 5)
-    tol = 1e-12 if precision == "fp64" else 2e-6
+    tol = 1e-12 if precision == "fp64" else 5e-7
     assert np.abs(e.values() - 7.25)[:, _wet(m)].max() <= tol * 7.25
 
 
@@ -176,15 +184,20 @@ def _closed_basin(nx, nl, seed):
     return Mesh(nx, nx, nl, Lx=L, Ly=L, depth=-zb[-1], periodic=False, orient_left=True, zbar=zb, elem_nlev=en), rng
 
 
+FP32_SUM_TOL = {"plain": 1e-9, "residual": 1e-11}
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("nx,nl", [(129, 33), (1025, 65)])
-def test_gpu_closed_basin_conservation_and_bounds(nx, nl):
+@pytest.mark.parametrize("form", ["plain", "residual"])
+def test_gpu_closed_basin_conservation_and_bounds(nx, nl, form):
     """Closed ragged basin (1025 grid points: the 1024^2 benchmark basin):
     FP64 conserves the volume integral to 1e-12 and FCT keeps every tracer in
-    its initial range; the FP32 form stays within 1e-5 of FP64 and conserves
-    to its own rounding."""
+    its initial range; the FP32 form (FP32 storage, or each value with its
+    rounding residual) stays within 2e-6 of FP64, keeps the range to 1e-6 and
+    conserves to 1e-9 (1e-11 with the residual)."""
     _gpu()
-    from fesom2_tracer_dwarf_gb300 import synthetic
+    from fesom2_tracer_dwarf_gb300 import engine, synthetic
 
     m, rng = _closed_basin(nx, nl, 11)
     vel, w = synthetic.streamfunction_flow(m, rng, 400.0, cfl=0.4, psi_wall_zero=True)
@@ -198,7 +211,10 @@ def test_gpu_closed_basin_conservation_and_bounds(nx, nl):
     e64.step(400.0, steps)
     v64 = e64.values()
     del e64
-    e32 = _engine(m, 2, "fp32", sch, vel, w, T)
+    e32 = engine.TracerAdvection(m, 2, "fp32", *sch, copy_ab=True, residual=form == "residual")
+    assert e32.residual == (form == "residual")
+    e32.set_tracers(T)
+    e32.set_velocity(vel, w)
     e32.step(400.0, steps)
     v32 = e32.values()
     for t in range(2):
@@ -207,16 +223,19 @@ def test_gpu_closed_basin_conservation_and_bounds(nx, nl):
         lo, hi = T[t][wet].min(), T[t][wet].max()
         assert v64[t][wet].min() >= lo - 1e-12 * abs(lo) and v64[t][wet].max() <= hi + 1e-12 * abs(hi)
         a32 = (v32[t] * vol).sum()
-        assert abs(a32 - before[t]) <= 1e-6 * abs(before[t])
-        assert np.abs(v32[t] - v64[t])[wet].max() <= 1e-5 * np.abs(v64[t]).max()
-        assert v32[t][wet].min() >= lo - 1e-5 * abs(lo) and v32[t][wet].max() <= hi + 1e-5 * abs(hi)
+        rel = abs(a32 - before[t]) / abs(before[t])
+        assert rel <= FP32_SUM_TOL[form], f"{form} tracer {t}: volume integral off by {rel:.3g}"
+        assert np.abs(v32[t] - v64[t])[wet].max() <= 2e-6 * np.abs(v64[t]).max()
+        assert v32[t][wet].min() >= lo - 1e-6 * abs(lo) and v32[t][wet].max() <= hi + 1e-6 * abs(hi)
 
 
 @pytest.mark.gpu
-def test_gpu_periodic_2048_fp32_properties():
+@pytest.mark.parametrize("form", ["plain", "residual"])
+def test_gpu_periodic_2048_fp32_properties(form):
     """The 2048^2 x 64-layer benchmark mesh, K = 4, MUSCL-FCT + PPM, FP32 form:
-    uniform tracers stay uniform, the volume integral of the others is
-    conserved to FP32 rounding and FCT creates no new extrema."""
+    uniform tracers stay uniform (5e-7), the volume integral of the others is
+    conserved to 1e-10 (1e-13 with the rounding residual) and FCT creates no
+    new extrema (1e-6 of the range)."""
     _gpu()
     from fesom2_tracer_dwarf_gb300 import synthetic
     from fesom2_tracer_dwarf_gb300.engine import TracerAdvection
@@ -228,7 +247,7 @@ def test_gpu_periodic_2048_fp32_properties():
     vel, w = synthetic.flat_streamfunction_device(m, rng, 400.0, torch.float32, "cuda", cfl=0.4)
     T = synthetic.tracers_device(m, 4, 3, torch.float32, "cuda")
     T[3, :, : m.nz] = 7.25
-    e = TracerAdvection(m, 4, "fp32", "MUSCL", "PPM", "FCT", copy_ab=True)
+    e = TracerAdvection(m, 4, "fp32", "MUSCL", "PPM", "FCT", copy_ab=True, residual=form == "residual")
     e.load_padded(T=T, vel=vel, w=w)
     vol = torch.as_tensor(m.get("areasvol")[:, : m.nz] * m.get("hnode_new"), device="cuda", dtype=torch.float64)
     Td = T[:, :, : m.nz].double()
@@ -236,11 +255,11 @@ def test_gpu_periodic_2048_fp32_properties():
     mn, mx = Td.amin(dim=(1, 2)), Td.amax(dim=(1, 2))
     del Td
     e.step(400.0, 3)
-    after_T = e.from_layout(e.T)[:, :, : m.nz].double()
+    after_T = e.full_values()[:, :, : m.nz]
     after = (after_T * vol).sum(dim=(1, 2))
     rel = ((after - before).abs() / before.abs()).cpu().numpy()
-    assert np.all(rel <= 1e-6), rel
+    assert np.all(rel <= (1e-13 if form == "residual" else 1e-10)), rel
     amn, amx = after_T.amin(dim=(1, 2)), after_T.amax(dim=(1, 2))
-    tol = 1e-5 * torch.maximum(mn.abs(), mx.abs())
+    tol = 1e-6 * torch.maximum(mn.abs(), mx.abs())
     assert bool(torch.all(amn >= mn - tol)) and bool(torch.all(amx <= mx + tol))
-    assert float((after_T[3] - 7.25).abs().max()) <= 2e-6 * 7.25
+    assert float((after_T[3] - 7.25).abs().max()) <= 5e-7 * 7.25
