@@ -801,7 +801,7 @@ __device__ __forceinline__ void vimpl_row(int k, int k0, int k1, float W0, float
 // at the upwind node; this node adds -v T_up (role 0, the edge's first node)
 // or +v T_up (role 1), the same rounded product at both ends of the edge.
 // ---------------------------------------------------------------------------
-template <int VER, int KV, int NS, bool WSPLIT>
+template <int VER, int KV, int NS, bool WSPLIT, bool COMP>
 __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
@@ -891,7 +891,7 @@ __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
     for (unsigned base = 0; base < LZ; base += kW * NS) {
       unsigned kk[NS];
       bool in[NS];
-      V<KV> acc[NS], tnk[NS];
+      V<KV> acc[NS], accc[NS], tnk[NS];
       float hnv[NS], hnnv[NS], avv[NS];
 #pragma unroll
       for (int i = 0; i < NS; ++i) {
@@ -899,6 +899,7 @@ __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
         in[i] = k < LZ;
         kk[i] = in[i] ? k : LZ - 1;
         acc[i] = splat<KV>(0.f);
+        accc[i] = splat<KV>(0.f);
         tnk[i] = sT[kk[i]];
         hnv[i] = g.hnode[n * LZ + kk[i]];
         hnnv[i] = g.hnode_new[n * LZ + kk[i]];
@@ -923,7 +924,9 @@ __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
 #pragma unroll
           for (int c = 0; c < KV; ++c) tu.v[c] = own_up ? tnk[i].v[c] : to[i].v[c];
           const V<KV> p = muls(tu, v[i]);
-          acc[i] = role ? add(acc[i], p) : sub(acc[i], p);
+          // with COMP the sum carries its rounding error (TwoSum)
+          if (COMP) two_sum(acc[i], accc[i], role ? p : sub(splat<KV>(0.f), p));
+          else acc[i] = role ? add(acc[i], p) : sub(acc[i], p);
         }
       }
       V<KV> lk[NS];
@@ -938,7 +941,7 @@ __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
         if (z >= nzmin && z <= nzmax - 1) {
           const float hn = hnv[i], hnn = hnnv[i], av = avv[i];
           const float ra = hn / hnn, rb = fdv(dt, av * hnn);  // ra IEEE: exactly 1 for an unchanged layer
-          l = fmas(add(acc[i], sub(sFlo[k], sFlo[k + 1])), rb, muls(tn, ra - 1.f));
+          l = fmas(add(COMP ? add(acc[i], accc[i]) : acc[i], sub(sFlo[k], sFlo[k + 1])), rb, muls(tn, ra - 1.f));
         }
         if (WSPLIT && NS == 2 && a.wsplit_fused) lk[i] = l;
         else st<KV>(lo, n * LZ + k, l);

@@ -44,16 +44,21 @@ void launch_hflux_ns(const DMesh& m, const FastPtrs& a, const LaunchArgs& L, cud
   }
 }
 
-template <int KV, int VER, int NS>
-void launch_lo_f(const DMesh& m, const FastPtrs& a, int nw, cudaStream_t s) {
+template <int KV, int VER, int NS, bool WSPLIT, bool COMP>
+void launch_lo_fc(const DMesh& m, const FastPtrs& a, int nw, cudaStream_t s) {
   const LoCols c = lo_cols(VER, a.we != a.w, a.TA != a.T);
   const size_t sm = nw * warp_bytes<KV>(c.scal, c.vec, m.LW);
+  allow_smem_f(kf_lo<VER, KV, NS, WSPLIT, COMP>, sm);
+  kf_lo<VER, KV, NS, WSPLIT, COMP><<<(m.N + nw - 1) / nw, nw * kW, sm, s>>>(m, a);
+}
+template <int KV, int VER, int NS>
+void launch_lo_f(const DMesh& m, const FastPtrs& a, int nw, cudaStream_t s) {
   if (a.wi) {
-    allow_smem_f(kf_lo<VER, KV, NS, true>, sm);
-    kf_lo<VER, KV, NS, true><<<(m.N + nw - 1) / nw, nw * kW, sm, s>>>(m, a);
+    if (a.comp & 1) launch_lo_fc<KV, VER, NS, true, true>(m, a, nw, s);
+    else launch_lo_fc<KV, VER, NS, true, false>(m, a, nw, s);
   } else {
-    allow_smem_f(kf_lo<VER, KV, NS, false>, sm);
-    kf_lo<VER, KV, NS, false><<<(m.N + nw - 1) / nw, nw * kW, sm, s>>>(m, a);
+    if (a.comp & 1) launch_lo_fc<KV, VER, NS, false, true>(m, a, nw, s);
+    else launch_lo_fc<KV, VER, NS, false, false>(m, a, nw, s);
   }
 }
 
