@@ -825,6 +825,8 @@ def run_gpu(args):
                 torch.cuda.empty_cache()  # the mesh and workspace allocations are the library's own
         result["fp32_over_fp64"] = value / result["fp64"]["value"]
         result["fp32_over_fp64_exact"] = value / result["fp64_exact"]["value"]
+        # the FP64 forms' bound: this device's FP64 FMA and division rates
+        result["fp64_peak"] = _lib.probe_fp64(ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
         if cfg.get("report_steps") and not args.no_report:
             result["precision_report"] = precision_report(m, eng, T0, e64, T64, cfg["dt"], cfg["report_steps"])
         del e64, m64, T64

@@ -73,6 +73,7 @@ ENGINE_SYMBOLS = [
     "fgb_hmesh_set_vertical", "fgb_mesh_create", "fgb_mesh_free", "fgb_mesh_dims", "fgb_mesh_update_vertical",
     "fgb_workspace_bytes", "fgb_workspace_offsets", "fgb_adv_step", "fgb_adv_stages", "fgb_stats_scratch_bytes",
     "fgb_tracer_stats", "fgb_tracer_stats_grouped", "fgb_last_launch_count", "fgb_static_workspace_bytes", "fgb_adv_step_static",
+    "fgb_probe_fp64",
 ]
 
 _lib = None
@@ -115,6 +116,7 @@ def load(build_if_missing: bool = True):
         "fgb_stats_scratch_bytes": (ctypes.c_longlong, [_vp, ctypes.c_int]),
         "fgb_static_workspace_bytes": (ctypes.c_longlong, []),
         "fgb_adv_step_static": (ctypes.c_int, [_vp, ctypes.POINTER(StepDesc), _vp]),
+        "fgb_probe_fp64": (ctypes.c_int, [_dp, _vp]),
         "fgb_tracer_stats": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_longlong, ctypes.c_int, _vp, _vp,
                                             _vp]),
         "fgb_tracer_stats_grouped": (ctypes.c_int, [_vp, _vp, ctypes.c_longlong, ctypes.c_int, ctypes.c_int, _vp,
@@ -130,6 +132,14 @@ def load(build_if_missing: bool = True):
 
 def last_error() -> str:
     return load().fgb_last_error().decode()
+
+
+def probe_fp64(stream=None) -> dict:
+    """The current device's FP64 rates (fgb_probe_fp64): fused multiply-add
+    TFLOP/s and IEEE double divisions in G/s."""
+    out = (ctypes.c_double * 3)()
+    check(load().fgb_probe_fp64(out, stream), "fgb_probe_fp64")
+    return {"fma_tflops": out[0], "div_g_per_s": out[1], "ms": out[2]}
 
 
 def check(rc: int, what: str):

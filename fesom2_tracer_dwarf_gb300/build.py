@@ -39,6 +39,7 @@ SOURCES = [
     ("fgb_fast_kv2.cu", "nvcc", []),
     ("fgb_fast_kv4.cu", "nvcc", []),
     ("fgb_static_ws.cu", "nvcc", []),
+    ("fgb_probe.cu", "nvcc", []),
 ]
 
 

@@ -321,6 +321,12 @@ int fgb_last_launch_count(void);
 long long fgb_static_workspace_bytes(void);
 int fgb_adv_step_static(const fgb_mesh* m, const fgb_step_desc* d, void* stream);
 
+/* No counterpart in the reference: the current device's FP64 rates, the bound
+ * of the FP64 forms. out3 receives fused multiply-add TFLOP/s, IEEE double
+ * divisions per second (in G/s) and the milliseconds the two timed launches
+ * took. Synchronises `stream`; 0 on success, -1 with a message. */
+int fgb_probe_fp64(double* out3, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -222,3 +222,15 @@ def test_fast_fp64_within_1e12(pkg, oracle_mod, meshname, hor, ver, lim):
     got = eng.values()
     rel = max(float(np.abs(got[t] - vals[t])[wet].max() / np.abs(vals[t][wet]).max()) for t in range(K))
     assert rel <= FAST64_TOL, f"{meshname} {hor}/{ver}/{lim}: fast FP64 relative error {rel:.3g}"
+
+
+def test_fp64_probe_rates(pkg):
+    """fgb_probe_fp64: the FP64 FMA and division rates of the device, the
+    bound of the FP64 forms. GB300's FP64 units give about 1.2 TFLOP/s of
+    FMA; the bounds only reject a probe that did not run or did no work."""
+    from fesom2_tracer_dwarf_gb300 import _lib
+
+    r = _lib.probe_fp64()
+    assert 0.05 < r["fma_tflops"] < 200.0, r
+    assert 0.5 < r["div_g_per_s"] < 20000.0, r
+    assert r["ms"] > 0.0
