@@ -94,6 +94,14 @@ bool validate(const HostMesh& h, std::string* err) {
     *err = std::string("mesh validation failed: ") + what;
     return false;
   };
+  if (!h.node_order.empty()) {  // a permutation of the nodes
+    if ((int)h.node_order.size() != h.N) return bad("node visit order size");
+    std::vector<char> seen(h.N, 0);
+    for (int n : h.node_order) {
+      if (n < 0 || n >= h.N || seen[n]) return bad("node visit order is not a permutation");
+      seen[n] = 1;
+    }
+  }
   for (int e = 0; e < h.E; ++e) {
     for (int r = 0; r < 2; ++r)
       if (h.edges[2 * e + r] < 0 || h.edges[2 * e + r] >= h.N) return bad("edge node index");
@@ -143,7 +151,7 @@ int fgb_hmesh_analytic(int nx, int ny, int nl, double Lx, double Ly, double dept
 
 int fgb_hmesh_from_files(const char* dir, int flags, fgb_hmesh** out) {
   if (!out || !dir) { set_error("null argument"); return -1; }
-  if (flags & ~7) { set_error("unknown mesh-file flags"); return -1; }
+  if (flags & ~15) { set_error("unknown mesh-file flags"); return -1; }
   std::string err;
   HostMesh* m = build_from_files(dir, flags, &err);
   if (!m) { set_error(err); return -1; }
@@ -158,7 +166,7 @@ int fgb_hmesh_from_arrays(int nod2D, int elem2D, int edge2D, int edge2D_in, int 
     set_error("null argument");
     return -1;
   }
-  if (flags & ~7) { set_error("unknown mesh-file flags"); return -1; }
+  if (flags & ~15) { set_error("unknown mesh-file flags"); return -1; }
   std::string err;
   HostMesh* m = build_from_arrays(nod2D, elem2D, edge2D, edge2D_in, nl, lonlat, elem, edges, edge_tri, elvls, nlvls,
                                   zbar, flags, &err);
@@ -208,7 +216,7 @@ long long fgb_hmesh_get(const fgb_hmesh* h, const char* name, void* out, int* ki
       {"nboundary_lay", &m.nboundary_lay}, {"ne_ptr", &m.ne_ptr}, {"ne_code", &m.ne_code},
       {"ne_other", &m.ne_other}, {"ne_lo", &m.ne_lo}, {"ne_hi", &m.ne_hi}, {"cl_ptr", &m.cl_ptr},
       {"cl_node", &m.cl_node}, {"cl_lev", &m.cl_lev}, {"cl_minlev", &m.cl_minlev}, {"edge_lev", &m.edge_lev},
-      {"edge_gm", &m.edge_gm}, {"edge_order", &m.edge_order}, {"nie_ptr", &m.nie_ptr}, {"nie_idx", &m.nie_idx}};
+      {"edge_gm", &m.edge_gm}, {"edge_order", &m.edge_order}, {"node_order", &m.node_order}, {"nie_ptr", &m.nie_ptr}, {"nie_idx", &m.nie_idx}};
   struct { const char* n; const std::vector<double>* v; } dbls[] = {
       {"coord", &m.coord}, {"zbar", &m.zbar}, {"Z", &m.Z}, {"elem_area", &m.elem_area}, {"area", &m.area},
       {"areasvol", &m.areasvol}, {"edge_dxdy", &m.edge_dxdy}, {"edge_cross_dxdy", &m.edge_cross},
@@ -361,6 +369,7 @@ int fgb_mesh_create(const fgb_hmesh* hm, fgb_mesh** out) {
             !upload(mm, h.edge_lev.data(), h.edge_lev.size(), &d.edge_lev) &&
             !upload(mm, h.edge_gm.data(), h.edge_gm.size(), &d.edge_gm) &&
             !upload(mm, h.edge_order.data(), h.edge_order.size(), &d.edge_order) &&
+            (h.node_order.empty() || !upload(mm, h.node_order.data(), h.node_order.size(), &d.node_order)) &&
             !upload_geo<double>(mm, h, d.g64, &mm->hnode64, &mm->hnode_new64, &mm->helem64) &&
             !upload_geo<float>(mm, h, d.g32, &mm->hnode32, &mm->hnode_new32, &mm->helem32);
   if (!ok) {

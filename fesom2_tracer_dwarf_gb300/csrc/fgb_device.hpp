@@ -47,6 +47,7 @@ struct DMesh {
   const int* edge_lev;    // (E,4)
   const int* edge_gm;     // (E,2)
   const int* edge_order;  // (E) order in which edge kernels visit the edges
+  const int* node_order;  // (N) order in which node kernels visit the columns; nullptr: node index
   // FP32 form, MUSCL/MFCT: per edge the two other vertices of the upwind and
   // downwind triangles (E,4) and the triangles' edge-direction weights (E,4)
   // each; valid when fast_tri_ok (each triangle holds its edge node).
@@ -68,6 +69,12 @@ struct DMesh {
   GeoPtrs<double> g64;
   GeoPtrs<float> g32;
 };
+
+// Node column of visit position i of a node kernel (every column is visited
+// once; the order only shapes which columns are in flight together).
+#ifdef __CUDACC__
+__device__ __forceinline__ int visit_node(const DMesh& m, int i) { return m.node_order ? __ldg(m.node_order + i) : i; }
+#endif
 
 // Per-launch field pointers. Tracer t of a batch lives at base + t*stride.
 template <typename R>

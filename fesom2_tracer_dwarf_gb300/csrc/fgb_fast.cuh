@@ -805,8 +805,9 @@ template <int VER, int KV, int NS, bool WSPLIT, bool COMP>
 __global__ void __launch_bounds__(128, 7) kf_lo(DMesh m, FastPtrs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
-  const int n = blockIdx.x * (blockDim.x / kW) + wib;
-  if (n >= m.N) return;
+  const int vi = blockIdx.x * (blockDim.x / kW) + wib;
+  if (vi >= m.N) return;
+  const int n = visit_node(m, vi);
   const GeoPtrs<float>& g = m.g32;
   const unsigned LZ = m.LZ, LW = m.LW;
   const int nl = m.nl, nz = m.nz;
@@ -988,8 +989,9 @@ template <int KV, int NS, bool COMP>
 __global__ void __launch_bounds__(128, (NS == 1 ? 10 : 7)) kf_ratio(DMesh m, FastPtrs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
-  const int n = blockIdx.x * (blockDim.x / kW) + wib;
-  if (n >= m.N) return;
+  const int vi = blockIdx.x * (blockDim.x / kW) + wib;
+  if (vi >= m.N) return;
+  const int n = visit_node(m, vi);
   const GeoPtrs<float>& g = m.g32;
   const unsigned LZ = m.LZ, LW = m.LW;
   const int nl = m.nl;
@@ -1149,8 +1151,9 @@ template <int KV, bool LEAN, bool COMP>
 __global__ void __launch_bounds__(128, LEAN ? 8 : 7) kf_ratio64(DMesh m, FastPtrs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kW - 1);
-  const int n = blockIdx.x * (blockDim.x / kW) + threadIdx.x / kW;
-  if (n >= m.N) return;
+  const int vi = blockIdx.x * (blockDim.x / kW) + threadIdx.x / kW;
+  if (vi >= m.N) return;
+  const int n = visit_node(m, vi);
   V<KV>* sB = reinterpret_cast<V<KV>*>(smem_raw) + (size_t)(threadIdx.x / kW) * 4 * kW;
   const GeoPtrs<float>& g = m.g32;
   const unsigned LZ = m.LZ, LW = m.LW;
@@ -1385,8 +1388,9 @@ template <int KV, int NS, bool DEL, bool COMP, bool RES = false>
 __global__ void __launch_bounds__(128, (NS == 1 ? (COMP || RES ? 8 : 9) : 4)) kf_update(DMesh m, FastPtrs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
-  const int n = blockIdx.x * (blockDim.x / kW) + wib;
-  if (n >= m.N) return;
+  const int vi = blockIdx.x * (blockDim.x / kW) + wib;
+  if (vi >= m.N) return;
+  const int n = visit_node(m, vi);
   const GeoPtrs<float>& g = m.g32;
   const unsigned LZ = m.LZ, LW = m.LW;
   const int nl = m.nl, nz = m.nz;
@@ -1544,8 +1548,9 @@ template <int VER, int KV, int NS>
 __global__ void __launch_bounds__(128, 8) kf_nofct(DMesh m, FastPtrs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
-  const int n = blockIdx.x * (blockDim.x / kW) + wib;
-  if (n >= m.N) return;
+  const int vi = blockIdx.x * (blockDim.x / kW) + wib;
+  if (vi >= m.N) return;
+  const int n = visit_node(m, vi);
   const GeoPtrs<float>& g = m.g32;
   const unsigned LZ = m.LZ, LW = m.LW;
   const int nl = m.nl, nz = m.nz;
@@ -1725,8 +1730,9 @@ __global__ void __launch_bounds__(kVimplWarpsF * kW) kf_vert_impl(DMesh m, FastP
 template <int KV>
 __global__ void __launch_bounds__(256) kf_vert_pcr(DMesh m, FastPtrs a) {
   const int lane = threadIdx.x & (kW - 1);
-  const int n = blockIdx.x * (blockDim.x / kW) + threadIdx.x / kW;
-  if (n >= m.N) return;
+  const int vi = blockIdx.x * (blockDim.x / kW) + threadIdx.x / kW;
+  if (vi >= m.N) return;
+  const int n = visit_node(m, vi);
   const unsigned LZ = m.LZ, LW = m.LW;
   const int k0 = m.ulev[n] - 1, k1 = m.nlev[n] - 2;
   const GeoPtrs<float>& g = m.g32;

@@ -38,8 +38,9 @@ template <int VER, int KV, bool TASEP, bool WESEP, bool COMP>
 __global__ void __launch_bounds__(kLo64Warps * kW, 7) kf_lo64(DMesh m, FastPtrs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kW - 1), wib = threadIdx.x / kW;
-  const int n = blockIdx.x * kLo64Warps + wib;
-  if (n >= m.N) return;
+  const int vi = blockIdx.x * kLo64Warps + wib;
+  if (vi >= m.N) return;
+  const int n = visit_node(m, vi);
   unsigned char* wp = smem_raw + (size_t)wib * lo64_warp_bytes(KV, VER, TASEP);
   V<KV>* sT = reinterpret_cast<V<KV>*>(wp);
   V<KV>* sTA = TASEP ? sT + 64 : sT;

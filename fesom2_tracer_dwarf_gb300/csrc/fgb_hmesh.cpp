@@ -467,7 +467,27 @@ HostMesh* build_analytic(int nx, int ny, int nl, double Lx, double Ly, double de
     m.edge_updn[2 * n + 1] = detail::updn_search(m, e2, x);
   }
   build_tables(m);
+  if (flags & kVisitHilbert) visit_order_hilbert(m);
   return mp;
+}
+
+// Visit order of the edge kernels: by the edge's first-visited node (the
+// lower node index without a node visit order), so that the horizontal,
+// vertical and diagonal edges of a grid row are swept together.
+static void edge_visit_order(HostMesh& m) {
+  const int N = m.N, E = m.E;
+  std::vector<int> rank;
+  if ((int)m.node_order.size() == N) {
+    rank.assign(N, 0);
+    for (int i = 0; i < N; ++i) rank[m.node_order[i]] = i;
+  }
+  auto first = [&](int e) {
+    const int a = m.edges[2 * e], b = m.edges[2 * e + 1];
+    return rank.empty() ? std::min(a, b) : std::min(rank[a], rank[b]);
+  };
+  m.edge_order.resize(E);
+  for (int e = 0; e < E; ++e) m.edge_order[e] = e;
+  std::stable_sort(m.edge_order.begin(), m.edge_order.end(), [&](int a, int b) { return first(a) < first(b); });
 }
 
 void build_tables(HostMesh& m) {
@@ -542,13 +562,7 @@ void build_tables(HostMesh& m) {
     }
     m.cl_ptr[n + 1] = (int)m.cl_node.size();
   }
-  // Visit order of the edge kernels: by lower node, so that the horizontal,
-  // vertical and diagonal edges of a grid row are swept together.
-  m.edge_order.resize(E);
-  for (int e = 0; e < E; ++e) m.edge_order[e] = e;
-  std::stable_sort(m.edge_order.begin(), m.edge_order.end(), [&](int a, int b) {
-    return std::min(m.edges[2 * a], m.edges[2 * a + 1]) < std::min(m.edges[2 * b], m.edges[2 * b + 1]);
-  });
+  edge_visit_order(m);
   // MUSCL gradient windows and edge lengths scaled to metres.
   m.edge_gm.assign((size_t)2 * E, -1);
   m.edge_dxa.assign((size_t)2 * E, 0.0);
@@ -644,8 +658,70 @@ HostMesh* union_meshes(const HostMesh* const* parts, int count, std::string* err
     no += m.N;
     mo += m.M;
   }
+  // each part keeps its own visit order, the parts one after another
+  bool any_order = false;
+  for (int p = 0; p < count; ++p) any_order = any_order || !parts[p]->node_order.empty();
+  if (any_order) {
+    int off = 0;
+    for (int p = 0; p < count; ++p) {
+      const HostMesh& m = *parts[p];
+      for (int i = 0; i < m.N; ++i) u.node_order.push_back(off + (m.node_order.empty() ? i : m.node_order[i]));
+      off += m.N;
+    }
+  }
   build_tables(u);
   return up;
+}
+
+namespace {
+
+// Position of cell (x, y) of a side x side grid (side a power of two) along
+// the Hilbert curve that fills it: two bits per level, the quadrant's place
+// on the curve, with the cell's coordinates reflected and swapped into the
+// quadrant's own frame before the next level (the curve's sub-squares are
+// rotated copies of the whole).
+uint64_t hilbert_index(uint32_t side, uint32_t x, uint32_t y) {
+  uint64_t d = 0;
+  for (uint32_t s = side / 2; s > 0; s /= 2) {
+    const uint32_t rx = (x & s) ? 1u : 0u, ry = (y & s) ? 1u : 0u;
+    d += (uint64_t)s * s * ((3u * rx) ^ ry);
+    if (ry == 0) {
+      if (rx == 1) {
+        x = side - 1 - x;
+        y = side - 1 - y;
+      }
+      std::swap(x, y);
+    }
+  }
+  return d;
+}
+
+}  // namespace
+
+void visit_order_hilbert(HostMesh& m) {
+  const int N = m.N;
+  if (N <= 0) return;
+  double lo[2] = {m.coord[0], m.coord[1]}, hi[2] = {m.coord[0], m.coord[1]};
+  for (int n = 0; n < N; ++n)
+    for (int c = 0; c < 2; ++c) {
+      lo[c] = std::min(lo[c], m.coord[2 * n + c]);
+      hi[c] = std::max(hi[c], m.coord[2 * n + c]);
+    }
+  constexpr uint32_t kSide = 1u << 16;
+  std::vector<std::pair<uint64_t, int>> key(N);
+  for (int n = 0; n < N; ++n) {
+    uint32_t q[2];
+    for (int c = 0; c < 2; ++c) {
+      const double span = hi[c] - lo[c];
+      const double t = span > 0 ? (m.coord[2 * n + c] - lo[c]) / span : 0.0;
+      q[c] = (uint32_t)std::min<double>(kSide - 1, std::max(0.0, t * (kSide - 1)));
+    }
+    key[n] = {hilbert_index(kSide, q[0], q[1]), n};
+  }
+  std::sort(key.begin(), key.end());
+  m.node_order.resize(N);
+  for (int i = 0; i < N; ++i) m.node_order[i] = key[i].second;
+  edge_visit_order(m);
 }
 
 }  // namespace fgb

@@ -59,7 +59,8 @@ struct HostMesh {
   std::vector<int> edge_lev;          // (E,4) nu1,nl1,nu2,nl2 (1-based layers; nl = nlevels-1)
   std::vector<int> edge_gm;           // (E,2) layer window using the triangle gradients, -1 if none
   std::vector<double> edge_dxa;       // (E,2) edge_dxdy(1)*a, edge_dxdy(2)*r_earth
-  std::vector<int> edge_order;        // (E) edges sorted by their lower node (locality of edge sweeps)
+  std::vector<int> edge_order;        // (E) edges sorted by their first-visited node (locality of edge sweeps)
+  std::vector<int> node_order;        // (N) order in which node kernels visit the columns; empty: node index
 };
 
 // Analytic mesh of lib/analytic_mesh.F90:114-829 with its geometry.
@@ -69,6 +70,7 @@ struct HostMesh {
 // the right of node1 -> node2, the orientation of FESOM mesh files).
 constexpr int kClusterFull = 1;
 constexpr int kOrientLeft = 2;
+constexpr int kVisitHilbert = 4;  // node and edge visit order along a Hilbert curve (visit_order_hilbert)
 HostMesh* build_analytic(int nx, int ny, int nl, double Lx, double Ly, double depth, int periodic,
                          int flags, const double* zbar, const int* elem_nlev, std::string* err);
 
@@ -80,6 +82,7 @@ HostMesh* build_analytic(int nx, int ny, int nl, double Lx, double Ly, double de
 constexpr int kFileNoRotation = 1;
 constexpr int kFileEulerDegrees = 2;
 constexpr int kFileCyclic2Pi = 4;
+constexpr int kFileKeepOrder = 8;  // visit nodes and edges in file order (default: along a Hilbert curve)
 HostMesh* build_from_files(const std::string& dir, int flags, std::string* err);
 // The same from arrays laid out as the files are: lonlat (N,2) degrees, elem
 // (M,3), edges and edge_tri (E,2) 1-based (edge_tri <= 0: none), elvls (M),
@@ -90,6 +93,11 @@ HostMesh* build_from_arrays(int N, int M, int E, int Ein, int nl, const double* 
 
 // Derived tables (CSR, cluster, per-edge level windows). Called by the builders.
 void build_tables(HostMesh& m);
+
+// Visit order of the kernels along a Hilbert curve through the nodes'
+// coordinates: node_order, and edge_order by the first-visited node of each
+// edge. Only the order of the work changes, not any index, array or result.
+void visit_order_hilbert(HostMesh& m);
 
 // Recompute the vertical arrays from zbar (the analytic driver's ALE set-up).
 void ale_from_zbar(HostMesh& m);

@@ -418,6 +418,7 @@ HostMesh* build_from_arrays(int N, int M, int E, int Ein, int nl, const double* 
     m.edge_updn[2 * n + 1] = detail::updn_search(m, e2, x);
   }
   build_tables(m);
+  if (!(flags & kFileKeepOrder)) visit_order_hilbert(m);
   return mp;
 }
 

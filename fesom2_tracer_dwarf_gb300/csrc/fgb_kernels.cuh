@@ -709,8 +709,9 @@ template <typename R, int VER, int KC>
 __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_fct_lo(DMesh m, StepPtrs<R> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kWarp - 1), wib = threadIdx.x / kWarp;
-  const int n = blockIdx.x * (blockDim.x / kWarp) + wib;
-  if (n >= m.N) return;
+  const int vi = blockIdx.x * (blockDim.x / kWarp) + wib;
+  if (vi >= m.N) return;
+  const int n = visit_node(m, vi);
   const GeoPtrs<R>& g = GeoSel<R>::get(m);
   const size_t LZ = m.LZ, LW = m.LW;
   const int nl = m.nl, nz = m.nz;
@@ -831,8 +832,9 @@ template <typename R, int KC>
 __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_fct_ratio(DMesh m, StepPtrs<R> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kWarp - 1), wib = threadIdx.x / kWarp;
-  const int n = blockIdx.x * (blockDim.x / kWarp) + wib;
-  if (n >= m.N) return;
+  const int vi = blockIdx.x * (blockDim.x / kWarp) + wib;
+  if (vi >= m.N) return;
+  const int n = visit_node(m, vi);
   const GeoPtrs<R>& g = GeoSel<R>::get(m);
   const size_t LZ = m.LZ, LW = m.LW;
   unsigned char* base = smem_raw + (size_t)wib * warp_smem<R>(ratio_slices(KC), m.LW, kClBytes);
@@ -972,8 +974,9 @@ template <typename R, int KC>
 __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_fct_update(DMesh m, StepPtrs<R> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kWarp - 1), wib = threadIdx.x / kWarp;
-  const int n = blockIdx.x * (blockDim.x / kWarp) + wib;
-  if (n >= m.N) return;
+  const int vi = blockIdx.x * (blockDim.x / kWarp) + wib;
+  if (vi >= m.N) return;
+  const int n = visit_node(m, vi);
   const GeoPtrs<R>& g = GeoSel<R>::get(m);
   const size_t LZ = m.LZ, LW = m.LW;
   const int nz = m.nz, nl = m.nl;
@@ -1103,8 +1106,9 @@ template <typename R, int VER, int KC>
 __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 8 : 4)) k_nofct_update(DMesh m, StepPtrs<R> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & (kWarp - 1), wib = threadIdx.x / kWarp;
-  const int n = blockIdx.x * (blockDim.x / kWarp) + wib;
-  if (n >= m.N) return;
+  const int vi = blockIdx.x * (blockDim.x / kWarp) + wib;
+  if (vi >= m.N) return;
+  const int n = visit_node(m, vi);
   const GeoPtrs<R>& g = GeoSel<R>::get(m);
   const size_t LZ = m.LZ, LW = m.LW;
   const int nl = m.nl, nz = m.nz;

@@ -46,8 +46,9 @@ __global__ void __launch_bounds__(kVimplWarps * 32) k_vert_impl(DMesh m, GeoPtrs
                                                                long long sG, R dt) {
   extern __shared__ __align__(16) unsigned char vimpl_smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int n = blockIdx.x * kVimplWarps + wib;
-  if (n >= m.N) return;
+  const int vi = blockIdx.x * kVimplWarps + wib;
+  if (vi >= m.N) return;
+  const int n = visit_node(m, vi);
   const int LZ = m.LZ, LW = m.LW, S = vimpl_stride(LZ);
   R* sh = reinterpret_cast<R*>(vimpl_smem + (size_t)wib * vimpl_warp_bytes<R>(LZ));
   R *sa = sh, *sb = sh + S, *sc = sh + 2 * S, *sm = sh + 3 * S, *scp = sh + 4 * S;

@@ -25,15 +25,17 @@ class Mesh:
 
     cluster_full and orient_left select the two documented corrections of the
     reference's analytic mesh (see fgb_hmesh_analytic in the C header); the
-    defaults reproduce the reference mesh exactly."""
+    defaults reproduce the reference mesh exactly. hilbert=True makes the
+    kernels visit node columns along a Hilbert curve (the order of the work
+    only; file meshes do so unless keep_order=True)."""
 
     def __init__(self, nx: int, ny: int, nl: int, Lx: float = 100000.0, Ly: float = 100000.0,
                  depth: float = 1000.0, periodic: bool = True, cluster_full: bool = False,
-                 orient_left: bool = False, zbar=None, elem_nlev=None, upload: bool = True):
+                 orient_left: bool = False, zbar=None, elem_nlev=None, upload: bool = True, hilbert: bool = False):
         L = _lib.load()
         self.nx, self.ny, self.Lx, self.Ly, self.depth = nx, ny, Lx, Ly, depth
         self.periodic, self.cluster_full, self.orient_left = periodic, cluster_full, orient_left
-        flags = (1 if cluster_full else 0) | (2 if orient_left else 0)
+        flags = (1 if cluster_full else 0) | (2 if orient_left else 0) | (4 if hilbert else 0)
         zb = None if zbar is None else np.ascontiguousarray(zbar, dtype=np.float64)
         en = None if elem_nlev is None else np.ascontiguousarray(elem_nlev, dtype=np.int32)
         h = ctypes.c_void_p()
@@ -58,15 +60,18 @@ class Mesh:
 
     @classmethod
     def from_files(cls, path: str, rotate: bool = True, euler_degrees: bool = False, cyclic_2pi: bool = False,
-                   upload: bool = True) -> "Mesh":
+                   upload: bool = True, keep_order: bool = False) -> "Mesh":
         """A FESOM mesh directory (nod2d.out, elem2d.out, aux3d.out,
         edgenum.out, edges.out, edge_tri.out, elvls.out, nlvls.out) as one
         partition, set up as lib/oce_mesh.F90 mesh_setup does on the sphere.
         The defaults are the reference's (rotation with the Euler angles
         50/15/-90 used as given, cyclic_length 360 against radians);
-        euler_degrees and cyclic_2pi select FESOM2's namelist handling."""
+        euler_degrees and cyclic_2pi select FESOM2's namelist handling. The
+        kernels visit node columns along a Hilbert curve through the node
+        coordinates (keep_order=True: in file order); numbering, layouts and
+        results are the file's either way."""
         L = _lib.load()
-        flags = (0 if rotate else 1) | (2 if euler_degrees else 0) | (4 if cyclic_2pi else 0)
+        flags = (0 if rotate else 1) | (2 if euler_degrees else 0) | (4 if cyclic_2pi else 0) | (8 if keep_order else 0)
         h = ctypes.c_void_p()
         _lib.check(L.fgb_hmesh_from_files(str(path).encode(), flags, ctypes.byref(h)), "fgb_hmesh_from_files")
         self = cls.__new__(cls)
@@ -80,11 +85,12 @@ class Mesh:
 
     @classmethod
     def from_arrays(cls, lonlat, elem, edges, edge_tri, edgenum, elvls, nlvls, zbar, rotate: bool = True,
-                    euler_degrees: bool = False, cyclic_2pi: bool = False, upload: bool = True) -> "Mesh":
+                    euler_degrees: bool = False, cyclic_2pi: bool = False, upload: bool = True,
+                    keep_order: bool = False) -> "Mesh":
         """The same as ``from_files`` from arrays laid out as the files are
         (``fgb_hmesh_from_arrays``; e.g. ``meshfiles.refine`` output)."""
         L = _lib.load()
-        flags = (0 if rotate else 1) | (2 if euler_degrees else 0) | (4 if cyclic_2pi else 0)
+        flags = (0 if rotate else 1) | (2 if euler_degrees else 0) | (4 if cyclic_2pi else 0) | (8 if keep_order else 0)
         i32 = [np.ascontiguousarray(a, dtype=np.int32) for a in (elem, edges, edge_tri, elvls, nlvls)]
         ll = np.ascontiguousarray(lonlat, dtype=np.float64)
         zb = np.ascontiguousarray(zbar, dtype=np.float64)

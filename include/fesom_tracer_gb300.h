@@ -139,8 +139,12 @@ int fgb_version(void);
  * (lib/analytic_mesh.F90:675-707) by the full lists; FGB_MESH_ORIENT_LEFT
  * swaps an edge's nodes where edge_tri(1) lies to the right of
  * node1 -> node2 (the analytic grid does so for horizontal and vertical
- * edges, lib/analytic_mesh.F90:386-426; FESOM mesh files keep it left). */
-enum { FGB_MESH_CLUSTER_FULL = 1, FGB_MESH_ORIENT_LEFT = 2 };
+ * edges, lib/analytic_mesh.F90:386-426; FESOM mesh files keep it left).
+ * FGB_MESH_VISIT_HILBERT makes the kernels visit node columns along a
+ * Hilbert curve through the node coordinates, and edges by their
+ * first-visited node (the default for file meshes, below); it changes the
+ * order of the work only, never an index, a layout or a result. */
+enum { FGB_MESH_CLUSTER_FULL = 1, FGB_MESH_ORIENT_LEFT = 2, FGB_MESH_VISIT_HILBERT = 4 };
 int fgb_hmesh_analytic(int nx, int ny, int nl, double Lx, double Ly, double depth, int periodic, int flags,
                        const double* zbar, const int* elem_nlev, fgb_hmesh** out);
 /* A FESOM mesh directory (nod2d.out, elem2d.out, aux3d.out, edgenum.out,
@@ -150,8 +154,19 @@ int fgb_hmesh_analytic(int nx, int ny, int nl, double Lx, double Ly, double dept
  * (lib/gen_modules_config.F90:81-88: rotation on, the Euler angles 50/15/-90
  * used as given, cyclic_length = 360 against radian coordinates);
  * FGB_MESH_FILE_NO_ROTATION, FGB_MESH_FILE_EULER_DEGREES and
- * FGB_MESH_FILE_CYCLIC_2PI select FESOM2's namelist handling instead. */
-enum { FGB_MESH_FILE_NO_ROTATION = 1, FGB_MESH_FILE_EULER_DEGREES = 2, FGB_MESH_FILE_CYCLIC_2PI = 4 };
+ * FGB_MESH_FILE_CYCLIC_2PI select FESOM2's namelist handling instead.
+ * The kernels visit the node columns of a file mesh along a Hilbert curve
+ * through the (rotated) node coordinates and each edge with its
+ * first-visited node, whatever the file order (a partitioner's or a mesh
+ * generator's numbering); nodes, edges, elements and every array keep the
+ * file's numbering, and results do not depend on the visit order.
+ * FGB_MESH_FILE_KEEP_ORDER visits them in file order instead. */
+enum {
+  FGB_MESH_FILE_NO_ROTATION = 1,
+  FGB_MESH_FILE_EULER_DEGREES = 2,
+  FGB_MESH_FILE_CYCLIC_2PI = 4,
+  FGB_MESH_FILE_KEEP_ORDER = 8
+};
 int fgb_hmesh_from_files(const char* dir, int flags, fgb_hmesh** out);
 /* The same from arrays laid out as the files are (a host that holds its mesh
  * in memory): lonlat (nod2D,2) degrees, elem (elem2D,3), edges and edge_tri
@@ -263,7 +278,9 @@ typedef struct {
    * compensated. 1: the low-order fluxes of the LO stage; 2: the flux
    * divergence of the update; 4: the FCT +/- sums of the limiter (these only
    * scale each edge's flux, the same factor at both ends, so they never
-   * affect conservation); 7: all plain. The FP64 forms ignore it. */
+   * affect conservation); 7: all plain. With Tlo set, 6 (the LO sums
+   * compensated) keeps the tracer sum to ~1e-12 over 100 steps at a few
+   * per cent of the step's time. The FP64 forms ignore it. */
   int fp32_plain_sums;
   /* FP32 form, optional (NULL: off): the rounding residual of every tracer
    * value, an array of T's layout and strideT. The value of a cell is

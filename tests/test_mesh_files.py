@@ -215,6 +215,49 @@ def test_union_with_a_file_mesh_shifts_its_tables(pi_dir):
         assert np.array_equal(u.get("gradient_sca")[o["elem"]: o["elem"] + p.M], p.get("gradient_sca"))
 
 
+def test_visit_order_follows_a_hilbert_curve(pi_dir, pi_refined_dir):
+    """File meshes: the kernels visit node columns along a Hilbert curve and
+    each edge with its first-visited node; numbering and every mesh array stay
+    the file's (keep_order=True: node index order, edges by lower node)."""
+    from fesom2_tracer_dwarf_gb300.mesh import Mesh
+
+    for d in (pi_dir, pi_refined_dir):
+        h, k = _mesh(d), _mesh(d, keep_order=True)
+        order = h.get("node_order")
+        assert sorted(order.tolist()) == list(range(h.N))
+        assert not np.array_equal(order, np.arange(h.N))
+        assert k.get("node_order").size == 0
+        for name in ("edges", "elem_nodes", "edge_tri", "ne_ptr", "ne_code", "cl_node", "nlevels_nod2D"):
+            assert np.array_equal(h.get(name), k.get(name)), name
+        for name in ("area", "gradient_sca", "edge_cross_dxdy"):
+            assert np.array_equal(h.get(name), k.get(name)), name
+        rank = np.empty(h.N, np.int64)
+        rank[order] = np.arange(h.N)
+        ed = h.get("edges")
+        first = np.minimum(rank[ed[:, 0]], rank[ed[:, 1]])
+        eo = h.get("edge_order")
+        assert sorted(eo.tolist()) == list(range(h.E))
+        assert np.all(np.diff(first[eo]) >= 0)
+        eo_k = k.get("edge_order")
+        assert np.all(np.diff(ed[eo_k].min(axis=1)) >= 0)
+        # consecutive columns along the curve are close: the mean step is a
+        # small multiple of the mean edge length
+        c = h.get("coord")
+        step = np.hypot(*(c[order[1:]] - c[order[:-1]]).T)
+        elen = np.hypot(*(c[ed[:, 0]] - c[ed[:, 1]]).T)
+        assert np.median(step) <= 2.0 * np.median(elen)
+    # analytic meshes keep node index order unless asked
+    assert Mesh(9, 8, 6, periodic=True, upload=False).get("node_order").size == 0
+    hm = Mesh(9, 8, 6, periodic=True, upload=False, hilbert=True)
+    assert sorted(hm.get("node_order").tolist()) == list(range(hm.N))
+    # a union keeps each part's visit order, the parts one after another
+    parts = [_mesh(pi_dir), Mesh(9, 8, 6, periodic=True, upload=False)]
+    u = Mesh.union(parts, upload=False)
+    uo = u.get("node_order")
+    assert np.array_equal(uo[: parts[0].N], parts[0].get("node_order"))
+    assert np.array_equal(uo[parts[0].N:], parts[0].N + np.arange(parts[1].N))
+
+
 def test_layered_flow_is_continuity_consistent(pi_refined_dir):
     """synthetic.layered_flow's W equals diagnose_w of its velocity, and its
     Courant numbers are at most the target."""
@@ -339,6 +382,33 @@ def test_step_on_refined_pi_matches_oracle(oracle_mod, pi_refined_dir, schemes):
             assert np.array_equal(got, vals), f"max |diff| {np.abs(got - vals).max()}"
         else:
             assert np.abs(got - vals).max() <= 1e-5 * max(1.0, np.abs(vals).max())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "fp32", "fp64fast"])
+def test_visit_order_changes_no_result(pi_refined_dir, precision):
+    """The same steps with the Hilbert visit order and with file order give
+    the same values bit for bit, in every form (each column and edge is
+    computed once whatever the order)."""
+    _gpu()
+    from fesom2_tracer_dwarf_gb300 import engine, synthetic
+
+    kw = FLAGS[1]
+    out = []
+    for keep in (False, True):
+        m = _mesh(pi_refined_dir, upload=True, keep_order=keep, **kw)
+        rng = np.random.default_rng(31)
+        u, s, w = synthetic.layered_flow(m, rng, 900.0, cfl=0.5)
+        vel = np.ascontiguousarray(u[:, None, :] * s[None, :, None])
+        T = synthetic.random_field(m, rng, 4)
+        eng = engine.TracerAdvection(m, 4, precision, "MUSCL", "PPM", "FCT", copy_ab=True)
+        eng.set_launch([0] * 9 + [1] if precision == "fp32" else [0] * 12)
+        eng.set_tracers(T)
+        eng.set_velocity(vel, w)
+        eng.step(900.0, 3)
+        torch.cuda.synchronize()
+        out.append(eng.values())
+    assert np.array_equal(out[0], out[1])
 
 
 @pytest.mark.gpu
