@@ -31,6 +31,7 @@ SOURCES = [
     ("fgb_hmesh.cpp", "cxx", []),
     ("fgb_hmesh_files.cpp", "cxx", []),
     ("fgb_capi.cpp", "cxx", []),
+    ("fgb_restart.cpp", "cxx", []),
     ("fgb_api.cu", "nvcc", []),
     ("fgb_step_f64.cu", "nvcc", ["-fmad=false"]),
     ("fgb_step_f64fast.cu", "nvcc", []),

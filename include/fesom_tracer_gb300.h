@@ -36,9 +36,13 @@ extern "C" {
 int tracer_init_mpi(int mpi_comm);
 /* lib/tracer_c_interface.F90:89. Returns 0. */
 int tracer_finalize_mpi(void);
-/* lib/tracer_c_interface.F90:113. Binary restarts are not read by this
- * library: returns -1 with the reference's message when <dir>/np<npes> is
- * missing, and -1 ("restart reader not available") otherwise. */
+/* lib/tracer_c_interface.F90:113. Reads the derived-type binary restarts
+ * <dir>/np1/t_mesh.0, t_partit.0, t_tracer.0 and t_dynamics.0
+ * (read_all_bin_restarts, lib/io_restart_derivedtype.F90:132-199; one
+ * process, so npes = 1): mesh, tracers with their schemes, del_ttf, uv, w,
+ * w_e and (under use_wsplit) w_i. -1 with the reference's message when
+ * <dir>/np<npes> is missing; -1 with the file and field when a record does
+ * not parse or does not fit the mesh. */
 int tracer_init(const char* restart_dir);
 /* lib/tracer_c_interface.F90:163. One do_oce_adv_tra for tracer 1 plus the
  * tendency update; del_ttf accumulates across calls as in the reference. */
@@ -49,8 +53,13 @@ int tracer_get_stats(double* tmin, double* tmax, double* tsum);
 int tracer_get_size(int* nz, int* nn);
 /* lib/tracer_c_interface.F90:280. Copies tracer 1 into values(nz,nn). */
 int tracer_get_values(double* values, int nz, int nn);
-/* lib/tracer_c_interface.F90:308. Restart writing is not provided: marks
- * the system uninitialised and returns -1. */
+/* lib/tracer_c_interface.F90:308. Writes <dir>/np1/t_mesh.0, t_partit.0,
+ * t_tracer.0, t_dynamics.0 and <dir>/meta.time (write_all_bin_restarts,
+ * lib/io_restart_derivedtype.F90:33-125) and marks the system
+ * uninitialised. After tracer_init the records read are written back with
+ * the state's values, valuesAB, schemes, del_ttf, thicknesses and
+ * velocities; otherwise the fields the step does not keep are written
+ * unallocated and the types' scalars at their defaults. */
 int tracer_finalize(const char* output_dir);
 /* lib/tracer_c_interface.F90:356. init + nsteps x (step, stats) + finalize. */
 int tracer_run_workflow(const char* restart_dir, int nsteps, double dt);
@@ -76,7 +85,9 @@ int tracer_set_velocity_zero(int nl, int nod2D, int edge2D);
 int tracer_set_velocity(const double* uv, const double* w, int nl, int nod2D, int edge2D);
 /* lib/tracer_c_interface.F90:749 */
 int tracer_init_complete(void);
-/* lib/tracer_c_interface.F90:769. Restart partitions are not read: -1. */
+/* lib/tracer_c_interface.F90:769. Reads t_mesh.0, t_partit.0 and
+ * t_dynamics.0 of <dir>/np1 (no tracers; the MUSCL tables come from
+ * t_tracer.0 when the directory holds one). */
 int tracer_load_mesh_partition(const char* restart_dir);
 /* lib/tracer_c_interface.F90:830. Reads the FESOM mesh files of mesh_path
  * (nod2d.out, elem2d.out, aux3d.out, edgenum.out, edges.out, edge_tri.out,

@@ -34,7 +34,7 @@ def test_status_codes_before_initialisation(tracer, tmp_path):
         tracer.get_tracer_values()
     assert tracer.initialize(str(tmp_path / "missing")) == -1  # :136-141
     os.makedirs(tmp_path / "np1")
-    assert tracer.initialize(str(tmp_path)) == -1              # reader not provided
+    assert tracer.initialize(str(tmp_path)) == -1              # no restart files in it
     assert L.tracer_load_mesh_from_files(b"/nonexistent/") == -1
     assert tracer.finalize(str(tmp_path)) == -1
     assert L.tracer_run_workflow(str(tmp_path / "missing").encode(), 3, 1.0) == -1
