@@ -67,13 +67,14 @@ REFERENCE_SYMBOLS = [
     "tracer_init_complete", "tracer_load_mesh_partition", "tracer_load_mesh_from_files",
     "tracer_init_ale_arrays", "tracer_init_for_advection",
 ]
-EXTENSION_SYMBOLS = ["tracer_generate_analytic_mesh", "tracer_set_schemes", "tracer_set_precision"]
+EXTENSION_SYMBOLS = ["tracer_generate_analytic_mesh", "tracer_set_schemes", "tracer_set_precision",
+                     "tracer_set_input_checks"]
 ENGINE_SYMBOLS = [
     "fgb_last_error", "fgb_version", "fgb_hmesh_analytic", "fgb_hmesh_from_files", "fgb_hmesh_from_arrays", "fgb_hmesh_union", "fgb_hmesh_free", "fgb_hmesh_sizes", "fgb_hmesh_get",
     "fgb_hmesh_set_vertical", "fgb_mesh_create", "fgb_mesh_free", "fgb_mesh_dims", "fgb_mesh_update_vertical",
     "fgb_workspace_bytes", "fgb_workspace_offsets", "fgb_adv_step", "fgb_adv_stages", "fgb_stats_scratch_bytes",
     "fgb_tracer_stats", "fgb_tracer_stats_grouped", "fgb_last_launch_count", "fgb_static_workspace_bytes", "fgb_adv_step_static",
-    "fgb_probe_fp64",
+    "fgb_probe_fp64", "fgb_check_inputs",
 ]
 
 _lib = None
@@ -117,6 +118,7 @@ def load(build_if_missing: bool = True):
         "fgb_static_workspace_bytes": (ctypes.c_longlong, []),
         "fgb_adv_step_static": (ctypes.c_int, [_vp, ctypes.POINTER(StepDesc), _vp]),
         "fgb_probe_fp64": (ctypes.c_int, [_dp, _vp]),
+        "fgb_check_inputs": (ctypes.c_int, [_vp, ctypes.POINTER(StepDesc), _vp, _ip]),
         "fgb_tracer_stats": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_longlong, ctypes.c_int, _vp, _vp,
                                             _vp]),
         "fgb_tracer_stats_grouped": (ctypes.c_int, [_vp, _vp, ctypes.c_longlong, ctypes.c_int, ctypes.c_int, _vp,

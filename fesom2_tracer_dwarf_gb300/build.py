@@ -41,6 +41,7 @@ SOURCES = [
     ("fgb_fast_kv4.cu", "nvcc", []),
     ("fgb_static_ws.cu", "nvcc", []),
     ("fgb_probe.cu", "nvcc", []),
+    ("fgb_check.cu", "nvcc", []),
 ]
 
 

@@ -66,6 +66,7 @@ struct State {
   bool from_restart = false;
   fgb::restart::Record rmesh, rpartit, rtracer, rdyn;
   int precision = FGB_FP64;
+  bool input_checks = false;  // tracer_set_input_checks
   // device
   void *dT = nullptr, *dTA = nullptr, *dvel = nullptr, *dw = nullptr, *dwe = nullptr, *ddel = nullptr;
   void *dwi = nullptr, *dws = nullptr;
@@ -455,6 +456,19 @@ int tracer_advect_step(double dt) {
   d.del = g.ddel;
   d.workspace = g.dws;
   d.workspace_bytes = g.ws_bytes;
+  if (g.input_checks) {
+    int flags = 0;
+    if (fgb_check_inputs(g.dmesh, &d, nullptr, &flags)) return fail(fgb_last_error());
+    if (flags) {
+      std::string what = "non-finite input values:";
+      const std::pair<int, const char*> names[] = {{FGB_CHECK_T, " values"}, {FGB_CHECK_TA, " valuesAB"},
+                                                   {FGB_CHECK_VEL, " uv"},    {FGB_CHECK_W, " w"},
+                                                   {FGB_CHECK_WE, " w_e"},    {FGB_CHECK_WI, " w_i"}};
+      for (const auto& nm : names)
+        if (flags & nm.first) what += nm.second;
+      return fail(what.c_str());
+    }
+  }
   if (fgb_adv_step(g.dmesh, &d, nullptr)) return fail(fgb_last_error());
   if (cudaDeviceSynchronize() != cudaSuccess) return fail("device error during the step");
   g.values_on_device = true;
@@ -836,6 +850,11 @@ int tracer_set_schemes(int tracer_id, const char* hor, const char* ver, const ch
   t.lim = c;
   t.ph = ph;
   t.pv = pv;
+  return 0;
+}
+
+int tracer_set_input_checks(int on) {
+  g.input_checks = on != 0;
   return 0;
 }
 

@@ -68,6 +68,7 @@ class FESOMTracerAdvection:
             "tracer_set_schemes": (ctypes.c_int, [ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p,
                                                   ctypes.c_char_p, ctypes.c_double, ctypes.c_double]),
             "tracer_set_precision": (ctypes.c_int, [ctypes.c_int]),
+            "tracer_set_input_checks": (ctypes.c_int, [ctypes.c_int]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -167,6 +168,10 @@ class FESOMTracerAdvection:
 
     def set_precision(self, precision="fp64"):
         return self.lib.tracer_set_precision({"fp64": 0, "fp32": 1}[precision])
+
+    def set_input_checks(self, on=True):
+        """Check before every step that its inputs are finite (tracer_set_input_checks)."""
+        return self.lib.tracer_set_input_checks(int(bool(on)))
 
     def init_ale_arrays(self):
         return self.lib.tracer_init_ale_arrays()

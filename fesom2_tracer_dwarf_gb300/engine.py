@@ -294,6 +294,20 @@ class TracerAdvection:
             _lib.check(L.fgb_adv_stages(self.mesh.handle, ctypes.byref(d), stages, stream), "fgb_adv_stages")
             self.launches += L.fgb_last_launch_count()
 
+    CHECK_BITS = {"T": 1, "TA": 2, "vel": 4, "w": 8, "we": 16, "wi": 32, "Tlo": 64}
+
+    def check_inputs(self, dt: float = 1.0):
+        """Names of the arrays a step would read that hold a NaN or an
+        infinity (fgb_check_inputs: one device reduction per array, padding
+        layers included); an empty list when every value is finite."""
+        L = _lib.load()
+        d = self._desc(dt)
+        flags = ctypes.c_int()
+        stream = ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+        _lib.check(L.fgb_check_inputs(self.mesh.handle, ctypes.byref(d), stream, ctypes.byref(flags)),
+                   "fgb_check_inputs")
+        return [k for k, bit in self.CHECK_BITS.items() if flags.value & bit]
+
     def run_host(self, host_in, host_out, dt: float, nsteps: int = 1, copy_streams: int = 1):
         """Advance independent batches of tracer fields that live in host
         memory: batch i is copied to the device from ``host_in[i]``, advanced

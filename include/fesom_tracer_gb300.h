@@ -112,6 +112,11 @@ int tracer_set_schemes(int tracer_id, const char* hor, const char* ver, const ch
                        double pv);
 /* Device form of the step: 0 = FP64 (default), 1 = FP32. */
 int tracer_set_precision(int precision);
+/* on != 0: every tracer_advect_step first checks that its inputs (values,
+ * valuesAB, uv, w, w_e, w_i) are finite on the device (fgb_check_inputs)
+ * and returns -1 with the arrays named instead of stepping. Off by default,
+ * as in the reference, which carries NaN and Inf through the step. */
+int tracer_set_input_checks(int on);
 
 /* ===================================================================== */
 /* 2. Engine interface                                                    */
@@ -348,6 +353,24 @@ int fgb_last_launch_count(void);
 #define FGB_STATIC_WORKSPACE_BYTES (64LL * 1024 * 1024)
 long long fgb_static_workspace_bytes(void);
 int fgb_adv_step_static(const fgb_mesh* m, const fgb_step_desc* d, void* stream);
+
+/* No counterpart in the reference: checks that every value of the arrays the
+ * step described by d reads is finite (T and TA per tracer group, Tlo, vel,
+ * w, we, wi; padding layers included, which the step requires finite). One
+ * device reduction per array into a status word; synchronises `stream`.
+ * *flags_out: 0 when all are finite, else the FGB_CHECK_* bits of the arrays
+ * that hold a NaN or an infinity. Returns 0, or -1 with a message on a bad
+ * argument or a CUDA error. */
+enum {
+  FGB_CHECK_T = 1,
+  FGB_CHECK_TA = 2,
+  FGB_CHECK_VEL = 4,
+  FGB_CHECK_W = 8,
+  FGB_CHECK_WE = 16,
+  FGB_CHECK_WI = 32,
+  FGB_CHECK_TLO = 64
+};
+int fgb_check_inputs(const fgb_mesh* m, const fgb_step_desc* d, void* stream, int* flags_out);
 
 /* No counterpart in the reference: the current device's FP64 rates, the bound
  * of the FP64 forms. out3 receives fused multiply-add TFLOP/s, IEEE double

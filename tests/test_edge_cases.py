@@ -130,3 +130,76 @@ def test_stats_with_nan(oracle_mod, precision, V):
             assert np.isnan(st[t, 2]) and st[t, 3] == 2
         else:
             assert abs(st[t, 2] - ref[2]) <= 1e-12 * abs(ref[2])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,V,residual", [("fp64", 1, False), ("fp32", 4, True), ("fp32", 2, False)])
+def test_input_check_names_non_finite_arrays(precision, V, residual):
+    """fgb_check_inputs (engine.check_inputs): one device reduction per
+    array; every array finite -> [], a NaN or an infinity planted in one
+    input -> that array's name only. NaN and Inf are data, not faults: the
+    step itself would carry them through, as the reference's does."""
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA GPU")
+    from fesom2_tracer_dwarf_gb300 import engine, synthetic
+    from fesom2_tracer_dwarf_gb300.mesh import Mesh
+
+    m = Mesh(14, 12, 9, periodic=True, orient_left=True)
+    rng = np.random.default_rng(17)
+    vel, w = synthetic.streamfunction_flow(m, rng, 300.0, cfl=0.4)
+    T = synthetic.random_field(m, rng, 4)
+    kw = dict(tracer_vec=V, residual=residual) if precision == "fp32" else {}
+    e = engine.TracerAdvection(m, 4, precision, "MUSCL", "PPM", "FCT", **kw)
+    e.set_tracers(T)
+    e.set_velocity(vel, w)
+    assert e.check_inputs() == []
+    for field, bad in (("T", np.nan), ("vel", np.inf), ("w", -np.inf)):
+        if field == "T":
+            T2 = T.copy()
+            T2[3, 5, 2] = bad  # the last tracer of the last group
+            e.set_tracers(T2)
+        elif field == "vel":
+            v2 = vel.copy()
+            v2[7, 1, 0] = bad
+            e.set_velocity(v2, w)
+        else:
+            w2 = w.copy()
+            w2[4, 3] = bad
+            e.set_velocity(vel, w2)
+        assert e.check_inputs() == [field], field
+        e.set_tracers(T)
+        e.set_velocity(vel, w)
+        assert e.check_inputs() == []
+    if residual:
+        e.Tlo.view(-1)[123] = float("nan")
+        assert e.check_inputs() == ["Tlo"]
+
+
+@pytest.mark.gpu
+def test_cabi_input_checks_refuse_non_finite_values():
+    """tracer_set_input_checks(1): tracer_advect_step returns -1 and names
+    the array instead of stepping; off (the reference's behaviour) the step
+    runs and the NaN propagates."""
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA GPU")
+    from fesom2_tracer_dwarf_gb300.demo_tracer import FESOMTracerAdvection
+
+    t = FESOMTracerAdvection(verbose=False)
+    t.cleanup()
+    try:
+        assert t.generate_analytic_mesh(10, 9, 6, periodic=True) == 0
+        nz, N = 5, t.nod2D
+        assert t.allocate_tracers(1, 6, N) == 0
+        v = np.asfortranarray(np.ones((nz, N)))
+        v[2, 7] = np.nan
+        assert t.set_values(1, v) == 0
+        assert t.set_velocity_zero() == 0
+        assert t.init_for_advection() == 0 and t.init_complete() == 0
+        assert t.set_input_checks(True) == 0
+        assert t.advect_step(10.0) == -1
+        assert "values" in t.lib.fgb_last_error().decode()
+        assert t.set_input_checks(False) == 0
+        assert t.advect_step(10.0) == 0
+        assert np.isnan(t.get_tracer_values()[2, 7])
+    finally:
+        t.cleanup()
