@@ -63,7 +63,7 @@ WORKLOADS = {
     # Closed ragged basin: 1024^2 with seeded bathymetry (8..64 layers), walls,
     # MUSCL-FCT + PPM; FP32 form against plain FP64 over 100 steps.
     "closed_1024": dict(kind="closed", nx=1025, L=1024e3, nz=64, min_layers=8, K=2, hor="MUSCL", ver="PPM",
-                        lim="FCT", dt=400.0, precision="fp32", compare_fp64=True, report_steps=100),
+                        lim="FCT", dt=400.0, precision="fp32", compare_fp64=True, report_steps=100, residual=True),
     # An unstructured global ocean mesh: the reference's pi mesh (coasts,
     # ragged bottom, 47 layers) with every triangle split into four 5 times
     # (3.0 M nodes, 9.0 M edges); FP32 form against plain FP64.
@@ -397,11 +397,11 @@ def build_case(cfg, precision, device, seed=20260301):
     from fesom2_tracer_dwarf_gb300.mesh import Mesh
 
     sch = (cfg["hor"], cfg["ver"], cfg["lim"])
+    res = bool(cfg.get("residual")) and precision == "fp32"  # the FP32 rounding residual
     if cfg["kind"] == "flat":
         m, vel, w, T0 = _flat_part(cfg["nx"] - 1, cfg["nz"], precision, device, cfg["dt"], 0.4, cfg["K"], seed)
         eng = TracerAdvection(m, cfg["K"], precision, *sch, copy_ab=True, device=device,
-                              tracer_vec=cfg.get("tracer_vec") if precision == "fp32" else None,
-                              residual=bool(cfg.get("residual")) and precision == "fp32")
+                              tracer_vec=cfg.get("tracer_vec") if precision == "fp32" else None, residual=res)
         eng.load_padded(T=T0, vel=vel, w=w)
         if cfg.get("wsplit"):
             c = float(w.abs().max()) * cfg["wsplit"]
@@ -411,7 +411,7 @@ def build_case(cfg, precision, device, seed=20260301):
     elif cfg["kind"] == "files":
         m, vel, w, T0 = _files_case(cfg, precision, device, seed)
         eng = TracerAdvection(m, cfg["K"], precision, *sch, copy_ab=True, device=device,
-                              tracer_vec=cfg.get("tracer_vec") if precision == "fp32" else None)
+                              tracer_vec=cfg.get("tracer_vec") if precision == "fp32" else None, residual=res)
         eng.load_padded(T=T0, vel=vel, w=w)
         del vel, w, T0
     elif cfg["kind"] == "closed":
@@ -424,7 +424,7 @@ def build_case(cfg, precision, device, seed=20260301):
         T = np.stack([synthetic.gaussian_T(m, rng), synthetic.salinity(m, rng)] +
                      [synthetic.passive_blob(m, rng) for _ in range(cfg["K"] - 2)])
         eng = TracerAdvection(m, cfg["K"], precision, *sch, copy_ab=True, device=device,
-                              tracer_vec=cfg.get("tracer_vec") if precision == "fp32" else None)
+                              tracer_vec=cfg.get("tracer_vec") if precision == "fp32" else None, residual=res)
         eng.set_velocity(vel, w)
         eng.set_tracers(T)
         del vel, w, T
@@ -442,7 +442,7 @@ def build_case(cfg, precision, device, seed=20260301):
         T0 = torch.cat([_pad_dim(t, 2, m.LZ) for t in Ts], dim=1)
         del vels, ws, Ts
         eng = TracerAdvection(m, cfg["K"], precision, *sch, copy_ab=True, device=device,
-                              tracer_vec=cfg.get("tracer_vec") if precision == "fp32" else None)
+                              tracer_vec=cfg.get("tracer_vec") if precision == "fp32" else None, residual=res)
         eng.load_padded(T=T0, vel=vel, w=w)
     return m, eng, eng.T.clone()
 
