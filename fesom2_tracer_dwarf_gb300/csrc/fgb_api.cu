@@ -450,7 +450,18 @@ namespace {
 constexpr int kStatBlocks = 1024;
 constexpr int kStatThreads = 256;
 
-// Tracer t of a batch in groups of KV (KV = 1: one tracer per stride).
+// Sum with its rounding error carried (TwoSum, Knuth): s + c is the exact
+// sum of the terms added so far up to the rounding of c.
+__device__ __forceinline__ void comp_add(double& s, double& c, double x) {
+  const double t = s + x, bp = t - s;
+  c += (s - (t - bp)) + (x - bp);
+  s = t;
+}
+
+// Tracer t of a batch in groups of KV (KV = 1: one tracer per stride): min,
+// max, compensated sum and NaN count per blockIdx.y; each block's partial
+// sum is s + c rounded once (the final sum adds the blocks' partial sums
+// compensated again).
 template <typename R>
 __global__ void k_stats_partial(const R* __restrict__ T, long long sT, int KV, int N, int nz, int LZ,
                                 double* __restrict__ part) {
@@ -459,7 +470,7 @@ __global__ void k_stats_partial(const R* __restrict__ T, long long sT, int KV, i
   const long long total = (long long)N * nz;
   const long long per = (total + gridDim.x - 1) / gridDim.x;
   const long long lo = blockIdx.x * per, hi = min(total, lo + per);
-  double mn = INFINITY, mx = -INFINITY, sm = 0.0, nan = 0.0;
+  double mn = INFINITY, mx = -INFINITY, sm = 0.0, sc = 0.0, nan = 0.0;
   for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
     const long long n = i / nz, k = i - n * nz;
     const double v = (double)base[(n * LZ + k) * KV];
@@ -470,35 +481,43 @@ __global__ void k_stats_partial(const R* __restrict__ T, long long sT, int KV, i
     }
     mn = fmin(mn, v);
     mx = fmax(mx, v);
-    sm += v;
+    comp_add(sm, sc, v);
   }
-  __shared__ double s[4][kStatThreads];
+  __shared__ double s[5][kStatThreads];
   s[0][threadIdx.x] = mn; s[1][threadIdx.x] = mx; s[2][threadIdx.x] = sm; s[3][threadIdx.x] = nan;
+  s[4][threadIdx.x] = sc;
   __syncthreads();
   for (int w = kStatThreads / 2; w > 0; w >>= 1) {
     if (threadIdx.x < w) {
       s[0][threadIdx.x] = fmin(s[0][threadIdx.x], s[0][threadIdx.x + w]);
       s[1][threadIdx.x] = fmax(s[1][threadIdx.x], s[1][threadIdx.x + w]);
-      s[2][threadIdx.x] += s[2][threadIdx.x + w];
+      double a = s[2][threadIdx.x], c = s[4][threadIdx.x] + s[4][threadIdx.x + w];
+      comp_add(a, c, s[2][threadIdx.x + w]);
+      s[2][threadIdx.x] = a;
+      s[4][threadIdx.x] = c;
       s[3][threadIdx.x] += s[3][threadIdx.x + w];
     }
     __syncthreads();
   }
-  if (threadIdx.x < 4) part[((size_t)t * gridDim.x + blockIdx.x) * 4 + threadIdx.x] = s[threadIdx.x][0];
+  if (threadIdx.x < 4)
+    part[((size_t)t * gridDim.x + blockIdx.x) * 4 + threadIdx.x] =
+        threadIdx.x == 2 ? (isinf(s[2][0]) ? s[2][0] : s[2][0] + s[4][0]) : s[threadIdx.x][0];
 }
 
 __global__ void k_stats_final(const double* __restrict__ part, int nblk, double* __restrict__ out) {
   const int t = blockIdx.x;
   if (threadIdx.x != 0) return;
-  double mn = INFINITY, mx = -INFINITY, sm = 0.0, nan = 0.0;
+  double mn = INFINITY, mx = -INFINITY, sm = 0.0, sc = 0.0, nan = 0.0;
   for (int b = 0; b < nblk; ++b) {
     const double* p = part + ((size_t)t * nblk + b) * 4;
     mn = fmin(mn, p[0]);
     mx = fmax(mx, p[1]);
-    sm += p[2];
+    comp_add(sm, sc, p[2]);
     nan += p[3];
   }
-  out[4 * t] = mn; out[4 * t + 1] = mx; out[4 * t + 2] = sm; out[4 * t + 3] = nan;
+  // a NaN anywhere makes the sum NaN, as the plain sum; an infinite sum stays
+  // infinite (its compensation term is NaN: inf - inf)
+  out[4 * t] = mn; out[4 * t + 1] = mx; out[4 * t + 2] = isinf(sm) ? sm : sm + sc; out[4 * t + 3] = nan;
 }
 }  // namespace
 }  // namespace fgb

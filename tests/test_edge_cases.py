@@ -149,7 +149,7 @@ def test_input_check_names_non_finite_arrays(precision, V, residual):
     vel, w = synthetic.streamfunction_flow(m, rng, 300.0, cfl=0.4)
     T = synthetic.random_field(m, rng, 4)
     kw = dict(tracer_vec=V, residual=residual) if precision == "fp32" else {}
-    e = engine.TracerAdvection(m, 4, precision, "MUSCL", "PPM", "FCT", **kw)
+    e = engine.TracerAdvection(m, 4, precision, "MUSCL", "PPM", "FCT", copy_ab=True, **kw)
     e.set_tracers(T)
     e.set_velocity(vel, w)
     assert e.check_inputs() == []
@@ -173,6 +173,13 @@ def test_input_check_names_non_finite_arrays(precision, V, residual):
     if residual:
         e.Tlo.view(-1)[123] = float("nan")
         assert e.check_inputs() == ["Tlo"]
+    # a separate valuesAB array (frozen AB level) is checked as well
+    f = engine.TracerAdvection(m, 4, precision, "MUSCL", "PPM", "FCT", **kw)
+    T2 = T.copy()
+    T2[0, 1, 1] = np.nan
+    f.set_tracers(T2)
+    f.set_velocity(vel, w)
+    assert f.check_inputs() == ["T", "TA"]
 
 
 @pytest.mark.gpu
@@ -203,3 +210,32 @@ def test_cabi_input_checks_refuse_non_finite_values():
         assert np.isnan(t.get_tracer_values()[2, 7])
     finally:
         t.cleanup()
+
+
+@pytest.mark.gpu
+def test_stats_sum_is_compensated():
+    """The statistics' sum is a compensated FP64 sum: on values 1e10 + u,
+    u in [0, 1), whose plain running sum loses about 1e-10 of its value, it
+    agrees with the exactly rounded sum (math.fsum) to a few units in the
+    last place; an infinite value gives an infinite sum, a NaN a NaN sum."""
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA GPU")
+    import math
+
+    from fesom2_tracer_dwarf_gb300 import engine
+    from fesom2_tracer_dwarf_gb300.mesh import Mesh
+
+    m = Mesh(130, 130, 33, periodic=True)
+    rng = np.random.default_rng(23)
+    T = 1e10 + rng.random((2, m.N, m.nz))
+    eng = engine.TracerAdvection(m, 2, "fp64")
+    eng.set_tracers(T)
+    st = eng.stats()
+    for t in range(2):
+        exact = math.fsum(T[t].ravel())
+        assert abs(st[t, 2] - exact) <= 4 * math.ulp(exact), (st[t, 2], exact)
+    T[0, 5, 3] = np.inf
+    T[1, 9, 1] = np.nan
+    eng.set_tracers(T)
+    st = eng.stats()
+    assert st[0, 2] == np.inf and np.isnan(st[1, 2]) and st[1, 3] == 1
