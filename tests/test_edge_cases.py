@@ -166,7 +166,9 @@ def test_input_check_names_non_finite_arrays(precision, V, residual):
             w2 = w.copy()
             w2[4, 3] = bad
             e.set_velocity(vel, w2)
-        assert e.check_inputs() == [field], field
+        # a NaN value set with the residual kept also makes its residual NaN (value - float(value))
+        want = ["T", "Tlo"] if (field == "T" and residual) else [field]
+        assert e.check_inputs() == want, field
         e.set_tracers(T)
         e.set_velocity(vel, w)
         assert e.check_inputs() == []
@@ -179,7 +181,7 @@ def test_input_check_names_non_finite_arrays(precision, V, residual):
     T2[0, 1, 1] = np.nan
     f.set_tracers(T2)
     f.set_velocity(vel, w)
-    assert f.check_inputs() == ["T", "TA"]
+    assert f.check_inputs() == (["T", "TA", "Tlo"] if residual else ["T", "TA"])
 
 
 @pytest.mark.gpu
