@@ -301,3 +301,26 @@ def test_steps_continue_across_a_restart(tracer, tmp_path, schemes):
     assert np.array_equal(got, want), f"max |diff| {np.abs(got - want).max()}"
     tr = parse_tracer(read_record(tmp_path / "np1" / "t_tracer.0"))
     assert tr["work%del_ttf"].any()  # the accumulated tendency was carried over
+
+
+@pytest.mark.gpu
+def test_run_workflow_from_a_restart(tracer, tmp_path):
+    """tracer_run_workflow(dir, nsteps, dt) (lib/tracer_c_interface.F90:356-388):
+    tracer_init from dir, nsteps steps with statistics, tracer_finalize back
+    into dir; the restart it leaves equals stepping the same state by hand."""
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA GPU")
+    _state(tracer, nx=12, ny=11, nl=8, schemes=("MFCT", "PPM", "FCT"), seed=13)
+    a, b = tmp_path / "a", tmp_path / "b"
+    assert tracer.finalize(str(a)) == 0
+    shutil.copytree(a, b)
+    tracer.cleanup()
+    assert tracer.lib.tracer_run_workflow(str(a).encode(), 4, 120.0) == 0
+    tracer.cleanup()
+    assert tracer.initialize(str(b)) == 0
+    for _ in range(4):
+        assert tracer.advect_step(120.0) == 0
+    assert tracer.finalize(str(b)) == 0
+    ta, tb = (parse_tracer(read_record(d / "np1" / "t_tracer.0")) for d in (a, b))
+    assert np.array_equal(ta["data(1)%values"], tb["data(1)%values"])
+    assert np.array_equal(ta["work%del_ttf"], tb["work%del_ttf"]) and ta["work%del_ttf"].any()
