@@ -12,8 +12,9 @@
 
 The FP64 form must equal the oracle bit for bit (do_oce_adv_tra,
 lib/oce_adv_tra_driver.F90:23-294, in the reference's evaluation order); the
-fast FP64 form is held to 1e-12 and the FP32 form to the FP32 bar of the other
-tests (relative max-norm 1e-5) against the same oracle run. The oracle runs on every host core (its loops
+fast FP64 form is held to 1e-12 and the FP32 form (FP32 storage, and each
+value with its rounding residual) to the FP32 bar of the other tests
+(relative max-norm 1e-5) against the same oracle run. The oracle runs on every host core (its loops
 are threaded without changing any result).
 """
 import os
@@ -72,10 +73,8 @@ def _divergent(m, synthetic, rng, vel, dt, frac=0.3, efold=500.0, cfl=0.4):
     return (u2 * scale)[:, None, :] * s[None, :, None], w * scale
 
 
-def _run(O, om, m, engine, vel, w, T, sch, steps, dt, precision):
-    vals = np.ascontiguousarray(T.copy())
-    vab = vals.copy()
-    eng = engine.TracerAdvection(m, T.shape[0], precision, *sch, copy_ab=True)
+def _run(O, om, m, engine, vel, w, T, sch, steps, dt, precision, residual=False):
+    eng = engine.TracerAdvection(m, T.shape[0], precision, *sch, copy_ab=True, residual=residual)
     eng.set_tracers(T)
     eng.set_velocity(vel, w)
     eng.step(dt, steps)
@@ -116,10 +115,11 @@ def test_config2_512_fp64_bit_exact(config2, hor, flow):
     got = _run(O, om, m, engine, vel, w, T, sch, steps, dt, "fp64")
     err = float(np.abs(got - vals).max())
     assert err == 0.0, f"512^2 x 48 {hor}-FCT/QR4C {flow}: max |GPU - oracle| = {err}"
-    got32 = _run(O, om, m, engine, vel, w, T, sch, steps, dt, "fp32")
-    for t in range(2):
-        rel = float(np.abs(got32[t] - vals[t]).max() / np.abs(vals[t]).max())
-        assert rel <= REL_TOL_FP32, f"FP32 form, tracer {t}: {rel:.3g}"
+    for residual in (False, True):
+        got32 = _run(O, om, m, engine, vel, w, T, sch, steps, dt, "fp32", residual)
+        for t in range(2):
+            rel = float(np.abs(got32[t] - vals[t]).max() / np.abs(vals[t]).max())
+            assert rel <= REL_TOL_FP32, f"FP32 form (residual={residual}), tracer {t}: {rel:.3g}"
     gotf = _run(O, om, m, engine, vel, w, T, sch, steps, dt, "fp64fast")
     for t in range(2):
         rel = float(np.abs(gotf[t] - vals[t]).max() / np.abs(vals[t]).max())
@@ -150,7 +150,8 @@ def test_config3_closed_1024_fp64_bit_exact(pkg, oracle_mod):
     wet = np.arange(nz)[None, :] < lev[:, None]
     err = float(np.abs(got - vals)[:, wet].max())
     assert err == 0.0, f"1024^2 closed MUSCL-FCT/PPM: max |GPU - oracle| = {err}"
-    got32 = _run(O, om, m, engine, vel, w, T, sch, 1, dt, "fp32")
-    for t in range(2):
-        rel = float(np.abs(got32[t] - vals[t])[wet].max() / np.abs(vals[t][wet]).max())
-        assert rel <= REL_TOL_FP32, f"FP32 form, tracer {t}: {rel:.3g}"
+    for residual in (False, True):
+        got32 = _run(O, om, m, engine, vel, w, T, sch, 1, dt, "fp32", residual)
+        for t in range(2):
+            rel = float(np.abs(got32[t] - vals[t])[wet].max() / np.abs(vals[t][wet]).max())
+            assert rel <= REL_TOL_FP32, f"FP32 form (residual={residual}), tracer {t}: {rel:.3g}"

@@ -74,14 +74,16 @@ def test_fp32_single_step_all_schemes(pkg, oracle_mod, meshname, hor, ver, lim):
     vab = np.ascontiguousarray(TA.copy())
     W = O.Work(om)
     O.analytic_step(om, W, dt, vel, w, vals, vab, [(hor, ver, lim, 0.7, 0.6)] * K)
-    eng = engine.TracerAdvection(m, K, "fp32", hor, ver, lim, ph=0.7, pv=0.6)
-    assert eng.V == 4
-    eng.set_tracers(T, TA)
-    eng.set_velocity(vel, w)
-    eng.step(dt)
-    torch.cuda.synchronize()
-    err = _rel(eng.values(), vals)
-    assert err <= REL_TOL, f"{meshname} {hor}/{ver}/{lim}: relative max error {err:.3g}"
+    # FCT: also with each value's FP32 rounding residual (the benchmark's form)
+    for residual in ((False, True) if lim == "FCT" else (False,)):
+        eng = engine.TracerAdvection(m, K, "fp32", hor, ver, lim, ph=0.7, pv=0.6, residual=residual)
+        assert eng.V == 4 and eng.residual == residual
+        eng.set_tracers(T, TA)
+        eng.set_velocity(vel, w)
+        eng.step(dt)
+        torch.cuda.synchronize()
+        err = _rel(eng.values(), vals)
+        assert err <= REL_TOL, f"{meshname} {hor}/{ver}/{lim} residual={residual}: relative max error {err:.3g}"
 
 
 @pytest.mark.parametrize("K,V", [(1, 1), (2, 2), (3, 1), (6, 2), (8, 4), (4, 1), (4, 2)])
@@ -132,14 +134,17 @@ def test_fp32_multistep(pkg, oracle_mod, case):
     vals = np.ascontiguousarray(T.copy())
     vab = vals.copy()
     W = O.Work(om)
-    eng = engine.TracerAdvection(m, K, "fp32", *sch, copy_ab=copy_ab)
-    eng.set_tracers(T)
-    eng.set_velocity(vel, w)
+    engs = [engine.TracerAdvection(m, K, "fp32", *sch, copy_ab=copy_ab, residual=r) for r in (False, True)]
+    for eng in engs:
+        eng.set_tracers(T)
+        eng.set_velocity(vel, w)
     for _ in range(20):
         O.analytic_step(om, W, dt, vel, w, vals, vab, [sch] * K, copy_ab=copy_ab)
-        eng.step(dt)
+        for eng in engs:
+            eng.step(dt)
     torch.cuda.synchronize()
-    assert _rel(eng.values(), vals) <= REL_TOL
+    for eng in engs:
+        assert _rel(eng.values(), vals) <= REL_TOL, f"residual={eng.residual}"
 
 
 def test_fp32_workspace_views_follow_groups(pkg, oracle_mod):
