@@ -1440,29 +1440,40 @@ __global__ void __launch_bounds__(128, (NS == 1 ? (COMP || RES ? 8 : 9) : 4)) kf
     const float* __restrict__ Lg = a.lo + gi * a.gN;
     float* __restrict__ Tg = a.T + gi * a.gT;
     float* del = DEL ? a.del + gi * a.gN : nullptr;
-    // passes below the column's deepest layer change nothing: skipped
+    // passes below the column's deepest layer change nothing: skipped; in the
+    // last pass the lanes below the column load, compute and store nothing
+    // (their values, and valuesAB there, keep what they hold)
     const unsigned lz_col = min(LZ, (unsigned)max(nzmax - 1, 1));
     for (unsigned base = 0; base < lz_col; base += kW * NS) {
       unsigned kk[NS];
+      bool act[NS];
       V<KV> dh[NS], dc[NS], rpn[NS], rmn[NS], lo[NS], Tn[NS], d0[NS], tl[NS];
       float av[NS], hnn[NS], hn[NS];
 #pragma unroll
       for (int i = 0; i < NS; ++i) {
         const unsigned k = base + lane + kW * i;
         kk[i] = k < LZ ? k : LZ - 1;
+        act[i] = (int)k + 1 >= nzmin && (int)k + 1 <= nzmax - 1;  // the column's layers (k < nz <= LZ)
         const unsigned kr = kk[i] < (unsigned)nz ? kk[i] : (unsigned)nz - 1;
         dh[i] = splat<KV>(0.f);
         dc[i] = splat<KV>(0.f);
         rpn[i] = sRp[kr];
         rmn[i] = sRm[kr];
         // the final update's inputs travel with the first neighbours
-        lo[i] = ld<KV>(Lg, n * LZ + kk[i]);
-        Tn[i] = ld<KV>(Tg, n * LZ + kk[i]);
-        d0[i] = DEL ? ld<KV>(del, n * LZ + kk[i]) : splat<KV>(0.f);
-        tl[i] = RES ? ld<KV>(a.Tlo + gi * a.gT, n * LZ + kk[i]) : splat<KV>(0.f);
-        av[i] = g.areasvol[n * LZ + kk[i]];
-        hnn[i] = g.hnode_new[n * LZ + kk[i]];
-        hn[i] = g.hnode[n * LZ + kk[i]];
+        lo[i] = splat<KV>(0.f);
+        Tn[i] = lo[i];
+        d0[i] = lo[i];
+        tl[i] = lo[i];
+        av[i] = hnn[i] = hn[i] = 1.f;
+        if (act[i]) {
+          lo[i] = ld<KV>(Lg, n * LZ + kk[i]);
+          Tn[i] = ld<KV>(Tg, n * LZ + kk[i]);
+          if (DEL) d0[i] = ld<KV>(del, n * LZ + kk[i]);
+          if (RES) tl[i] = ld<KV>(a.Tlo + gi * a.gT, n * LZ + kk[i]);
+          av[i] = g.areasvol[n * LZ + kk[i]];
+          hnn[i] = g.hnode_new[n * LZ + kk[i]];
+          hn[i] = g.hnode[n * LZ + kk[i]];
+        }
       }
 #pragma unroll 2
       for (int j = 0; j < nb.deg; ++j) {
@@ -1472,9 +1483,14 @@ __global__ void __launch_bounds__(128, (NS == 1 ? (COMP || RES ? 8 : 9) : 4)) kf
         V<KV> f[NS], rpo[NS], rmo[NS];
 #pragma unroll
         for (int i = 0; i < NS; ++i) {
-          f[i] = ld<KV>(Fg, ed * LZ + kk[i]);
-          rpo[i] = ld<KV>(Rg, 2 * (q.y * LZ + kk[i]));
-          rmo[i] = ld<KV>(Rg, 2 * (q.y * LZ + kk[i]) + 1);
+          f[i] = splat<KV>(0.f);
+          rpo[i] = f[i];
+          rmo[i] = f[i];
+          if (act[i]) {
+            f[i] = ld<KV>(Fg, ed * LZ + kk[i]);
+            rpo[i] = ld<KV>(Rg, 2 * (q.y * LZ + kk[i]));
+            rmo[i] = ld<KV>(Rg, 2 * (q.y * LZ + kk[i]) + 1);
+          }
         }
 #pragma unroll
         for (int i = 0; i < NS; ++i) {
@@ -1496,10 +1512,9 @@ __global__ void __launch_bounds__(128, (NS == 1 ? (COMP || RES ? 8 : 9) : 4)) kf
 #pragma unroll
       for (int i = 0; i < NS; ++i) {
         const unsigned k = base + lane + kW * i;
-        if (k >= LZ) continue;
-        const int z = (int)k + 1;
+        if (!act[i]) continue;
         V<KV> tnew = Tn[i], enew = d0[i], tlnew = tl[i];
-        if (z >= nzmin && z <= nzmax - 1) {
+        {
           const float r = fdv(dt, av[i]);
           const float ra = hn[i] / hnn[i];  // IEEE: exactly 1 for an unchanged layer
           // lo holds LO - T, so LO - T hnode / hnode_new = (LO - T) + T (1 - ra),
