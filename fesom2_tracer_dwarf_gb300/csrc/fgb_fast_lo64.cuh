@@ -64,19 +64,15 @@ __global__ void __launch_bounds__(kLo64Warps * kW, 7) kf_lo64(DMesh m, FastPtrs 
   // arithmetic; its interface fluxes are zero (still written: the bottom
   // interface is read by the update) and its LO increments are never read.
   const bool s1 = nzmax - 2 >= kW;
-  // per slice: layer / interface index, geometry and velocity (tracer
-  // independent). Lanes below the column load nothing (lay: the column's
-  // layers, itf: its interfaces down to the bottom one); the LO increments of
-  // the slice are still stored (zeros below the column: out).
+  // per slice: layer / interface index, geometry and velocity (tracer independent)
   int k[2];
-  bool lay[2], itf[2], out[2];
+  bool lay[2], itf[2];
   float hn[2], hnn[2], av[2], w[2], wl[2], ar[2], zq[2], zbq[2];
 #pragma unroll
   for (int s = 0; s < 2; ++s) {
     k[s] = lane + kW * s;
-    out[s] = k[s] < LZ && (s == 0 || s1);
-    lay[s] = out[s] && k[s] <= nzmax - 2;
-    itf[s] = k[s] < LW && (s == 0 || s1) && k[s] <= nzmax - 1;
+    lay[s] = k[s] < LZ && (s == 0 || s1);
+    itf[s] = k[s] < LW && (s == 0 || s1);
     const unsigned iz = (unsigned)n * LZ + k[s], iw = (unsigned)n * LW + k[s];
     hn[s] = lay[s] ? g.hnode[iz] : 1.f;
     hnn[s] = lay[s] ? g.hnode_new[iz] : 1.f;
@@ -285,7 +281,7 @@ __global__ void __launch_bounds__(kLo64Warps * kW, 7) kf_lo64(DMesh m, FastPtrs 
     float* __restrict__ lo = a.lo + gi * a.gN;
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
-      if (!out[s]) continue;
+      if (!lay[s]) continue;
       const int z = k[s] + 1;
       // the increment LO - T = (fluxes) dt / (areasvol hnode_new) + T (hnode / hnode_new - 1)
       V<KV> l = splat<KV>(0.f);
