@@ -10,7 +10,9 @@ value's FP32 rounding residual carried by the update; the plain FP64 path
 for every tracer plus the tendency update, inputs resident in HBM (they are
 far larger than the 129 MB L2, so no flush is needed). The batching form
 (batch_16: 16 meshes in one union, CUDA graphs of 50 steps, against per-mesh
-sequential FP64 steps) is the line's second figure, under "batch_16".
+sequential FP64 steps) is the line's second figure, under "batch_16"; the
+closed 1024^2 basin (FP32 residual form against fast FP64) and the 512^2 x 48
+FP64 configuration with MUSCL and with upwind fluxes follow under "side".
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME]
   python bench.py --impl reference ...   # the CPU implementation of the path
@@ -46,7 +48,7 @@ WORKLOADS = {
     # conservation target) and the LO fluxes summed with compensation.
     "precision_2048": dict(kind="flat", nx=2049, L=2048e3, nz=64, K=4, hor="MUSCL", ver="PPM", lim="FCT",
                            dt=400.0, precision="fp32", compare_fp64=True, report_steps=100, residual=True,
-                           batch="batch_16"),
+                           batch="batch_16", side=("closed_1024", "fp64_512", "fp64_512_upw1")),
     # The default workload with w_split: w = we + wi, we clipped at a quarter of
     # max |w|; the LO stage adds the implicit vertical solve with wi.
     "wsplit_2048": dict(kind="flat", nx=2049, L=2048e3, nz=64, K=4, hor="MUSCL", ver="PPM", lim="FCT",
@@ -60,6 +62,9 @@ WORKLOADS = {
     # The plain FP64 drop-in: 512^2 x 48 periodic, 2 tracers, MUSCL-FCT + QR4C.
     "fp64_512": dict(kind="flat", nx=513, L=512e3, nz=48, K=2, hor="MUSCL", ver="QR4C", lim="FCT", dt=400.0,
                      precision="fp64", compare_fp64=False),
+    # The same with upwind horizontal fluxes (the other scheme of that configuration).
+    "fp64_512_upw1": dict(kind="flat", nx=513, L=512e3, nz=48, K=2, hor="UPW1", ver="QR4C", lim="FCT", dt=400.0,
+                          precision="fp64", compare_fp64=False),
     # Closed ragged basin: 1024^2 with seeded bathymetry (8..64 layers), walls,
     # MUSCL-FCT + PPM; FP32 form against plain FP64 over 100 steps.
     "closed_1024": dict(kind="closed", nx=1025, L=1024e3, nz=64, min_layers=8, K=2, hor="MUSCL", ver="PPM",
@@ -740,6 +745,40 @@ def sequential_fp64(cfg, n64, device, dist, cells):
             "mode": "per-mesh sequential eager launches", "gpu_launches": l64}
 
 
+def run_side_figure(name, args, device, dist, barrier):
+    """A further configuration's figures on the same run: its own form timed
+    over whole steps after tuning, and for an FP32 workload the fast FP64 form
+    beside it (no precision report, no e2e: the headline carries those)."""
+    import torch
+
+    from fesom2_tracer_dwarf_gb300 import autotune
+
+    cfg = WORKLOADS[name]
+    m, eng, T0 = build_case(cfg, cfg["precision"], device)
+    cells = m.wet_cells() * cfg["K"]
+    tuned = None if args.no_tune else autotune.tune(eng, cfg["dt"], reps=1)
+    steps = max(3, min(args.steps, 10))
+    tot, per, launches = time_engine(eng, T0, cfg["dt"], steps, min(args.warmup, 3), barrier, stage_steps=2)
+    t_max, value = job_rate(tot / steps, cells, dist, device)
+    out = {"workload": name, "config": workload_config(name, cfg, dist.get_world_size() if dist else 1),
+           "form": cfg["precision"], "residual": bool(eng.residual), "value": value, "unit": UNIT,
+           "ms_per_step": t_max, "steps": steps, "tracer_cells_per_step": cells,
+           "stage_ms": {k: round(v, 4) for k, v in per.items()},
+           "launch_cfg": tuned["cfg"] if tuned else "default", "gpu_launches": launches}
+    del eng, m, T0
+    torch.cuda.empty_cache()
+    if cfg["precision"] == "fp32" and not args.no_fp64:
+        m64, e64, T64 = build_case(cfg, "fp64fast", device)
+        n64 = max(2, min(args.steps, args.fp64_steps))
+        tot64, _, _ = time_engine(e64, T64, cfg["dt"], n64, min(args.warmup, 2), barrier, stage_steps=1)
+        out["fp64"] = {"form": "fp64fast", "ms_per_step": tot64 / n64, "value": job_rate(tot64 / n64, cells, dist,
+                                                                                          device)[1]}
+        out["fp32_over_fp64"] = value / out["fp64"]["value"]
+        del e64, m64, T64
+        torch.cuda.empty_cache()
+    return out
+
+
 def run_batch_form(name, args, device, dist, barrier, local):
     """The batching form as a second figure of a run: the union of the
     workload's meshes stepped by CUDA graphs of graph_steps steps (one launch
@@ -887,6 +926,10 @@ def run_gpu(args):
     if cfg.get("batch") and not args.no_batch:
         torch.cuda.empty_cache()
         result[cfg["batch"]] = run_batch_form(cfg["batch"], args, device, dist, barrier, local)
+    if cfg.get("side") and not args.no_side:
+        del eng, T0  # the headline's engine and tracer buffers
+        torch.cuda.empty_cache()
+        result["side"] = {name: run_side_figure(name, args, device, dist, barrier) for name in cfg["side"]}
     if cfg["kind"] == "files":
         lev = m.get("nlevels_nod2D") - 1
         result["mesh_layers"] = {"min": int(lev.min()), "max": int(lev.max()), "mean": float(lev.mean())}
@@ -976,6 +1019,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-report", action="store_true", help="skip the FP32-vs-FP64 precision report")
     ap.add_argument("--no-batch", action="store_true", help="skip the batching form's second figure")
+    ap.add_argument("--no-side", action="store_true", help="skip the further configurations' figures")
     ap.add_argument("--batch-steps", type=int, default=100,
                     help="steps of the batching form's second figure (whole CUDA graphs)")
     ap.add_argument("--no-tune", action="store_true", help="use the default launch configuration")
