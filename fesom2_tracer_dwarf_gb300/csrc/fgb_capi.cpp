@@ -26,6 +26,7 @@
 #include <cuda_runtime.h>
 #include <sys/stat.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>

@@ -4,7 +4,6 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
-#include <functional>
 
 #include "fgb_hmesh.hpp"
 
@@ -148,7 +147,18 @@ struct Reader {
           f.dims[d] = scalar<int32_t>(f.name);
           if (f.dims[d] < 0 && err.empty()) err = f.name + ": negative extent";
         }
-        const size_t n = f.count(), w = f.kind == Kind::ArrI4 ? 4 : 8;
+        // the extents' product, refused once it exceeds what the record can hold
+        const size_t w = f.kind == Kind::ArrI4 ? 4 : 8, cap = b.size() / w + 1;
+        size_t n = 1;
+        for (int32_t d : f.dims) {
+          const size_t e = d > 0 ? (size_t)d : 0;
+          if (e && n > cap / e) {
+            if (err.empty()) err = f.name + ": extents larger than the record";
+            n = 0;
+            break;
+          }
+          n *= e;
+        }
         if (n && need(n * w, f.name)) {
           if (f.kind == Kind::ArrI4) {
             f.vi.resize(n);

@@ -260,6 +260,10 @@ def test_bad_restarts_are_refused(tracer, tmp_path):
     assert bad != payload
     open(p, "wb").write(frame(bad, 1 << 30))
     assert tracer.initialize(str(tmp_path)) == -1 and "Unknown horizontal advection type" in last()
+    # extents whose product exceeds the record (data(1)%values: the two extents after num_tracers)
+    huge = payload[:4] + struct.pack("<ii", 2 ** 30, 2 ** 30) + payload[12:]
+    open(p, "wb").write(frame(huge, 1 << 30))
+    assert tracer.initialize(str(tmp_path)) == -1 and "t_tracer" in last()
     # a missing file
     os.remove(p)
     assert tracer.initialize(str(tmp_path)) == -1 and "t_tracer" in last()
