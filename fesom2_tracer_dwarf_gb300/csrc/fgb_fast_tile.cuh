@@ -31,20 +31,26 @@ __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
 }
 
-// Shared memory: edge records, the edges' node slots, the node ids, the TA
-// rows (+ T rows when T_AB is separate under FCT) of the mesh's largest tile
-// (maxn nodes) and the volume-flux rows of one pass.
+// Shared memory: edge records, the start of each edge's six node rows in the
+// staged rows (16 bits each: slot x kTileChunk; 12 bytes per edge, which keeps
+// seven blocks of the largest tiles on an SM), the node ids, the TA rows
+// (+ T rows when T_AB is separate under FCT) of the mesh's largest tile (maxn
+// nodes) and the volume-flux rows of one pass.
 __host__ __device__ constexpr size_t tile_smem_bytes(int KV, bool tsep, int maxn) {
-  return (size_t)kTileEdges * sizeof(EdgeRec) + (size_t)kTileEdges * 8 + (size_t)kTileNodes * 4 +
+  return (size_t)kTileEdges * sizeof(EdgeRec) + (size_t)kTileEdges * 12 + (size_t)kTileNodes * 4 +
          (size_t)(tsep ? 2 : 1) * maxn * kTileChunk * KV * 4 + (size_t)kTileEdges * kTileChunk * 4;
 }
+static_assert(kTileNodes * kTileChunk < 65536, "row starts are 16-bit");
 
 template <int HOR, bool FCT, int KV>
 __global__ void __launch_bounds__(kTileThreads) kf_hflux_tile(DMesh m, FastPtrs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   EdgeRec* recs = reinterpret_cast<EdgeRec*>(smem_raw);
-  unsigned char* slots = smem_raw + kTileEdges * sizeof(EdgeRec);  // 8 per edge
-  int* nodes = reinterpret_cast<int*>(slots + kTileEdges * 8);
+  // row starts of n1 | n2 and of the upwind triangle's two other vertices (rsA), of
+  // the downwind triangle's two others (rsD)
+  uint2* rsA = reinterpret_cast<uint2*>(smem_raw + kTileEdges * sizeof(EdgeRec));
+  unsigned* rsD = reinterpret_cast<unsigned*>(rsA + kTileEdges);
+  int* nodes = reinterpret_cast<int*>(rsD + kTileEdges);
   const bool ta_sep = a.TA != a.T;
   const bool tsep = FCT && ta_sep;
   V<KV>* rowsA = reinterpret_cast<V<KV>*>(nodes + kTileNodes);  // [node slot][layer of the pass]
@@ -59,7 +65,10 @@ __global__ void __launch_bounds__(kTileThreads) kf_hflux_tile(DMesh m, FastPtrs 
   __syncthreads();
   for (int i = tid; i < ne; i += kTileThreads) {
     fill_edge<HOR>(m, p0 + i, recs[i]);
-    *reinterpret_cast<uint2*>(slots + 8 * i) = *reinterpret_cast<const uint2*>(m.tile_slots + 8 * (size_t)(p0 + i));
+    const uint2 sl = *reinterpret_cast<const uint2*>(m.tile_slots + 8 * (size_t)(p0 + i));
+    auto two = [](unsigned a, unsigned b) { return (a * kTileChunk) | ((b * kTileChunk) << 16); };
+    rsA[i] = make_uint2(two(sl.x & 0xff, (sl.x >> 8) & 0xff), two((sl.x >> 16) & 0xff, sl.x >> 24));
+    rsD[i] = two(sl.y & 0xff, (sl.y >> 8) & 0xff);
     atomicMax(&s_hi, recs[i].hi);
   }
   for (int i = tid; i < nn; i += kTileThreads) nodes[i] = m.tile_nodes[q0 + i];
@@ -83,21 +92,26 @@ __global__ void __launch_bounds__(kTileThreads) kf_hflux_tile(DMesh m, FastPtrs 
       // pass are rows * KV floats from (node * LZ + k0) * KV, a multiple of 16
       // bytes from a 16-byte boundary (LZ, k0 and rows are multiples of 4).
       {
+        // each thread copies the same 16-byte unit u of every (kTileThreads / upr)-th row
         constexpr int upr = kTileChunk * KV / 4;  // 16-byte units per staged node row
+        static_assert(kTileThreads % upr == 0, "whole rows per round");
         const int used = rows * KV / 4;
-        for (int i = tid; i < nn * upr; i += kTileThreads) {
-          const int j = i / upr, u = i % upr;
-          if (u < used) {
+        const int u = tid % upr;
+        if (u < used) {
+          float* dA = reinterpret_cast<float*>(rowsA) + 4 * u;
+          float* dT = reinterpret_cast<float*>(rowsT) + 4 * u;
+          for (int j = tid / upr; j < nn; j += kTileThreads / upr) {
             const size_t off = ((size_t)nodes[j] * LZ + k0) * KV + 4 * u;
-            cp_async16(reinterpret_cast<float*>(rowsA) + (size_t)j * kTileChunk * KV + 4 * u, TAg + off);
-            if (tsep) cp_async16(reinterpret_cast<float*>(rowsT) + (size_t)j * kTileChunk * KV + 4 * u, Tg + off);
+            cp_async16(dA + (size_t)j * kTileChunk * KV, TAg + off);
+            if (tsep) cp_async16(dT + (size_t)j * kTileChunk * KV, Tg + off);
           }
         }
         constexpr int upv = kTileChunk / 4;
-        for (int i = tid; i < ne * upv; i += kTileThreads) {
-          const int j = i / upv, u = i % upv;
-          if (4 * u < rows) cp_async16(rowsV + j * kTileChunk + 4 * u, a.vf + (size_t)recs[j].e * LZ + k0 + 4 * u);
-        }
+        static_assert(kTileThreads % upv == 0, "whole rows per round");
+        const int uv = tid % upv;
+        if (4 * uv < rows)
+          for (int j = tid / upv; j < ne; j += kTileThreads / upv)
+            cp_async16(rowsV + j * kTileChunk + 4 * uv, a.vf + (size_t)recs[j].e * LZ + k0 + 4 * uv);
         cp_async_wait_all();
       }
       __syncthreads();
@@ -108,13 +122,13 @@ __global__ void __launch_bounds__(kTileThreads) kf_hflux_tile(DMesh m, FastPtrs 
         // the edge's record in vector reads (broadcast to the warp)
         const int4* rv = reinterpret_cast<const int4*>(&recs[j]);
         const int4 r0 = rv[0], r1 = rv[1];  // e, n1, n2, hi | gm0, gm1, nb1, nb2
-        const uint2 sl = *reinterpret_cast<const uint2*>(slots + 8 * j);
+        const uint2 rs = rsA[j];
         const int e = r0.x, hi = r0.w;
         const bool act = (int)k < nz && z <= hi;
         const float v = rowsV[j * kTileChunk + lane];
         const float vp = v + fabsf(v), vm = v - fabsf(v);
-        const V<KV> s1 = rowsA[(sl.x & 0xff) * kTileChunk + lane];
-        const V<KV> s2 = rowsA[((sl.x >> 8) & 0xff) * kTileChunk + lane];
+        const V<KV> s1 = rowsA[(rs.x & 0xffff) + lane];
+        const V<KV> s2 = rowsA[(rs.x >> 16) + lane];
         V<KV> h;
         if (HOR == 0) {
           h = muls(fmas(s2, vm, muls(s1, vp)), -0.5f);
@@ -128,10 +142,11 @@ __global__ void __launch_bounds__(kTileThreads) kf_hflux_tile(DMesh m, FastPtrs 
           const V<KV> dT3 = muls(sub(s2, s1), 1.f / 3.f);
           V<KV> p1, p2;
           if (tri_ok) {
-            const V<KV> u1 = rowsA[((sl.x >> 16) & 0xff) * kTileChunk + lane];
-            const V<KV> u2 = rowsA[(sl.x >> 24) * kTileChunk + lane];
-            const V<KV> d1 = rowsA[(sl.y & 0xff) * kTileChunk + lane];
-            const V<KV> d2 = rowsA[((sl.y >> 8) & 0xff) * kTileChunk + lane];
+            const unsigned rd = rsD[j];
+            const V<KV> u1 = rowsA[(rs.y & 0xffff) + lane];
+            const V<KV> u2 = rowsA[(rs.y >> 16) + lane];
+            const V<KV> d1 = rowsA[(rd & 0xffff) + lane];
+            const V<KV> d2 = rowsA[(rd >> 16) + lane];
             p1 = fmas(u2, wu.z, fmas(u1, wu.y, fmas(s1, wu.x, dT3)));
             p2 = fmas(d2, wd.z, fmas(d1, wd.y, fmas(s2, wd.x, dT3)));
           } else if (act) {
@@ -151,8 +166,8 @@ __global__ void __launch_bounds__(kTileThreads) kf_hflux_tile(DMesh m, FastPtrs 
         }
         V<KV> r = h;
         if (FCT) {
-          const V<KV> q1 = tsep ? rowsT[(sl.x & 0xff) * kTileChunk + lane] : s1;
-          const V<KV> q2 = tsep ? rowsT[((sl.x >> 8) & 0xff) * kTileChunk + lane] : s2;
+          const V<KV> q1 = tsep ? rowsT[(rs.x & 0xffff) + lane] : s1;
+          const V<KV> q2 = tsep ? rowsT[(rs.x >> 16) + lane] : s2;
           r = fmas(fmas(q2, vm, muls(q1, vp)), 0.5f, r);
         }
         if (!act) r = splat<KV>(0.f);
