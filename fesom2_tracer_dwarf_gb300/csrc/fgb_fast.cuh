@@ -56,6 +56,45 @@ template <int KV>
 __device__ __forceinline__ void st(float* base, unsigned i, const V<KV>& a) {
   reinterpret_cast<V<KV>*>(base)[i] = a;
 }
+// The limiting factors R+ and R- of one node-layer are adjacent (the pair
+// index i holds R+ at V index 2 i and R- at 2 i + 1): one load or store of
+// 2 x 4 KV bytes. For four tracers that is a 32-byte access (ld/st .v8.f32,
+// sm_100 and later; the workspace is 32-byte aligned), which halves the L1
+// requests of the update kernel's gathers of its neighbours' factors.
+template <int KV>
+__device__ __forceinline__ void ld_pair(const float* __restrict__ base, unsigned i, V<KV>& p, V<KV>& q) {
+  const V<KV>* a = reinterpret_cast<const V<KV>*>(base) + 2 * i;
+  if constexpr (KV == 4) {
+    asm("ld.global.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(p.v[0]), "=f"(p.v[1]), "=f"(p.v[2]), "=f"(p.v[3]), "=f"(q.v[0]), "=f"(q.v[1]), "=f"(q.v[2]),
+          "=f"(q.v[3])
+        : "l"(a));
+  } else if constexpr (KV == 2) {
+    const float4 t = *reinterpret_cast<const float4*>(a);
+    p.v[0] = t.x;
+    p.v[1] = t.y;
+    q.v[0] = t.z;
+    q.v[1] = t.w;
+  } else {
+    const float2 t = *reinterpret_cast<const float2*>(a);
+    p.v[0] = t.x;
+    q.v[0] = t.y;
+  }
+}
+template <int KV>
+__device__ __forceinline__ void st_pair(float* base, unsigned i, const V<KV>& p, const V<KV>& q) {
+  V<KV>* a = reinterpret_cast<V<KV>*>(base) + 2 * i;
+  if constexpr (KV == 4) {
+    asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(a), "f"(p.v[0]), "f"(p.v[1]),
+                 "f"(p.v[2]), "f"(p.v[3]), "f"(q.v[0]), "f"(q.v[1]), "f"(q.v[2]), "f"(q.v[3])
+                 : "memory");
+  } else if constexpr (KV == 2) {
+    *reinterpret_cast<float4*>(a) = make_float4(p.v[0], p.v[1], q.v[0], q.v[1]);
+  } else {
+    *reinterpret_cast<float2*>(a) = make_float2(p.v[0], q.v[0]);
+  }
+}
+
 template <int KV>
 __device__ __forceinline__ V<KV> splat(float s) {
   V<KV> r;
@@ -1127,8 +1166,7 @@ __global__ void __launch_bounds__(128, (NS == 1 ? 10 : 7)) kf_ratio(DMesh m, Fas
             rm.v[t] = fminf(1.f, __fdividef(bmin, mi[i].v[t] * r - 1e-16f));
           }
         }
-        st<KV>(Rg, 2 * (n * LZ + k), rp);
-        st<KV>(Rg, 2 * (n * LZ + k) + 1, rm);
+        st_pair<KV>(Rg, n * LZ + k, rp, rm);
       }
     }
     __syncwarp();
@@ -1310,8 +1348,7 @@ __global__ void __launch_bounds__(128, LEAN ? 8 : 7) kf_ratio64(DMesh m, FastPtr
           rm.v[t] = fminf(1.f, fdv(bmin[i].v[t], mi[i].v[t] * r - 1e-16f));
         }
       }
-      st<KV>(Rg, 2 * (n * LZ + k), rp);
-      st<KV>(Rg, 2 * (n * LZ + k) + 1, rm);
+      st_pair<KV>(Rg, n * LZ + k, rp, rm);
     }
   }
 }
@@ -1411,8 +1448,9 @@ __global__ void __launch_bounds__(128, (NS == 1 ? (COMP || RES ? 8 : 9) : 4)) kf
         const int k = c0 + lane + kW * c;
         const int kr = k < nz ? k : nz - 1, kv = k < nl ? k : nl - 1;
         const bool need = k <= nzmax - 1;  // layers and interfaces of the column (to its bottom)
-        rp[c] = need ? ld<KV>(Rg, 2 * (n * LZ + kr)) : splat<KV>(0.f);
-        rm[c] = need ? ld<KV>(Rg, 2 * (n * LZ + kr) + 1) : splat<KV>(0.f);
+        rp[c] = splat<KV>(0.f);
+        rm[c] = rp[c];
+        if (need) ld_pair<KV>(Rg, n * LZ + kr, rp[c], rm[c]);
         fv[c] = need ? ld<KV>(adfv, n * LW + kv) : splat<KV>(0.f);
       }
 #pragma unroll
@@ -1488,8 +1526,7 @@ __global__ void __launch_bounds__(128, (NS == 1 ? (COMP || RES ? 8 : 9) : 4)) kf
           rmo[i] = f[i];
           if (act[i]) {
             f[i] = ld<KV>(Fg, ed * LZ + kk[i]);
-            rpo[i] = ld<KV>(Rg, 2 * (q.y * LZ + kk[i]));
-            rmo[i] = ld<KV>(Rg, 2 * (q.y * LZ + kk[i]) + 1);
+            ld_pair<KV>(Rg, q.y * LZ + kk[i], rpo[i], rmo[i]);
           }
         }
 #pragma unroll

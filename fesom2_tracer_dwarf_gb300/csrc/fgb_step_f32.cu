@@ -52,6 +52,12 @@ int launch_stages_f32(const DMesh& m, const fgb_step_desc& d, int mask, cudaStre
     *err = "FP32 tracer arrays must be aligned to their group (4 * tracer_vec bytes, strides multiples of tracer_vec)";
     return -1;
   }
+  // the workspace's arrays start at multiples of 256 bytes from its base; the
+  // pairs of limiting factors are read and written 32 bytes at a time
+  if (reinterpret_cast<uintptr_t>(d.workspace) % 32 != 0) {
+    *err = "the FP32 form's workspace must be 32-byte aligned (cudaMalloc gives 256)";
+    return -1;
+  }
   const bool wsplit = d.lim == FGB_LIM_FCT && d.wi;
   if (wsplit) {
     if (m.min_layers < 2) { *err = "w_split needs at least two layers in every column"; return -1; }

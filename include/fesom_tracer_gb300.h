@@ -228,7 +228,7 @@ int fgb_workspace_offsets(const fgb_mesh* m, int precision, int ntracers, long l
  *   TAout  optional, receives the new values (copy-AB time level)
  *   vel    (M,LZ,2) velocity on elements; w, we (N,LW) vertical velocities
  *   del    optional (K,N,LZ) persistent tendency (reference C-ABI semantics)
- *   workspace of fgb_workspace_bytes.
+ *   workspace of fgb_workspace_bytes (32-byte aligned for the FP32 form).
  * Tracer grouping (FP32 form only): with tracer_vec = V in {2, 4} (V divides
  * ntracers) the per-tracer arrays T, TA, TAout and del hold groups of V
  * tracers interleaved per node-layer: tracer t, node n, layer k is element
