@@ -1174,9 +1174,7 @@ __global__ void __launch_bounds__(128, (NS == 1 ? 10 : 7)) kf_ratio(DMesh m, Fas
 }
 
 // Shared memory of one warp of kf_ratio64: bmax, bmin of the lane's two layers.
-__host__ __device__ constexpr size_t ratio64_warp_bytes(int KV) {
-  return (size_t)4 * kW * KV * 4 + kMaxClF * sizeof(int2) + kMaxDegF * sizeof(int);
-}
+__host__ __device__ constexpr size_t ratio64_warp_bytes(int KV) { return (size_t)4 * kW * KV * 4; }
 
 // Columns of at most 64 layers: one warp holds the whole column (lanes own
 // layers l and l + 32), so the vertical bound window (layers k-1, k, k+1) comes
@@ -1186,8 +1184,7 @@ __host__ __device__ constexpr size_t ratio64_warp_bytes(int KV) {
 
 // LEAN: fewer registers (64, one cluster node in flight) for more resident warps.
 // COMP: the +/- sums of the antidiffusive fluxes are compensated sums.
-// Shared memory: ratio64_warp_bytes per warp, where the finished bounds wait,
-// and the node's cluster and incident-edge lists.
+// Shared memory: ratio64_warp_bytes per warp, where the finished bounds wait.
 template <int KV, bool LEAN, bool COMP>
 __global__ void __launch_bounds__(128, LEAN ? 8 : 7) kf_ratio64(DMesh m, FastPtrs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1195,21 +1192,13 @@ __global__ void __launch_bounds__(128, LEAN ? 8 : 7) kf_ratio64(DMesh m, FastPtr
   const int vi = blockIdx.x * (blockDim.x / kW) + threadIdx.x / kW;
   if (vi >= m.N) return;
   const int n = visit_node(m, vi);
-  V<KV>* sB = reinterpret_cast<V<KV>*>(smem_raw + (size_t)(threadIdx.x / kW) * ratio64_warp_bytes(KV));
+  V<KV>* sB = reinterpret_cast<V<KV>*>(smem_raw) + (size_t)(threadIdx.x / kW) * 4 * kW;
   const GeoPtrs<float>& g = m.g32;
   const unsigned LZ = m.LZ, LW = m.LW;
   const int j0 = m.ne_ptr[n], deg = m.ne_ptr[n + 1] - j0;
   const int c0 = m.cl_ptr[n], ncl = m.cl_ptr[n + 1] - c0, minlev = m.cl_minlev[n];
   const int nzmin = m.ulev[n], nzmax = m.nlev[n];
   const float dt = a.dt;
-  // the cluster and incident-edge lists staged in shared memory: no gather
-  // waits on a global index load
-  int2* sCl = reinterpret_cast<int2*>(sB + 4 * kW);
-  int* sNe = reinterpret_cast<int*>(sCl + kMaxClF);
-  const bool cl_st = ncl <= kMaxClF, ne_st = deg <= kMaxDegF;
-  if (cl_st && lane < ncl) sCl[lane] = make_int2(m.cl_node[c0 + lane], m.cl_lev[c0 + lane]);
-  if (ne_st && lane < deg) sNe[lane] = m.ne_code[j0 + lane];
-  __syncwarp();
   // layers 32..63 are gathered only when the column reaches them; otherwise
   // their limiting factors are stored as zeros (neighbours read them)
   const bool s1 = nzmax - 2 >= kW;
@@ -1240,8 +1229,7 @@ __global__ void __launch_bounds__(128, LEAN ? 8 : 7) kf_ratio64(DMesh m, FastPtr
     }
 #pragma unroll(LEAN ? 1 : 2)
     for (int j = 0; j < ncl; ++j) {
-      const int2 cl = cl_st ? sCl[j] : make_int2(m.cl_node[c0 + j], m.cl_lev[c0 + j]);
-      const int c = cl.x, lev = cl.y;
+      const int c = m.cl_node[c0 + j], lev = m.cl_lev[c0 + j];
       V<KV> lv[2], tv[2];
 #pragma unroll
       for (int i = 0; i < 2; ++i) {
@@ -1305,7 +1293,7 @@ __global__ void __launch_bounds__(128, LEAN ? 8 : 7) kf_ratio64(DMesh m, FastPtr
     }
 #pragma unroll 2
     for (int j = 0; j < deg; ++j) {
-      const int code = ne_st ? sNe[j] : m.ne_code[j0 + j];
+      const int code = m.ne_code[j0 + j];
       const unsigned ed = (unsigned)(code >> 1);
       const float sg = (code & 1) ? -1.f : 1.f;
       V<KV> f[2];
