@@ -28,10 +28,11 @@ __device__ __forceinline__ float frcp(float x) { return __fdividef(1.f, x); }
 // Shared memory of one warp (bytes), 16-byte aligned pieces: T (64), T_AB
 // (64, separate T_AB), PPM slopes (64) and edge values (68), LO vertical
 // fluxes (68), PPM layer thicknesses hnode_new and hnode (64 each), QR4C
-// Z_3d_n (64) and zbar_3d_n (68), the incident-edge list.
+// Z_3d_n (64) and zbar_3d_n (68), the low-order update factors ra and rb
+// (64 each), the incident-edge list.
 __host__ __device__ constexpr size_t lo64_warp_bytes(int KV, int ver, bool tasep) {
   return (size_t)KV * 4 * (64 + (tasep ? 64 : 0) + (ver == 3 ? 64 + 68 : 0) + 68) +
-         (ver == 3 ? 2 * 64 * 4 : 0) + (ver == 1 ? (64 + 68) * 4 : 0) + kMaxDegF * sizeof(int2);
+         (ver == 3 ? 2 * 64 * 4 : 0) + (ver == 1 ? (64 + 68) * 4 : 0) + 2 * 64 * 4 + kMaxDegF * sizeof(int2);
 }
 
 template <int VER, int KV, bool TASEP, bool WESEP, bool COMP>
@@ -51,7 +52,9 @@ __global__ void __launch_bounds__(kLo64Warps * kW, 7) kf_lo64(DMesh m, FastPtrs 
   float* sHn = sHnn + (VER == 3 ? 64 : 0);
   float* sZ = sHn + (VER == 3 ? 64 : 0);            // QR4C
   float* sZb = sZ + (VER == 1 ? 64 : 0);
-  int2* sNb = reinterpret_cast<int2*>(sZb + (VER == 1 ? 68 : 0));
+  float* sRa = sZb + (VER == 1 ? 68 : 0);
+  float* sRb = sRa + 64;
+  int2* sNb = reinterpret_cast<int2*>(sRb + 64);
   const GeoPtrs<float>& g = m.g32;
   const int LZ = m.LZ, LW = m.LW, nl = m.nl;
   const int nzmin = m.ulev[n], nzmax = m.nlev[n];  // 1-based, as the reference
@@ -92,12 +95,13 @@ __global__ void __launch_bounds__(kLo64Warps * kW, 7) kf_lo64(DMesh m, FastPtrs 
     }
   }
   // the low-order update factors: ra = hnode / hnode_new (exactly 1 for an
-  // unchanged layer), rb = dt / (areasvol hnode_new)
-  float ra[2], rb[2];
+  // unchanged layer), rb = dt / (areasvol hnode_new); kept in shared memory
+  // until the epilogue, out of the registers the gather needs. Each lane
+  // reads back only its own layers.
 #pragma unroll
   for (int s = 0; s < 2; ++s) {
-    ra[s] = hn[s] == hnn[s] ? 1.f : fdv(hn[s], hnn[s]);
-    rb[s] = fdv(dt, av[s] * hnn[s]);
+    sRa[k[s]] = hn[s] == hnn[s] ? 1.f : fdv(hn[s], hnn[s]);
+    sRb[k[s]] = fdv(dt, av[s] * hnn[s]);
   }
   for (int gi = 0; gi < a.G; ++gi) {
     const float* __restrict__ Tg = a.T + gi * a.gT;
@@ -170,8 +174,9 @@ __global__ void __launch_bounds__(kLo64Warps * kW, 7) kf_lo64(DMesh m, FastPtrs 
       __syncwarp();
     }
     // vertical fluxes at the own interfaces: LO upwind on T with w_e, HO on T_AB
-    // with w, adf_v = HO - LO
-    V<KV> flo[2];
+    // with w, adf_v = HO - LO; the LO fluxes are kept in shared memory only
+    // (held in registers across the gather they pushed the compensated
+    // variant into local-memory spills)
     float* __restrict__ adfv = a.adfv + gi * a.gW;
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
@@ -227,7 +232,7 @@ __global__ void __launch_bounds__(kLo64Warps * kW, 7) kf_lo64(DMesh m, FastPtrs 
             // the upwind layer's parabola: the layer below (W > 0) or above
             const bool up = W > 0.f;
             const int zl = up ? iz : iz - 1;
-            const float h = up ? hn[s] : sHn[zl];
+            const float h = sHn[zl];
             const float x = fminf(fdv(fabsf(W) * dt, h), 1.f);
             const V<KV> aL = up ? tv[s] : sTV[zl], aR = up ? sTV[zl + 1] : tv[s];
             const V<KV> T0 = up ? ta[s] : TAup;
@@ -235,7 +240,6 @@ __global__ void __launch_bounds__(kLo64Warps * kW, 7) kf_lo64(DMesh m, FastPtrs 
           }
         }
       }
-      flo[s] = lo;
       sF[iz] = lo;
       const V<KV> d = sub(ho, lo);
       if (iz < nl) st<KV>(adfv, (unsigned)n * LW + iz, twice ? sub(ho, d) : d);
@@ -286,7 +290,8 @@ __global__ void __launch_bounds__(kLo64Warps * kW, 7) kf_lo64(DMesh m, FastPtrs 
       // the increment LO - T = (fluxes) dt / (areasvol hnode_new) + T (hnode / hnode_new - 1)
       V<KV> l = splat<KV>(0.f);
       if (z >= nzmin && z <= nzmax - 1)
-        l = fmas(add(COMP ? add(acc[s], accc[s]) : acc[s], sub(flo[s], sF[k[s] + 1])), rb[s], muls(t[s], ra[s] - 1.f));
+        l = fmas(add(COMP ? add(acc[s], accc[s]) : acc[s], sub(sF[k[s]], sF[k[s] + 1])), sRb[k[s]],
+                 muls(t[s], sRa[k[s]] - 1.f));
       st<KV>(lo, (unsigned)n * LZ + k[s], l);
     }
   }
