@@ -1182,7 +1182,8 @@ __host__ __device__ constexpr size_t ratio64_warp_bytes(int KV) { return (size_t
 // the edge and cluster lists are read through L1. Fewer resources per warp,
 // more resident warps.
 
-// LEAN: fewer registers (64, one cluster node in flight) for more resident warps.
+// LEAN: fewer registers (64, one cluster node and one incident edge in flight:
+// with two edges in flight it spilled) for more resident warps.
 // COMP: the +/- sums of the antidiffusive fluxes are compensated sums.
 // Shared memory: ratio64_warp_bytes per warp, where the finished bounds wait.
 template <int KV, bool LEAN, bool COMP>
@@ -1291,7 +1292,7 @@ __global__ void __launch_bounds__(128, LEAN ? 8 : 7) kf_ratio64(DMesh m, FastPtr
       plc[i] = splat<KV>(0.f);
       mic[i] = plc[i];
     }
-#pragma unroll 2
+#pragma unroll(LEAN ? 1 : 2)
     for (int j = 0; j < deg; ++j) {
       const int code = m.ne_code[j0 + j];
       const unsigned ed = (unsigned)(code >> 1);
