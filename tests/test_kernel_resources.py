@@ -3,8 +3,9 @@ report (`-Xptxas -v`) for sm_103a; no GPU is needed.
 
 The kernels the 2048x2048x64 residual-form step runs (the whole-column LO
 kernel with compensated sums, the lean whole-column ratio kernel, the update
-with the rounding residual, the tiled edge-flux kernel, the volume fluxes)
-compile without local-memory spills at their launch bounds. A spill keeps a
+with the rounding residual, the tiled edge-flux kernel, the volume fluxes;
+the node kernels also for groups of 2 tracers) compile without local-memory
+spills at their launch bounds. A spill keeps a
 thread's values in local memory, read back through L1 inside the gathers;
 the compensated LO kernel once lost 17 % of its time to one. The register
 counts must also fit the resident blocks the launch bounds ask for.
@@ -31,6 +32,9 @@ EXPECTED = {
     "kf_hflux_tile<1, true, 4>": None,
     "kf_hflux_tile<2, true, 4>": None,
     "kf_vflux": None,
+    "kf_lo64<3, 2, false, false, true>": 7,
+    "kf_ratio64<2, true, false>": 8,
+    "kf_update<2, 1, false, false, true>": 8,
 }
 
 
