@@ -5,10 +5,10 @@ The kernels the 2048x2048x64 residual-form step runs (the whole-column LO
 kernel with compensated sums, the lean whole-column ratio kernel, the update
 with the rounding residual, the tiled edge-flux kernel, the volume fluxes;
 the node kernels also for groups of 2 tracers) compile without local-memory
-spills at their launch bounds. A spill keeps a
-thread's values in local memory, read back through L1 inside the gathers;
-the compensated LO kernel once lost 17 % of its time to one. The register
-counts must also fit the resident blocks the launch bounds ask for.
+spills at their launch bounds. A spill keeps a thread's values in local
+memory, read back through L1 inside the gathers; the compensated LO kernel
+once lost 17 % of its time to one. The register counts must also fit the
+resident blocks the launch bounds ask for.
 """
 import os
 import re
